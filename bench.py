@@ -1,0 +1,362 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 GARM-LS per-timestep pipeline.
+
+Workload: the 3D dam break on a 128^3 MAC grid (unit cube, solid walls, liquid
+{x<0.4, y<0.5, z<0.6} at rest, gravity -9.8, CFL 1.0, frame rate 25, WENO5 x30
+reinitialisation every step, Jacobi-PCG to rel tol 1e-8).  A step is one
+LevelSetLiquid::advance(dt) of the whole scene.  `value` is interior cell-steps
+per second of the plain FP64 form measured with CUDA events over exactly K
+steps; the state (> 1 GB) is larger than L2, so no flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl garm|reference]
+
+Under torchrun each rank advances its own replica of the scene (replicas
+only: the path does not shard), `value` = all ranks' cell-steps / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO / "garm-ls_gb300"))
+sys.path.insert(0, str(REPO))
+
+METRIC = "cell-steps/s mixed vs FP64 on 1 GB300 at φ err≤1e-3·dx; p50/p99 step latency"
+UNIT = "cell-steps/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["garm", "reference"], default="garm")
+    p.add_argument("--n", type=int, default=128, help="interior cells per axis")
+    p.add_argument("--no-mixed", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        cmd = ["nvidia-smi", f"--id={self.index}",
+               "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+               "--format=csv,noheader,nounits", "-lms", "200"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def reduce_max(x: float, world: int) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def measured_peaks() -> dict:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            pass
+    return {}
+
+
+def state_fields():
+    from garm import capi
+    return [capi.FIELD_VELOCITY, capi.FIELD_REF_MAP, capi.FIELD_REF_MAP_GRAD, capi.FIELD_REF_LEVEL_SET,
+            capi.FIELD_REF_LEVEL_SET_GRAD, capi.FIELD_ADV_REGION]
+
+
+def reinit_roofline(sim, torch, stream, n_cells: int, esz: int, iters: int, peaks: dict) -> dict:
+    """Time the WENO5 reinitialisation stage alone with CUDA events on the sim's stream
+    and express its algorithmic bytes per launch against the measured HBM peak."""
+    launches = 3 * iters
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sim.stage("reinit")  # warm
+    reps = 2
+    ev0.record(stream)
+    for _ in range(reps):
+        sim.stage("reinit")
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms_per_launch = ev0.elapsed_time(ev1) / (reps * launches)
+    # per launch: read the input plane, write the output plane; 2 of 3 sub-stages also read φ
+    bytes_per_launch = (2.0 + 2.0 / 3.0) * n_cells * esz
+    achieved = bytes_per_launch / (ms_per_launch * 1e-3) / 1e9
+    peak = peaks.get("hbm_gbs")
+    src = "measured"
+    if not peak:
+        peak, src = 6800.0, "fallback"
+    return {"kernel": "kReinitStage (WENO5 TVD-RK3 sub-stage)", "bound": "hbm", "achieved": round(achieved, 1),
+            "peak": peak, "peak_source": src, "unit": "GB/s", "frac": round(achieved / peak, 4),
+            "traffic": None, "ms_per_launch": round(ms_per_launch, 4), "algorithmic_bytes_per_launch": int(bytes_per_launch)}
+
+
+def run_garm(args) -> None:
+    import numpy as np
+    import torch
+    from garm import capi, scenes
+
+    rank, local, world = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    capi.load()
+    n, K, W = args.n, args.steps, args.warmup
+    scene = scenes.dam_break(3, n)
+    dx = scene.grid.spacing
+    interior = n ** 3
+
+    def make(precision):
+        cfg = capi.default_config(precision=precision)
+        sim = capi.Simulation(scene.grid, cfg, stream=stream.cuda_stream)
+        sim.upload(capi.FIELD_LEVEL_SET, scene.phi.ravel())
+        sim.upload(capi.FIELD_VELOCITY, scene.velocity)
+        sim.initialize()
+        sim.stage("restart")
+        return sim
+
+    sim = make(capi.PRECISION_FP64)
+    gen = scenes.frame_time_steps(sim.max_speed, W + K, 25, 1.0, dx)
+    for _ in range(W):
+        sim.advance(next(gen))
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    l0 = sim.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    step_ms, cg_it, restarts, dts = [], [], 0, []
+    ev0.record(stream)
+    for _ in range(K):
+        dt = next(gen)
+        st = sim.advance(dt)
+        dts.append(dt)
+        step_ms.append(st["ms_total"])
+        cg_it.append(st["cg_iterations"])
+        restarts += st["restarted"]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = sim.launch_count() - l0
+    elapsed_ms = reduce_max(ev0.elapsed_time(ev1), world)
+    barrier(world)
+    value = world * interior * K / (elapsed_ms * 1e-3)
+    peaks = measured_peaks()
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": elapsed_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"3D dam break {n}^3 MAC grid, plain FP64 form (BASELINE config C2)", "n": n,
+                   "interior_cells": interior, "storage_cells": (n + 4) ** 3, "cfl": 1.0, "frame_rate": 25,
+                   "reinit": "WENO5 x30 every step", "pcg_tol": 1e-8, "replicas": world,
+                   "l2": "no flush: device state > 1 GB, larger than L2"},
+        "p50_step_ms": statistics.median(step_ms), "p99_step_ms": float(np.percentile(step_ms, 99)),
+        "cg_iterations_mean": statistics.mean(cg_it), "restarts": restarts,
+        "clocks": clk, "gpu_launches": launches,
+    }
+    if rank == 0:
+        out["roofline"] = reinit_roofline(sim, torch, stream, int(scene.phi.size), 8, 30, peaks)
+
+    # end to end through the C ABI with host buffers: upload the step's input state
+    # from pinned memory, advance, download the state and the level set
+    if not args.no_e2e:
+        fields = state_fields()
+        pinned_in = {f: torch.from_numpy(sim.download(f)).pin_memory().numpy() for f in fields}
+        pinned_out = {f: torch.empty(len(pinned_in[f]), dtype=torch.float64 if f != capi.FIELD_ADV_REGION else torch.uint8).pin_memory().numpy()
+                      for f in fields + [capi.FIELD_LEVEL_SET]}
+        if capi.FIELD_LEVEL_SET not in pinned_in:
+            pass
+        h2d = sum(a.nbytes for a in pinned_in.values())
+        d2h = sum(a.nbytes for a in pinned_out.values())
+        barrier(world)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(K):
+            for f in fields:
+                sim.upload(f, pinned_in[f])
+            sim.advance(next(scenes.frame_time_steps(sim.max_speed, 1, 25, 1.0, dx)))
+            for f, buf in pinned_out.items():
+                sim.download(f, buf)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        e2e_ms = reduce_max(e0.elapsed_time(e1), world)
+        out["e2e"] = {"value": world * interior * K / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                      "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms / K, "host_wall_ms_per_step": 1e3 * wall / K,
+                      "api": "garm_sim_upload x6 (.sav state) + garm_sim_advance + garm_sim_download x7"}
+
+    # mixed precision on the same workload: throughput and φ error against the FP64 form
+    if not args.no_mixed:
+        ref = make(capi.PRECISION_FP64)
+        mix = make(capi.PRECISION_MIXED)
+        dt0 = next(scenes.frame_time_steps(ref.max_speed, 1, 25, 1.0, dx))
+        ref.advance(dt0)
+        mix.advance(dt0)
+        phi_err = float(np.max(np.abs(ref.download(capi.FIELD_LEVEL_SET) - mix.download(capi.FIELD_LEVEL_SET)))) / dx
+        ref.close()
+        g2 = scenes.frame_time_steps(mix.max_speed, W + K, 25, 1.0, dx)
+        for _ in range(W):
+            mix.advance(next(g2))
+        barrier(world)
+        torch.cuda.synchronize()
+        m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        mms = []
+        m0.record(stream)
+        for _ in range(K):
+            mms.append(mix.advance(next(g2))["ms_total"])
+        m1.record(stream)
+        torch.cuda.synchronize()
+        mix_ms = reduce_max(m0.elapsed_time(m1), world)
+        mval = world * interior * K / (mix_ms * 1e-3)
+        out["mixed"] = {"value": mval, "unit": UNIT, "ms_per_step": mix_ms / K, "p50_step_ms": statistics.median(mms),
+                        "p99_step_ms": float(np.percentile(mms, 99)), "phi_err_dx_after_1_step_vs_fp64": phi_err,
+                        "speedup_vs_fp64": mval / value, "dtype": "f32 storage+math, f64 dots/residual/refinement/RM test"}
+        if rank == 0:
+            out["mixed"]["roofline"] = reinit_roofline(mix, torch, stream, int(scene.phi.size), 4, 30, peaks)
+        mix.close()
+
+    # CPU baseline: the oracle (a CPU port of the reference's FP64 path) on this host,
+    # one step of the same 128^3 workload started from the GPU's state
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        o = O.OracleSim(scene.grid, sim.cfg)
+        for f in state_fields() + [capi.FIELD_LEVEL_SET, capi.FIELD_ORI_LEVEL_SET, capi.FIELD_FRACTION]:
+            o.upload(f, sim.download(f))
+        dt = next(scenes.frame_time_steps(o.max_speed, 1, 25, 1.0, dx))
+        t0 = time.perf_counter()
+        o.advance(dt)
+        secs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": interior / secs, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+                               "sample": f"1 oracle advance of the {n}^3 dam break from the GPU state ({secs:.1f} s)"}
+        o.close()
+    sim.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_reference(args) -> None:
+    """The reference's FP64 CPU path (the oracle port; the reference itself needs Eigen
+    and yaml-cpp, absent here) on the same workload, all host threads."""
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
+    from garm import scenes
+    from garm.build import build_oracle
+    build_oracle()
+    from oracle import oracle as O
+    sys.path.insert(0, str(REPO / "tests"))
+    from helpers import host_default_config, load_scene
+
+    n, K, W = args.n, args.steps, args.warmup
+    scene = scenes.dam_break(3, n)
+    dx = scene.grid.spacing
+    o = O.OracleSim(scene.grid, host_default_config())
+    load_scene(o, scene)
+    o.initialize()
+    o.stage("restart")
+    gen = scenes.frame_time_steps(o.max_speed, min(W, 1) + K, 25, 1.0, dx)
+    for _ in range(min(W, 1)):
+        o.advance(next(gen))
+    times = []
+    for _ in range(K):
+        t0 = time.perf_counter()
+        o.advance(next(gen))
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = n ** 3 * K / total
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": 1e3 * total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"3D dam break {n}^3 MAC grid, plain FP64 form (BASELINE config C2)", "n": n},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+                         "sample": f"{K} full oracle steps of the {n}^3 dam break; warm-up capped at 1 step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_garm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,555 @@
+// garm_capi.cu — the C ABI (include/garm.h): state allocation, .sav-layout
+// transfers and the per-step orchestration of LevelSetLiquid<Dim>::advance
+// (Source/Core/LevelSetLiquid.cpp:608-698) and ::initialize (:528-598).
+#include "garm_internal.h"
+
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <new>
+
+using namespace garm;
+
+struct garm_sim {
+	State s;
+};
+
+namespace {
+
+template <typename T>
+__global__ void kDeinterleave(const double *src, int ncomp, int64_t n, T *d0, T *d1, T *d2, T *d3, T *d4, T *d5, T *d6, T *d7, T *d8) {
+	const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	T *d[9] = {d0, d1, d2, d3, d4, d5, d6, d7, d8};
+	for (int c = 0; c < ncomp; c++) d[c][i] = T(src[i * ncomp + c]);
+}
+
+template <typename T>
+__global__ void kInterleave(double *dst, int ncomp, int64_t n, const T *d0, const T *d1, const T *d2, const T *d3, const T *d4, const T *d5, const T *d6,
+                            const T *d7, const T *d8) {
+	const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const T *d[9] = {d0, d1, d2, d3, d4, d5, d6, d7, d8};
+	for (int c = 0; c < ncomp; c++) dst[i * ncomp + c] = double(d[c][i]);
+}
+
+__global__ void kPressureToCells(int64_t N, const int *grid2mat, const double *p, double *out) {
+	const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (i >= N) return;
+	const int r = grid2mat[i];
+	out[i] = r >= 0 ? p[r] : 0.0;
+}
+
+garm_status dalloc(State &s, void **p, size_t bytes) {
+	*p = nullptr;
+	if (bytes == 0) return GARM_OK;
+	if (s.nAllocs >= int(sizeof(s.allocs) / sizeof(s.allocs[0]))) return GARM_OOM;
+	if (cudaMalloc(p, bytes) != cudaSuccess) { cudaGetLastError(); *p = nullptr; return GARM_OOM; }
+	if (cudaMemsetAsync(*p, 0, bytes, s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
+	s.allocs[s.nAllocs++] = *p;
+	s.deviceBytes += bytes;
+	return GARM_OK;
+}
+template <typename P>
+garm_status dalloc(State &s, P **p, size_t bytes) {
+	void *v = nullptr;
+	const garm_status r = dalloc(s, &v, bytes);
+	*p = static_cast<P *>(v);
+	return r;
+}
+
+void freeAll(State &s) {
+	for (int i = 0; i < s.nAllocs; i++) cudaFree(s.allocs[i]);
+	s.nAllocs = 0;
+	for (auto &e : s.ev) if (e) { cudaEventDestroy(e); e = nullptr; }
+	if (s.ownStream && s.stream) { cudaStreamDestroy(s.stream); s.stream = nullptr; }
+}
+
+garm_status allocState(State &s) {
+	const size_t e = s.esz;
+	const int D = s.dim;
+	const size_t N = size_t(s.N);
+	for (int a = 0; a < D; a++) {
+		const size_t F = size_t(s.F[a]);
+		GARM_TRY(dalloc(s, &s.u[a], F * e));
+		GARM_TRY(dalloc(s, &s.uNew[a], F * e));
+		for (int b = 0; b < D; b++) GARM_TRY(dalloc(s, &s.uGrad[a * 3 + b], F * e));
+		GARM_TRY(dalloc(s, &s.fraction[a], F * e));
+		GARM_TRY(dalloc(s, &s.bvel[a], F * e));
+		GARM_TRY(dalloc(s, &s.normal[a], F * e));
+		GARM_TRY(dalloc(s, &s.xi[a], N * e));
+		GARM_TRY(dalloc(s, &s.xiNew[a], N * e));
+		GARM_TRY(dalloc(s, &s.refGrad[a], N * e));
+	}
+	for (int q = 0; q < D * D; q++) { GARM_TRY(dalloc(s, &s.Pi[q], N * e)); GARM_TRY(dalloc(s, &s.PiNew[q], N * e)); }
+	const int nm = D == 3 ? 4 : 1;
+	for (int m = 0; m < nm; m++) {
+		GARM_TRY(dalloc(s, &s.refMixed[m], N * e));
+		for (int c = 0; c < D; c++) GARM_TRY(dalloc(s, &s.xiMixed[m * D + c], N * e));
+	}
+	GARM_TRY(dalloc(s, &s.phi, N * e));
+	GARM_TRY(dalloc(s, &s.tmp, N * e));
+	GARM_TRY(dalloc(s, &s.ori, N * e));
+	GARM_TRY(dalloc(s, &s.ref, N * e));
+	GARM_TRY(dalloc(s, &s.rA, N * e));
+	GARM_TRY(dalloc(s, &s.rB, N * e));
+	GARM_TRY(dalloc(s, &s.cellDist, N * e));
+	GARM_TRY(dalloc(s, &s.nodeDist, size_t(s.NN) * 8));
+	GARM_TRY(dalloc(s, &s.adv, N));
+	GARM_TRY(dalloc(s, &s.vis0, N));
+	GARM_TRY(dalloc(s, &s.vis1, N));
+	GARM_TRY(dalloc(s, &s.fvis0, size_t(s.Ftot)));
+	GARM_TRY(dalloc(s, &s.fvis1, size_t(s.Ftot)));
+	GARM_TRY(dalloc(s, &s.bcList, size_t(s.Ftot) * 8));
+	GARM_TRY(dalloc(s, &s.bcTmp, size_t(s.Ftot) * e));
+	// projection
+	GARM_TRY(dalloc(s, &s.grid2mat, N * 4));
+	GARM_TRY(dalloc(s, &s.mat2grid, N * 4));
+	GARM_TRY(dalloc(s, &s.scanBlock, size_t(gridFor(s.N)) * 4 + 64));
+	GARM_TRY(dalloc(s, &s.nUnknownsDev, 64));
+	GARM_TRY(dalloc(s, &s.nbr, N * 4 * 2 * D));
+	GARM_TRY(dalloc(s, &s.wts, N * 8 * 2 * D));
+	GARM_TRY(dalloc(s, &s.diag, N * 8));
+	GARM_TRY(dalloc(s, &s.invd, N * 8));
+	GARM_TRY(dalloc(s, &s.rhs, N * 8));
+	GARM_TRY(dalloc(s, &s.pres, N * 8));
+	GARM_TRY(dalloc(s, &s.cgR, N * 8));
+	if (!s.mixed) {
+		GARM_TRY(dalloc(s, &s.cgZ, N * 8));
+		GARM_TRY(dalloc(s, &s.cgP0, N * 8));
+		GARM_TRY(dalloc(s, &s.cgP1, N * 8));
+		GARM_TRY(dalloc(s, &s.cgQ, N * 8));
+	} else {
+		GARM_TRY(dalloc(s, &s.wts32, N * 4 * 2 * D));
+		GARM_TRY(dalloc(s, &s.diag32, N * 4));
+		GARM_TRY(dalloc(s, &s.fR, N * 4));
+		GARM_TRY(dalloc(s, &s.fZ, N * 4));
+		GARM_TRY(dalloc(s, &s.fP0, N * 4));
+		GARM_TRY(dalloc(s, &s.fP1, N * 4));
+		GARM_TRY(dalloc(s, &s.fQ, N * 4));
+		GARM_TRY(dalloc(s, &s.fE, N * 4));
+	}
+	s.maxBlocks = s.numSMs * 2;
+	GARM_TRY(dalloc(s, &s.partials, size_t(s.maxBlocks) * 4 * 8));
+	GARM_TRY(dalloc(s, &s.barrier, 64));
+	GARM_TRY(dalloc(s, &s.cgScalars, 64));
+	GARM_TRY(dalloc(s, &s.cgInts, 64));
+	GARM_TRY(dalloc(s, &s.redU64, 64));
+	GARM_TRY(dalloc(s, &s.redI32, 64));
+	// staging: the largest .sav field (Π: D*D doubles per cell)
+	size_t big = N * 8 * size_t(D * D);
+	if (size_t(s.Ftot) * 8 > big) big = size_t(s.Ftot) * 8;
+	if (size_t(s.NN) * 8 > big) big = size_t(s.NN) * 8;
+	s.stageBytes = big;
+	GARM_TRY(dalloc(s, &s.stage, big));
+	return GARM_OK;
+}
+
+// ---- precision/dimension dispatch ----
+#define GARM_DISPATCH(S, FN, ...)                                                   \
+	((S).dim == 2 ? ((S).mixed ? FN<2, float>(__VA_ARGS__) : FN<2, double>(__VA_ARGS__)) \
+	              : ((S).mixed ? FN<3, float>(__VA_ARGS__) : FN<3, double>(__VA_ARGS__)))
+
+bool validField(int f) { return f >= 0 && f < GARM_FIELD_COUNT; }
+
+size_t fieldBytes(const State &s, int field) {
+	const size_t N = size_t(s.N), D = size_t(s.dim);
+	switch (field) {
+	case GARM_FIELD_VELOCITY: case GARM_FIELD_FRACTION: case GARM_FIELD_BOUNDARY_VELOCITY: case GARM_FIELD_BOUNDARY_NORMAL: return size_t(s.Ftot) * 8;
+	case GARM_FIELD_LEVEL_SET: case GARM_FIELD_REF_LEVEL_SET: case GARM_FIELD_ORI_LEVEL_SET: case GARM_FIELD_TMP_LEVEL_SET:
+	case GARM_FIELD_CELL_DIST: case GARM_FIELD_PRESSURE: return N * 8;
+	case GARM_FIELD_REF_MAP: case GARM_FIELD_REF_LEVEL_SET_GRAD: return N * 8 * D;
+	case GARM_FIELD_REF_MAP_GRAD: return N * 8 * D * D;
+	case GARM_FIELD_ADV_REGION: return N;
+	case GARM_FIELD_NODE_DIST: return size_t(s.NN) * 8;
+	default: return 0;
+	}
+}
+
+// Planes backing a field, in .sav component order.
+int fieldPlanes(State &s, int field, void **pl, int64_t *len) {
+	const int D = s.dim;
+	switch (field) {
+	case GARM_FIELD_VELOCITY: for (int a = 0; a < D; a++) { pl[a] = s.u[a]; len[a] = s.F[a]; } return D;
+	case GARM_FIELD_FRACTION: for (int a = 0; a < D; a++) { pl[a] = s.fraction[a]; len[a] = s.F[a]; } return D;
+	case GARM_FIELD_BOUNDARY_VELOCITY: for (int a = 0; a < D; a++) { pl[a] = s.bvel[a]; len[a] = s.F[a]; } return D;
+	case GARM_FIELD_BOUNDARY_NORMAL: for (int a = 0; a < D; a++) { pl[a] = s.normal[a]; len[a] = s.F[a]; } return D;
+	case GARM_FIELD_LEVEL_SET: pl[0] = s.phi; len[0] = s.N; return 1;
+	case GARM_FIELD_REF_LEVEL_SET: pl[0] = s.ref; len[0] = s.N; return 1;
+	case GARM_FIELD_ORI_LEVEL_SET: pl[0] = s.ori; len[0] = s.N; return 1;
+	case GARM_FIELD_TMP_LEVEL_SET: pl[0] = s.tmp; len[0] = s.N; return 1;
+	case GARM_FIELD_CELL_DIST: pl[0] = s.cellDist; len[0] = s.N; return 1;
+	default: return 0;
+	}
+}
+
+template <typename T>
+garm_status toDevicePlanes(State &s, const double *devSrc, void **pl, int np, int64_t n) {
+	T *d[9] = {};
+	for (int c = 0; c < np; c++) d[c] = (T *)pl[c];
+	kDeinterleave<T><<<gridFor(n), kBlock, 0, s.stream>>>(devSrc, np, n, d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8]); s.launches++;
+	GARM_CHECK_LAUNCH();
+	return GARM_OK;
+}
+template <typename T>
+garm_status fromDevicePlanes(State &s, double *devDst, void *const *pl, int np, int64_t n) {
+	const T *d[9] = {};
+	for (int c = 0; c < np; c++) d[c] = (const T *)pl[c];
+	kInterleave<T><<<gridFor(n), kBlock, 0, s.stream>>>(devDst, np, n, d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8]); s.launches++;
+	GARM_CHECK_LAUNCH();
+	return GARM_OK;
+}
+
+garm_status sync(State &s) { return cudaStreamSynchronize(s.stream) == cudaSuccess ? GARM_OK : GARM_CUDA_ERROR; }
+
+garm_status upload(State &s, int field, const void *host, size_t bytes) {
+	if (!validField(field) || !host || bytes != fieldBytes(s, field) || bytes == 0) return GARM_INVALID;
+	if (field == GARM_FIELD_PRESSURE) return GARM_INVALID;
+	if (field == GARM_FIELD_ADV_REGION) {
+		if (cudaMemcpyAsync(s.adv, host, bytes, cudaMemcpyHostToDevice, s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
+		return sync(s);
+	}
+	if (field == GARM_FIELD_NODE_DIST) {
+		if (cudaMemcpyAsync(s.nodeDist, host, bytes, cudaMemcpyHostToDevice, s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
+		return sync(s);
+	}
+	if (cudaMemcpyAsync(s.stage, host, bytes, cudaMemcpyHostToDevice, s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
+	const double *src = (const double *)s.stage;
+	void *pl[9]; int64_t len[9];
+	const int np = fieldPlanes(s, field, pl, len);
+	if (np > 0) {  // concatenated planes (face fields) or one cell plane
+		int64_t off = 0;
+		for (int c = 0; c < np; c++) {
+			void *one[1] = {pl[c]};
+			GARM_TRY(s.mixed ? toDevicePlanes<float>(s, src + off, one, 1, len[c]) : toDevicePlanes<double>(s, src + off, one, 1, len[c]));
+			off += len[c];
+		}
+		return sync(s);
+	}
+	// interleaved per-cell vectors / matrices
+	int nc = 0;
+	if (field == GARM_FIELD_REF_MAP) { for (int c = 0; c < s.dim; c++) pl[c] = s.xi[c]; nc = s.dim; }
+	else if (field == GARM_FIELD_REF_MAP_GRAD) { for (int c = 0; c < s.dim * s.dim; c++) pl[c] = s.Pi[c]; nc = s.dim * s.dim; }
+	else if (field == GARM_FIELD_REF_LEVEL_SET_GRAD) { for (int c = 0; c < s.dim; c++) pl[c] = s.refGrad[c]; nc = s.dim; }
+	else return GARM_INVALID;
+	GARM_TRY(s.mixed ? toDevicePlanes<float>(s, src, pl, nc, s.N) : toDevicePlanes<double>(s, src, pl, nc, s.N));
+	if (field == GARM_FIELD_REF_LEVEL_SET_GRAD) GARM_TRY(GARM_DISPATCH(s, resetRefView, s));  // the view is reset after a load (LevelSetLiquid.cpp:511)
+	return sync(s);
+}
+
+garm_status download(State &s, int field, void *host, size_t bytes) {
+	if (!validField(field) || !host || bytes != fieldBytes(s, field) || bytes == 0) return GARM_INVALID;
+	if (field == GARM_FIELD_ADV_REGION) {
+		if (cudaMemcpyAsync(host, s.adv, bytes, cudaMemcpyDeviceToHost, s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
+		return sync(s);
+	}
+	if (field == GARM_FIELD_NODE_DIST) {
+		if (cudaMemcpyAsync(host, s.nodeDist, bytes, cudaMemcpyDeviceToHost, s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
+		return sync(s);
+	}
+	double *dst = (double *)s.stage;
+	if (field == GARM_FIELD_PRESSURE) {
+		kPressureToCells<<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, s.grid2mat, s.pres, dst); s.launches++;
+		GARM_CHECK_LAUNCH();
+	} else {
+		void *pl[9]; int64_t len[9];
+		const int np = fieldPlanes(s, field, pl, len);
+		if (np > 0) {
+			int64_t off = 0;
+			for (int c = 0; c < np; c++) {
+				void *one[1] = {pl[c]};
+				GARM_TRY(s.mixed ? fromDevicePlanes<float>(s, dst + off, one, 1, len[c]) : fromDevicePlanes<double>(s, dst + off, one, 1, len[c]));
+				off += len[c];
+			}
+		} else {
+			int nc = 0;
+			if (field == GARM_FIELD_REF_MAP) { for (int c = 0; c < s.dim; c++) pl[c] = s.xi[c]; nc = s.dim; }
+			else if (field == GARM_FIELD_REF_MAP_GRAD) { for (int c = 0; c < s.dim * s.dim; c++) pl[c] = s.Pi[c]; nc = s.dim * s.dim; }
+			else if (field == GARM_FIELD_REF_LEVEL_SET_GRAD) { for (int c = 0; c < s.dim; c++) pl[c] = s.refGrad[c]; nc = s.dim; }
+			else return GARM_INVALID;
+			GARM_TRY(s.mixed ? fromDevicePlanes<float>(s, dst, pl, nc, s.N) : fromDevicePlanes<double>(s, dst, pl, nc, s.N));
+		}
+	}
+	if (cudaMemcpyAsync(host, dst, bytes, cudaMemcpyDeviceToHost, s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
+	return sync(s);
+}
+
+// LevelSetLiquid::initialize (LevelSetLiquid.cpp:528-598)
+garm_status initialize(State &s) {
+	GARM_TRY(GARM_DISPATCH(s, finishBoundary, s));                       // _boundary.finish
+	GARM_TRY(GARM_DISPATCH(s, enforceBoundaryLevelSet, s, s.phi, 0.0));  // enforceBoundaryLevelSet(_levelSet)
+	GARM_TRY(GARM_DISPATCH(s, reinitialize, s));                         // reinitializeLevelSet
+	GARM_TRY(GARM_DISPATCH(s, copyField, s, s.tmp, s.phi, s.N));         // _tmpLevelSet = _levelSet
+	GARM_TRY(GARM_DISPATCH(s, copyField, s, s.ref, s.phi, s.N));         // _refLevelSet = _levelSet
+	GARM_TRY(GARM_DISPATCH(s, copyField, s, s.ori, s.phi, s.N));         // _oriLevelSet = _levelSet
+	GARM_TRY(GARM_DISPATCH(s, resetRefView, s));                         // _refLevelSetView.reset()
+	GARM_TRY(GARM_DISPATCH(s, initRefMap, s));                           // ξ = x, advRegion = 1, Π = I
+	garm_step_stats st{};
+	const garm_status pr = GARM_DISPATCH(s, project, s, &st);            // projectVelocity(0)
+	if (pr != GARM_OK && pr != GARM_NOT_CONVERGED) return pr;
+	GARM_TRY(GARM_DISPATCH(s, extrapolateToAir, s));                     // extrapolateFieldsToAir
+	GARM_TRY(GARM_DISPATCH(s, enforceBoundaryConditions, s));            // _boundary.enforce(_velocity)
+	s.stepIndex = 0;
+	GARM_TRY(sync(s));
+	return pr;
+}
+
+garm_status record(State &s, int i) { return cudaEventRecord(s.ev[i], s.stream) == cudaSuccess ? GARM_OK : GARM_CUDA_ERROR; }
+
+// LevelSetLiquid::advance (LevelSetLiquid.cpp:608-698)
+garm_status advance(State &s, double dt, garm_step_stats *st) {
+	garm_step_stats local{};
+	garm_step_stats &S = st ? *st : local;
+	std::memset(&S, 0, sizeof(S));
+	GARM_TRY(record(s, 0));
+	GARM_TRY(GARM_DISPATCH(s, advectFields, s, dt));
+	GARM_TRY(record(s, 1));
+	GARM_TRY(GARM_DISPATCH(s, generateCurrentFields, s));
+	GARM_TRY(record(s, 2));
+	const bool doReinit = s.cfg.reinit_interval <= 1 || (s.stepIndex % s.cfg.reinit_interval) == 0;
+	if (doReinit) GARM_TRY(GARM_DISPATCH(s, reinitialize, s));
+	GARM_TRY(record(s, 3));
+	GARM_TRY(GARM_DISPATCH(s, extrapolateToCollider, s));
+	GARM_TRY(record(s, 4));
+	int keep = 1, tot = 0, bad = 0;
+	GARM_TRY(GARM_DISPATCH(s, checkReferenceMap, s, &keep, &tot, &bad));
+	if (!keep) {
+		GARM_TRY(GARM_DISPATCH(s, restart, s));
+		GARM_TRY(GARM_DISPATCH(s, generateCurrentFields, s));
+		GARM_TRY(GARM_DISPATCH(s, extrapolateToCollider, s));
+	}
+	GARM_TRY(record(s, 5));
+	GARM_TRY(GARM_DISPATCH(s, bodyForce, s, dt));
+	GARM_TRY(record(s, 6));
+	const garm_status pr = GARM_DISPATCH(s, project, s, &S);
+	if (pr != GARM_OK && pr != GARM_NOT_CONVERGED) return pr;
+	GARM_TRY(record(s, 7));
+	GARM_TRY(GARM_DISPATCH(s, extrapolateToAir, s));
+	GARM_TRY(GARM_DISPATCH(s, enforceBoundaryConditions, s));
+	GARM_TRY(record(s, 8));
+	GARM_TRY(sync(s));
+	float ms = 0;
+	for (int i = 0; i < 8; i++) {
+		cudaEventElapsedTime(&ms, s.ev[i], s.ev[i + 1]);
+		S.ms_stage[i] = ms;
+	}
+	cudaEventElapsedTime(&ms, s.ev[0], s.ev[8]);
+	S.ms_total = ms;
+	S.restarted = keep ? 0 : 1;
+	S.rm_total = tot;
+	S.rm_bad = bad;
+	s.stepIndex++;
+	return pr;
+}
+
+}  // namespace
+
+extern "C" {
+
+int garm_abi_version(void) { return GARM_ABI_VERSION; }
+
+const char *garm_status_string(garm_status st) {
+	switch (st) {
+	case GARM_OK: return "ok";
+	case GARM_INVALID: return "invalid argument";
+	case GARM_OOM: return "device out of memory";
+	case GARM_NOT_CONVERGED: return "pressure solve did not converge";
+	case GARM_NUMERIC: return "non-finite value";
+	case GARM_CUDA_ERROR: return "CUDA error";
+	case GARM_TIMEOUT: return "device-side wait timed out";
+	case GARM_UNSUPPORTED: return "unsupported";
+	default: return "unknown status";
+	}
+}
+
+garm_status garm_config_default(garm_config *c) {
+	if (!c) return GARM_INVALID;
+	std::memset(c, 0, sizeof(*c));
+	c->precision = GARM_PRECISION_FP64;
+	c->reinit_iters = 30;
+	c->reinit_cfl = 0.9;
+	c->reinit_interval = 1;
+	c->cg_tolerance = 1e-8;
+	c->cg_max_iters = 2000;
+	c->boundary_extrap_radius = 6.0;
+	c->air_extrap_radius = 15.0;
+	c->rm_threshold = 0.883022221559489;
+	c->rm_band = 4.0;
+	c->rm_ratio = 1e-5;
+	c->enable_gravity = 1;
+	c->mixed_inner_tolerance = 1e-4;
+	c->mixed_max_refinements = 12;
+	return GARM_OK;
+}
+
+garm_status garm_sim_create(const garm_grid_desc *gd, const garm_config *cfg, void *stream, garm_sim **out) {
+	if (!gd || !out) return GARM_INVALID;
+	*out = nullptr;
+	if (gd->dim != 2 && gd->dim != 3) return GARM_INVALID;
+	if (!(gd->spacing > 0) || gd->boundary_width < 0) return GARM_INVALID;
+	for (int a = 0; a < gd->dim; a++)
+		if (gd->resolution[a] < 2 * gd->boundary_width + 1 || gd->resolution[a] > (1 << 14)) return GARM_INVALID;
+	garm_config c;
+	if (cfg) c = *cfg; else garm_config_default(&c);
+	if (c.precision != GARM_PRECISION_FP64 && c.precision != GARM_PRECISION_MIXED) return GARM_INVALID;
+	if (c.reinit_iters < 0 || c.cg_max_iters < 0 || !(c.cg_tolerance > 0)) return GARM_INVALID;
+
+	garm_sim *sim = new (std::nothrow) garm_sim();
+	if (!sim) return GARM_OOM;
+	State &s = sim->s;
+	s.cfg = c;
+	s.dim = gd->dim;
+	s.mixed = c.precision == GARM_PRECISION_MIXED;
+	s.esz = s.mixed ? 4 : 8;
+	s.geom.dim = gd->dim;
+	s.geom.bw = gd->boundary_width;
+	s.geom.dx = gd->spacing;
+	s.geom.inv_dx = 1 / gd->spacing;
+	for (int a = 0; a < 3; a++) {
+		s.geom.n[a] = a < gd->dim ? gd->resolution[a] : 1;
+		// StaggeredGrid origin = center - resolution * spacing / 2 (StaggeredGrid.h:32)
+		s.geom.o[a] = a < gd->dim ? gd->center[a] - double(gd->resolution[a]) * gd->spacing / 2 : 0.0;
+	}
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&s.numSMs, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+		cudaGetLastError();
+		delete sim;
+		return GARM_CUDA_ERROR;
+	}
+	if (stream) s.stream = (cudaStream_t)stream;
+	else {
+		if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess) { delete sim; return GARM_CUDA_ERROR; }
+		s.ownStream = true;
+	}
+	for (auto &e : s.ev)
+		if (cudaEventCreate(&e) != cudaSuccess) { freeAll(s); delete sim; return GARM_CUDA_ERROR; }
+	const int D = s.dim;
+	s.N = int64_t(s.geom.n[0]) * s.geom.n[1] * s.geom.n[2];
+	s.NN = int64_t(s.geom.n[0] + 1) * (s.geom.n[1] + 1) * (D == 3 ? s.geom.n[2] + 1 : 1);
+	s.Ftot = 0;
+	for (int a = 0; a < 3; a++) {
+		if (a < D) {
+			int64_t f = 1;
+			for (int b = 0; b < D; b++) f *= s.geom.n[b] + (b == a ? 1 : 0);
+			s.F[a] = f;
+		} else s.F[a] = 0;
+		s.Ftot += s.F[a];
+	}
+	garm_status r = allocState(s);
+	if (r == GARM_OK) r = GARM_DISPATCH(s, initBoundary, s);           // Boundary ctor → reset()
+	if (r == GARM_OK) {
+		// _levelSet starts at +inf (LevelSetLiquid.cpp:49); the scene is then uploaded
+		const double inf = std::numeric_limits<double>::infinity();
+		double *tmpHost = nullptr;
+		if (cudaMallocHost(&tmpHost, size_t(s.N) * 8) != cudaSuccess) r = GARM_OOM;
+		else {
+			for (int64_t i = 0; i < s.N; i++) tmpHost[i] = inf;
+			r = upload(s, GARM_FIELD_LEVEL_SET, tmpHost, size_t(s.N) * 8);
+			cudaFreeHost(tmpHost);
+		}
+	}
+	if (r == GARM_OK) r = sync(s);
+	if (r != GARM_OK) { freeAll(s); delete sim; return r; }
+	*out = sim;
+	return GARM_OK;
+}
+
+garm_status garm_sim_destroy(garm_sim *sim) {
+	if (!sim) return GARM_INVALID;
+	cudaStreamSynchronize(sim->s.stream);
+	freeAll(sim->s);
+	delete sim;
+	return GARM_OK;
+}
+
+garm_status garm_sim_launch_count(const garm_sim *sim, long long *count) {
+	if (!sim || !count) return GARM_INVALID;
+	*count = sim->s.launches;
+	return GARM_OK;
+}
+
+garm_status garm_sim_device_bytes(const garm_sim *sim, size_t *bytes) {
+	if (!sim || !bytes) return GARM_INVALID;
+	*bytes = sim->s.deviceBytes;
+	return GARM_OK;
+}
+
+garm_status garm_sim_field_bytes(const garm_sim *sim, int field, size_t *bytes) {
+	if (!sim || !bytes || !validField(field)) return GARM_INVALID;
+	*bytes = fieldBytes(sim->s, field);
+	return GARM_OK;
+}
+
+garm_status garm_sim_upload(garm_sim *sim, int field, const void *host, size_t bytes) { return sim ? upload(sim->s, field, host, bytes) : GARM_INVALID; }
+garm_status garm_sim_download(garm_sim *sim, int field, void *host, size_t bytes) { return sim ? download(sim->s, field, host, bytes) : GARM_INVALID; }
+garm_status garm_sim_initialize(garm_sim *sim) { return sim ? initialize(sim->s) : GARM_INVALID; }
+
+garm_status garm_sim_advance(garm_sim *sim, double dt, garm_step_stats *stats) {
+	if (!sim || !std::isfinite(dt) || dt < 0) return GARM_INVALID;
+	return advance(sim->s, dt, stats);
+}
+
+garm_status garm_sim_max_speed(garm_sim *sim, double *out) {
+	if (!sim || !out) return GARM_INVALID;
+	return GARM_DISPATCH(sim->s, maxSpeed, sim->s, out);
+}
+
+garm_status garm_sim_time_step(garm_sim *sim, double cfl, double *dt) {
+	if (!sim || !dt) return GARM_INVALID;
+	double m = 0;
+	GARM_TRY(garm_sim_max_speed(sim, &m));
+	*dt = cfl * sim->s.geom.dx / m;  // +inf when the fluid is at rest, as the reference
+	return GARM_OK;
+}
+
+#define STAGE_BODY(expr) do { if (!sim) return GARM_INVALID; State &s = sim->s; garm_status r_ = (expr); if (r_ == GARM_OK || r_ == GARM_NOT_CONVERGED) { garm_status q_ = sync(s); if (q_ != GARM_OK) return q_; } return r_; } while (0)
+
+garm_status garm_stage_advect(garm_sim *sim, double dt) { STAGE_BODY(GARM_DISPATCH(s, advectFields, s, dt)); }
+garm_status garm_stage_compose(garm_sim *sim) { STAGE_BODY(GARM_DISPATCH(s, generateCurrentFields, s)); }
+garm_status garm_stage_reinit(garm_sim *sim) { STAGE_BODY(GARM_DISPATCH(s, reinitialize, s)); }
+garm_status garm_stage_extrap_collider(garm_sim *sim) { STAGE_BODY(GARM_DISPATCH(s, extrapolateToCollider, s)); }
+garm_status garm_stage_rm_check(garm_sim *sim, int *keep, int *total, int *bad) { STAGE_BODY(GARM_DISPATCH(s, checkReferenceMap, s, keep, total, bad)); }
+garm_status garm_stage_restart(garm_sim *sim) { STAGE_BODY(GARM_DISPATCH(s, restart, s)); }
+garm_status garm_stage_body_force(garm_sim *sim, double dt) { STAGE_BODY(GARM_DISPATCH(s, bodyForce, s, dt)); }
+garm_status garm_stage_project(garm_sim *sim, garm_step_stats *stats) {
+	garm_step_stats local{};
+	garm_step_stats *st = stats ? stats : &local;
+	std::memset(st, 0, sizeof(*st));
+	STAGE_BODY(GARM_DISPATCH(s, project, s, st));
+}
+garm_status garm_stage_extrap_air(garm_sim *sim) { STAGE_BODY(GARM_DISPATCH(s, extrapolateToAir, s)); }
+garm_status garm_stage_enforce_bc(garm_sim *sim) { STAGE_BODY(GARM_DISPATCH(s, enforceBoundaryConditions, s)); }
+garm_status garm_stage_enforce_boundary_level_set(garm_sim *sim, double tol) { STAGE_BODY(GARM_DISPATCH(s, enforceBoundaryLevelSet, s, s.phi, tol)); }
+
+garm_status garm_reinit_host(int dim, const int *size, double spacing, double *phi, int iters, double cfl, int precision) {
+	if ((dim != 2 && dim != 3) || !size || !phi || !(spacing > 0) || iters < 0) return GARM_INVALID;
+	int64_t n = 1;
+	for (int a = 0; a < dim; a++) { if (size[a] <= 0) return GARM_INVALID; n *= size[a]; }
+	const bool f32 = precision == GARM_PRECISION_MIXED;
+	const size_t e = f32 ? 4 : 8;
+	void *buf = nullptr, *stage = nullptr;
+	if (cudaMalloc(&buf, size_t(n) * e * 3) != cudaSuccess) { cudaGetLastError(); return GARM_OOM; }
+	if (cudaMalloc(&stage, size_t(n) * 8) != cudaSuccess) { cudaGetLastError(); cudaFree(buf); return GARM_OOM; }
+	garm_status r = GARM_OK;
+	cudaStream_t st = nullptr;
+	if (cudaMemcpy(stage, phi, size_t(n) * 8, cudaMemcpyHostToDevice) != cudaSuccess) r = GARM_CUDA_ERROR;
+	if (r == GARM_OK) {
+		if (f32) {
+			float *p = (float *)buf;
+			kDeinterleave<float><<<gridFor(n), kBlock>>>((const double *)stage, 1, n, p, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+			r = dim == 2 ? reinitRaw<2, float>(st, size, spacing, p, p + n, p + 2 * n, iters, cfl) : reinitRaw<3, float>(st, size, spacing, p, p + n, p + 2 * n, iters, cfl);
+			if (r == GARM_OK) kInterleave<float><<<gridFor(n), kBlock>>>((double *)stage, 1, n, p, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+		} else {
+			double *p = (double *)buf;
+			cudaMemcpy(p, stage, size_t(n) * 8, cudaMemcpyDeviceToDevice);
+			r = dim == 2 ? reinitRaw<2, double>(st, size, spacing, p, p + n, p + 2 * n, iters, cfl) : reinitRaw<3, double>(st, size, spacing, p, p + n, p + 2 * n, iters, cfl);
+			if (r == GARM_OK) cudaMemcpy(stage, p, size_t(n) * 8, cudaMemcpyDeviceToDevice);
+		}
+	}
+	if (r == GARM_OK && cudaMemcpy(phi, stage, size_t(n) * 8, cudaMemcpyDeviceToHost) != cudaSuccess) r = GARM_CUDA_ERROR;
+	cudaFree(buf);
+	cudaFree(stage);
+	return r;
+}
+
+}  // extern "C"

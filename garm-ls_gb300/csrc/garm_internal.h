@@ -1,0 +1,109 @@
+// garm_internal.h — device state of one simulation and the stage entry points
+// shared by the kernel translation units and the C ABI (garm_capi.cu).
+#pragma once
+
+#include "../../include/garm.h"
+#include "garm_device.cuh"
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace garm {
+
+// Device buffers of one LevelSetLiquid<Dim> (Source/Core/LevelSetLiquid.h:27-121).
+// Field planes are stored in the working type T of the precision mode:
+// double for GARM_PRECISION_FP64, float for GARM_PRECISION_MIXED.
+struct State {
+	Geom geom{};
+	garm_config cfg{};
+	int dim = 3;
+	bool mixed = false;
+	size_t esz = 8;            // bytes per stored field element
+	cudaStream_t stream = nullptr;
+	bool ownStream = false;
+	int numSMs = 0;
+	long long stepIndex = 0;
+	long long launches = 0;    // kernels launched by this simulation (for the bench's gpu_launches)
+
+	int64_t N = 0, NN = 0;     // cells, nodes
+	int64_t F[3] = {0, 0, 0};  // faces per axis
+	int64_t Ftot = 0;
+
+	// velocity (_velocity) and advection ping-pong
+	void *u[3] = {}, *uNew[3] = {};
+	void *uGrad[9] = {};       // [axis*3+b]: d u_axis / d x_b on face grid `axis` (Derivatives::computeFirst<2>)
+	// reference map ξ and Jacobian Π (planes col*D+row)
+	void *xi[3] = {}, *xiNew[3] = {};
+	void *Pi[9] = {}, *PiNew[9] = {};
+	void *xiMixed[12] = {};    // Hermite mixed derivatives of ξ: [m*3+comp]
+	// level sets
+	void *phi = nullptr, *tmp = nullptr, *ori = nullptr, *ref = nullptr;
+	void *refGrad[3] = {};     // ψ0 = ∇φ0 (_refLevelSetGrad)
+	void *refMixed[4] = {};    // cached Hermite mixed derivatives of φ0 (_refLevelSetView)
+	void *rA = nullptr, *rB = nullptr;  // reinitialisation RK stages
+	uint8_t *adv = nullptr;    // _advRegion
+	uint8_t *vis0 = nullptr, *vis1 = nullptr;       // cell extrapolation masks
+	uint8_t *fvis0 = nullptr, *fvis1 = nullptr;     // face extrapolation masks (all axes, concatenated)
+	// boundary (Boundary<Dim>, Source/Core/Boundary.h:16-24)
+	void *cellDist = nullptr, *nodeDist = nullptr;
+	void *fraction[3] = {}, *bvel[3] = {}, *normal[3] = {};
+	int64_t *bcList = nullptr; int64_t nBc = 0;   // faces with fraction > 0.1 (Boundary::enforce work list), concatenated face ids
+	void *bcTmp = nullptr;
+	// projection (Projector<Dim>, Source/Core/Projector.h:14-21)
+	int *grid2mat = nullptr;   // cell -> unknown id or -1
+	int *mat2grid = nullptr;   // unknown id -> cell
+	int *scanBlock = nullptr;  // per-block counts for the compaction scan
+	int *nUnknownsDev = nullptr;
+	int nUnknowns = 0;
+	int *nbr = nullptr;        // [2D][N] neighbour unknown id, -1 if none
+	double *wts = nullptr;     // [2D][N] off-diagonal weights (positive w; matrix entry is -w)
+	double *diag = nullptr, *invd = nullptr, *rhs = nullptr, *pres = nullptr;
+	float *wts32 = nullptr, *diag32 = nullptr;
+	// PCG work vectors (FP64) and the FP32 inner vectors of the mixed form
+	double *cgX = nullptr, *cgR = nullptr, *cgZ = nullptr, *cgP0 = nullptr, *cgP1 = nullptr, *cgQ = nullptr;
+	float *fR = nullptr, *fZ = nullptr, *fP0 = nullptr, *fP1 = nullptr, *fQ = nullptr, *fE = nullptr;
+	double *partials = nullptr; int maxBlocks = 0;
+	unsigned *barrier = nullptr;   // [count, generation]
+	double *cgScalars = nullptr;   // device-side scalars written by the persistent solver
+	int *cgInts = nullptr;
+	// reductions
+	unsigned long long *redU64 = nullptr;
+	int *redI32 = nullptr;
+	// device staging for AoS<->SoA transfers
+	void *stage = nullptr; size_t stageBytes = 0;
+	// every device allocation, freed by garm_sim_destroy
+	void *allocs[160] = {}; int nAllocs = 0; size_t deviceBytes = 0;
+	// timing events
+	cudaEvent_t ev[10] = {};
+};
+
+// Stage entry points (templated on dimension D and working type T).
+template <int D, typename T> garm_status initBoundary(State &s);
+template <int D, typename T> garm_status finishBoundary(State &s);
+template <int D, typename T> garm_status advectFields(State &s, double dt);
+template <int D, typename T> garm_status generateCurrentFields(State &s);
+template <int D, typename T> garm_status reinitialize(State &s);
+template <int D, typename T> garm_status extrapolateToCollider(State &s);
+template <int D, typename T> garm_status checkReferenceMap(State &s, int *keep, int *tot, int *bad);
+template <int D, typename T> garm_status restart(State &s);
+template <int D, typename T> garm_status bodyForce(State &s, double dt);
+template <int D, typename T> garm_status project(State &s, garm_step_stats *st);
+template <int D, typename T> garm_status extrapolateToAir(State &s);
+template <int D, typename T> garm_status enforceBoundaryConditions(State &s);
+template <int D, typename T> garm_status enforceBoundaryLevelSet(State &s, void *field, double tol);
+template <int D, typename T> garm_status resetRefView(State &s);
+template <int D, typename T> garm_status initRefMap(State &s);
+template <int D, typename T> garm_status maxSpeed(State &s, double *out);
+template <int D, typename T> garm_status copyField(State &s, void *dst, const void *src, int64_t n);
+
+// Standalone WENO5 reinitialisation on raw device planes.
+template <int D, typename T> garm_status reinitRaw(cudaStream_t st, const int *size, double dx, T *phi, T *a, T *b, int iters, double cfl);
+
+inline garm_status cudaStatus(cudaError_t e) { return e == cudaSuccess ? GARM_OK : GARM_CUDA_ERROR; }
+#define GARM_CHECK_LAUNCH() do { cudaError_t _e = cudaGetLastError(); if (_e != cudaSuccess) return GARM_CUDA_ERROR; } while (0)
+#define GARM_TRY(x) do { garm_status _s = (x); if (_s != GARM_OK) return _s; } while (0)
+
+inline unsigned gridFor(int64_t n, int block = kBlock) { return unsigned((n + block - 1) / block); }
+
+}  // namespace garm

@@ -1,0 +1,355 @@
+// garm_levelset.cu — level-set stages of LevelSetLiquid::advance:
+//   generateCurrentFields   (Source/Core/LevelSetLiquid.cpp:1218-1244)
+//   reinitializeLevelSet    (LevelSetLiquid.cpp:1148-1160 → Reinitialization.h:20-80, Derivatives.h:134-159)
+//   checkReferenceMap       (LevelSetLiquid.cpp:1246-1283)
+//   restart, plain branch   (LevelSetLiquid.cpp:1320-1352)
+//   enforceBoundaryLevelSet (LevelSetLiquid.cpp:966-975)
+#include "garm_internal.h"
+
+namespace garm {
+
+// ---------------------------------------------------------------------------
+// generateCurrentFields: φ = H(φ0, ψ0)(ξ); air clamp; solid clamps; tmp; ori
+// ---------------------------------------------------------------------------
+template <int D, typename T>
+struct ComposeIO {
+	const T *xi[3];
+	const T *ref;
+	const T *refGrad[3];
+	const T *refMixed[4];
+	const uint8_t *adv;
+	const T *cellDist;
+	T *phi, *tmp, *ori;
+};
+
+// Scalar Hermite value at p (HermiteIntrpl::interpolate, HermiteIntrpl.h:32-41).
+template <int D, typename T>
+__device__ __forceinline__ T hermiteScalar(const G<D, T> &g, const T *p, const T *f, const T *const *grad, const T *const *mixed) {
+	int lo[3] = {0, 0, 0};
+	T B[3][2][2], Dd[3][2][2];
+#pragma unroll
+	for (int a = 0; a < D; a++) {
+		lo[a] = g.lower(a, p[a]);
+		hermiteBasis<T>(g.frac(a, p[a], lo[a]), g.dx, B[a], Dd[a]);
+	}
+	T val = T(0);
+#pragma unroll
+	for (int v = 0; v < (1 << D); v++) {
+		const int vb0 = v & 1, vb1 = (v >> 1) & 1, vb2 = (v >> 2) & 1;
+		const int64_t n = g.cidx(lo[0] + vb0, lo[1] + vb1, D == 3 ? lo[2] + vb2 : 0);
+		if (D == 2) {
+			const T c0 = ldg(f + n), c1 = ldg(grad[0] + n), c2 = ldg(grad[1] + n), c3 = ldg(mixed[0] + n);
+			const T s0 = c0 * B[0][vb0][0] + c1 * B[0][vb0][1];
+			const T s1 = c2 * B[0][vb0][0] + c3 * B[0][vb0][1];
+			val += s0 * B[1][vb1][0] + s1 * B[1][vb1][1];
+		} else {
+			const T c0 = ldg(f + n), c1 = ldg(grad[0] + n), c2 = ldg(grad[1] + n), c3 = ldg(mixed[0] + n);
+			const T c4 = ldg(grad[2] + n), c5 = ldg(mixed[1] + n), c6 = ldg(mixed[2] + n), c7 = ldg(mixed[3] + n);
+			const T bx0 = B[0][vb0][0], bx1 = B[0][vb0][1];
+			const T s00 = c0 * bx0 + c1 * bx1, s10 = c2 * bx0 + c3 * bx1;
+			const T s01 = c4 * bx0 + c5 * bx1, s11 = c6 * bx0 + c7 * bx1;
+			const T sy0 = s00 * B[1][vb1][0] + s10 * B[1][vb1][1];
+			const T sy1 = s01 * B[1][vb1][0] + s11 * B[1][vb1][1];
+			val += sy0 * B[2][vb2][0] + sy1 * B[2][vb2][1];
+		}
+	}
+	return val;
+}
+
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kCompose(Geom geom, ComposeIO<D, T> io, T airClamp, T solidTol) {
+	const G<D, T> g = cellGrid<D, T>(geom);
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= g.count()) return;
+	T p[3] = {io.xi[0][id], io.xi[1][id], D == 3 ? io.xi[2][id] : T(0)};
+	T phi = hermiteScalar<D, T>(g, p, io.ref, io.refGrad, io.refMixed);
+	if (io.adv[id] == 0 && phi < airClamp) phi = airClamp;
+	const T cd = io.cellDist[id];
+	if (phi < -cd - solidTol) phi = -cd - solidTol;  // enforceBoundaryLevelSet(φ, 3dx)
+	T tmp = phi;
+	if (tmp < -cd - T(0)) tmp = -cd - T(0);           // enforceBoundaryLevelSet(tmp, 0)
+	io.phi[id] = phi;
+	io.tmp[id] = tmp;
+	io.ori[id] = phi;
+}
+
+template <int D, typename T>
+garm_status generateCurrentFields(State &s) {
+	ComposeIO<D, T> io{};
+	for (int a = 0; a < D; a++) { io.xi[a] = (const T *)s.xi[a]; io.refGrad[a] = (const T *)s.refGrad[a]; }
+	for (int m = 0; m < 4; m++) io.refMixed[m] = (const T *)s.refMixed[m];
+	io.ref = (const T *)s.ref;
+	io.adv = s.adv;
+	io.cellDist = (const T *)s.cellDist;
+	io.phi = (T *)s.phi; io.tmp = (T *)s.tmp; io.ori = (T *)s.ori;
+	const double airClamp = s.cfg.air_extrap_radius * s.geom.dx;
+	kCompose<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, io, T(airClamp), T(3.0 * s.geom.dx)); s.launches++;
+	GARM_CHECK_LAUNCH();
+	return GARM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// WENO5 reinitialisation (Reinitialization.h:20-80)
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void weno5(const T v[7], T invDx, T &dm, T &dp) {
+#pragma unroll
+	for (int side = 0; side < 2; side++) {
+		T d0, d1, d2, d3, d4;
+		if (side) { d0 = v[6] - v[5]; d1 = v[5] - v[4]; d2 = v[4] - v[3]; d3 = v[3] - v[2]; d4 = v[2] - v[1]; }
+		else { d0 = v[1] - v[0]; d1 = v[2] - v[1]; d2 = v[3] - v[2]; d3 = v[4] - v[3]; d4 = v[5] - v[4]; }
+		T eps = fmax(fmax(fmax(d0 * d0, d1 * d1), fmax(d2 * d2, d3 * d3)), d4 * d4);
+		// 1e-99 in FP64 (Derivatives.h:144); FP32 needs a floor whose square stays normal
+		eps = eps * T(1e-6) + (sizeof(T) == 8 ? T(1e-99) : T(1e-18));
+		const T phix1 = d0 / T(3) - d1 * T(7) / T(6) + d2 * T(11) / T(6);
+		const T phix2 = -d1 / T(6) + d2 * T(5) / T(6) + d3 / T(3);
+		const T phix3 = d2 / T(3) + d3 * T(5) / T(6) - d4 / T(6);
+		const T e1 = d0 - T(2) * d1 + d2, f1 = d0 - T(4) * d1 + T(3) * d2;
+		const T e2 = d1 - T(2) * d2 + d3, f2 = d1 - d3;
+		const T e3 = d2 - T(2) * d3 + d4, f3 = T(3) * d2 - T(4) * d3 + d4;
+		const T s1 = e1 * e1 * T(13) / T(12) + f1 * f1 / T(4);
+		const T s2 = e2 * e2 * T(13) / T(12) + f2 * f2 / T(4);
+		const T s3 = e3 * e3 * T(13) / T(12) + f3 * f3 / T(4);
+		const T q1 = s1 + eps, q2 = s2 + eps, q3 = s3 + eps;
+		const T a1 = T(0.1) / (q1 * q1);
+		const T a2 = T(0.6) / (q2 * q2);
+		const T a3 = T(0.3) / (q3 * q3);
+		const T r = (a1 * phix1 + a2 * phix2 + a3 * phix3) / (a1 + a2 + a3) * invDx;
+		if (side) dp = r; else dm = r;
+	}
+}
+
+// One TVD-RK3 sub-stage: out = lin(base, in + dt*L(in)).
+// mode 0: out = adv;  mode 1: out = (3*base + adv)/4;  mode 2: out = (base + 2*adv)/3.
+template <int D, typename T, int Mode>
+__global__ void __launch_bounds__(kBlock) kReinitStage(G<D, T> g, const T *__restrict__ in, const T *base, T *out, T dt) {
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= g.count()) return;
+	int i, j, k;
+	g.coord(id, i, j, k);
+	const T f = ldg(in + id);
+	T sum = T(0);
+#pragma unroll
+	for (int a = 0; a < D; a++) {
+		T v[7];
+#pragma unroll
+		for (int t = 0; t < 7; t++) {
+			const int o = t - 3;
+			v[t] = ldg(in + g.cidx(i + (a == 0 ? o : 0), j + (a == 1 ? o : 0), k + (a == 2 ? o : 0)));
+		}
+		T dm, dp;
+		weno5<T>(v, g.inv, dm, dp);
+		if (f < T(0)) { const T x = fmin(dm, T(0)), y = fmax(dp, T(0)); sum += x * x; sum += y * y; }
+		else { const T x = fmax(dm, T(0)), y = fmin(dp, T(0)); sum += x * x; sum += y * y; }
+	}
+	sum = sqrt(sum);
+	const T sp = g.dx * sum;
+	const T sgn = f / sqrt(f * f + sp * sp);
+	const T adv = f + dt * sgn * (T(1) - sum);
+	T r;
+	if (Mode == 0) r = adv;
+	else if (Mode == 1) r = (base[id] * T(3) + adv) / T(4);
+	else r = (base[id] + adv * T(2)) / T(3);
+	out[id] = r;
+}
+
+template <int D, typename T>
+static garm_status reinitLoop(cudaStream_t st, const G<D, T> &g, T *phi, T *A, T *B, int iters, double cfl, long long *launches) {
+	const T dt = T(double(g.dx) * cfl);
+	const unsigned nb = gridFor(g.count());
+	for (int it = 0; it < iters; it++) {
+		kReinitStage<D, T, 0><<<nb, kBlock, 0, st>>>(g, phi, nullptr, A, dt);
+		kReinitStage<D, T, 1><<<nb, kBlock, 0, st>>>(g, A, phi, B, dt);
+		kReinitStage<D, T, 2><<<nb, kBlock, 0, st>>>(g, B, phi, phi, dt);
+		if (launches) *launches += 3;
+	}
+	GARM_CHECK_LAUNCH();
+	return GARM_OK;
+}
+
+template <int D, typename T>
+garm_status reinitialize(State &s) {
+	const G<D, T> g = cellGrid<D, T>(s.geom);
+	return reinitLoop<D, T>(s.stream, g, (T *)s.phi, (T *)s.rA, (T *)s.rB, s.cfg.reinit_iters, s.cfg.reinit_cfl, &s.launches);
+}
+
+template <int D, typename T>
+garm_status reinitRaw(cudaStream_t st, const int *size, double dx, T *phi, T *a, T *b, int iters, double cfl) {
+	G<D, T> g;
+	g.s[0] = size[0]; g.s[1] = size[1]; g.s[2] = D == 3 ? size[2] : 1;
+	for (int q = 0; q < 3; q++) g.org[q] = T(0);
+	g.dx = T(dx); g.inv = T(1.0 / dx);
+	return reinitLoop<D, T>(st, g, phi, a, b, iters, cfl, nullptr);
+}
+
+// ---------------------------------------------------------------------------
+// checkReferenceMap — FP64 arithmetic in every precision mode
+// ---------------------------------------------------------------------------
+template <int D, typename T>
+struct PiPtrs { const T *p[9]; };
+
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kCheckRefMap(int64_t N, const T *ori, const T *cellDist, PiPtrs<D, T> pi, double band, double threshold, int *counts) {
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	int tot = 0, bad = 0;
+	if (id < N) {
+		const double o = double(ori[id]);
+		if (fabs(o) < band && double(cellDist[id]) > 0) {
+			tot = 1;
+			double m[D * D];
+#pragma unroll
+			for (int q = 0; q < D * D; q++) m[q] = double(pi.p[q][id]);
+			auto dot = [&](int p, int q) { double s = m[p * D + 0] * m[q * D + 0]; for (int k = 1; k < D; k++) s = fma(m[p * D + k], m[q * D + k], s); return s; };
+			if (D == 2) {
+				const double ab = dot(0, 1);
+				if (ab * ab / dot(0, 0) / dot(1, 1) > threshold) bad = 1;
+			} else {
+				const double aa = dot(0, 0), bb = dot(1, 1), cc = dot(2, 2);
+				const double ab = dot(0, 1), ac = dot(0, 2), bc = dot(1, 2);
+				const double vab = ab * ab / aa / bb, vac = ac * ac / aa / cc, vbc = bc * bc / bb / cc;
+				if (vab > threshold || vac > threshold || vbc > threshold) bad = 1;
+			}
+		}
+	}
+	__shared__ int sh[2][kBlock / 32];
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+	for (int o = 16; o > 0; o >>= 1) { tot += __shfl_down_sync(0xffffffffu, tot, o); bad += __shfl_down_sync(0xffffffffu, bad, o); }
+	if (lane == 0) { sh[0][w] = tot; sh[1][w] = bad; }
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		int t = 0, b = 0;
+		for (int q = 0; q < kBlock / 32; q++) { t += sh[0][q]; b += sh[1][q]; }
+		if (t) atomicAdd(counts, t);
+		if (b) atomicAdd(counts + 1, b);
+	}
+}
+
+template <int D, typename T>
+garm_status checkReferenceMap(State &s, int *keep, int *tot, int *bad) {
+	cudaError_t e = cudaMemsetAsync(s.redI32, 0, 2 * sizeof(int), s.stream);
+	if (e != cudaSuccess) return GARM_CUDA_ERROR;
+	PiPtrs<D, T> pp{};
+	for (int q = 0; q < D * D; q++) pp.p[q] = (const T *)s.Pi[q];
+	kCheckRefMap<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, (const T *)s.ori, (const T *)s.cellDist, pp,
+		s.cfg.rm_band * s.geom.dx, s.cfg.rm_threshold, s.redI32); s.launches++;
+	GARM_CHECK_LAUNCH();
+	int h[2] = {0, 0};
+	e = cudaMemcpyAsync(h, s.redI32, sizeof(h), cudaMemcpyDeviceToHost, s.stream);
+	if (e != cudaSuccess) return GARM_CUDA_ERROR;
+	e = cudaStreamSynchronize(s.stream);
+	if (e != cudaSuccess) return GARM_CUDA_ERROR;
+	if (tot) *tot = h[0];
+	if (bad) *bad = h[1];
+	if (keep) *keep = (1.0 * h[1] <= s.cfg.rm_ratio * h[0]) ? 1 : 0;
+	return GARM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// restart (plain branch): φ0 = φ; ψ0 = 4th-order central ∇φ0; ξ = x; Π = I
+// ---------------------------------------------------------------------------
+template <int D, typename T>
+struct RestartIO {
+	const T *phi;
+	T *ref;
+	T *refGrad[3];
+	T *xi[3];
+	T *Pi[9];
+};
+
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kRestart(Geom geom, RestartIO<D, T> io) {
+	const G<D, T> g = cellGrid<D, T>(geom);
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= g.count()) return;
+	int i, j, k;
+	g.coord(id, i, j, k);
+	const T *f = io.phi;
+	io.ref[id] = f[id];
+	const T h = g.inv / T(12);
+#pragma unroll
+	for (int a = 0; a < D; a++) {
+		const int ex = a == 0, ey = a == 1, ez = a == 2;
+		const T v0 = ldg(f + g.cidx(i - 2 * ex, j - 2 * ey, k - 2 * ez));
+		const T v1 = ldg(f + g.cidx(i - ex, j - ey, k - ez));
+		const T v3 = ldg(f + g.cidx(i + ex, j + ey, k + ez));
+		const T v4 = ldg(f + g.cidx(i + 2 * ex, j + 2 * ey, k + 2 * ez));
+		io.refGrad[a][id] = (v0 - T(8) * v1 + T(8) * v3 - v4) * h;  // Derivatives.h:48
+	}
+	io.xi[0][id] = g.pos(0, i);
+	io.xi[1][id] = g.pos(1, j);
+	if (D == 3) io.xi[2][id] = g.pos(2, k);
+#pragma unroll
+	for (int q = 0; q < D * D; q++) io.Pi[q][id] = (q % (D + 1) == 0) ? T(1) : T(0);
+}
+
+template <int D, typename T>
+garm_status restart(State &s) {
+	RestartIO<D, T> io{};
+	io.phi = (const T *)s.phi;
+	io.ref = (T *)s.ref;
+	for (int a = 0; a < D; a++) { io.refGrad[a] = (T *)s.refGrad[a]; io.xi[a] = (T *)s.xi[a]; }
+	for (int q = 0; q < D * D; q++) io.Pi[q] = (T *)s.Pi[q];
+	kRestart<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, io); s.launches++;
+	GARM_CHECK_LAUNCH();
+	return resetRefView<D, T>(s);
+}
+
+// ξ = x, advRegion = 1, Π = I (LevelSetLiquid.cpp:560-566)
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kInitRefMap(Geom geom, RestartIO<D, T> io, uint8_t *adv) {
+	const G<D, T> g = cellGrid<D, T>(geom);
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= g.count()) return;
+	int i, j, k;
+	g.coord(id, i, j, k);
+	io.xi[0][id] = g.pos(0, i);
+	io.xi[1][id] = g.pos(1, j);
+	if (D == 3) io.xi[2][id] = g.pos(2, k);
+#pragma unroll
+	for (int q = 0; q < D * D; q++) io.Pi[q][id] = (q % (D + 1) == 0) ? T(1) : T(0);
+	adv[id] = 1;
+}
+
+template <int D, typename T>
+garm_status initRefMap(State &s) {
+	RestartIO<D, T> io{};
+	for (int a = 0; a < D; a++) io.xi[a] = (T *)s.xi[a];
+	for (int q = 0; q < D * D; q++) io.Pi[q] = (T *)s.Pi[q];
+	kInitRefMap<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, io, s.adv); s.launches++;
+	GARM_CHECK_LAUNCH();
+	return GARM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// enforceBoundaryLevelSet(sdf, tol): sdf = max(sdf, -cellDist - tol)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kBlock) kEnforceBoundaryLevelSet(int64_t N, T *sdf, const T *cellDist, T tol) {
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= N) return;
+	const T lim = -cellDist[id] - tol;
+	if (sdf[id] < lim) sdf[id] = lim;
+}
+
+template <int D, typename T>
+garm_status enforceBoundaryLevelSet(State &s, void *field, double tol) {
+	kEnforceBoundaryLevelSet<T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, (T *)field, (const T *)s.cellDist, T(tol)); s.launches++;
+	GARM_CHECK_LAUNCH();
+	return GARM_OK;
+}
+
+#define GARM_INST(D, T) \
+	template garm_status generateCurrentFields<D, T>(State &); \
+	template garm_status reinitialize<D, T>(State &); \
+	template garm_status reinitRaw<D, T>(cudaStream_t, const int *, double, T *, T *, T *, int, double); \
+	template garm_status checkReferenceMap<D, T>(State &, int *, int *, int *); \
+	template garm_status restart<D, T>(State &); \
+	template garm_status initRefMap<D, T>(State &); \
+	template garm_status enforceBoundaryLevelSet<D, T>(State &, void *, double);
+GARM_INST(2, double)
+GARM_INST(3, double)
+GARM_INST(2, float)
+GARM_INST(3, float)
+#undef GARM_INST
+
+}  // namespace garm

@@ -1,0 +1,83 @@
+"""Build the GB300 GARM-LS library (and, for tests, the CPU oracle).
+
+`build_library()` compiles garm-ls_gb300/csrc/*.cu for sm_103a with nvcc, one
+translation unit per process, and links garm-ls_gb300/libgarm.so in-tree.
+`build_oracle()` compiles oracle/garm_oracle.cpp with g++ into oracle/liboracle.so;
+the oracle is test infrastructure and is never loaded by the library itself.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG_DIR = Path(__file__).resolve().parents[1]          # garm-ls_gb300/
+REPO = PKG_DIR.parent
+CSRC = PKG_DIR / "csrc"
+BUILD_DIR = PKG_DIR / "_build"
+LIB_PATH = PKG_DIR / "libgarm.so"
+ORACLE_SRC = REPO / "oracle" / "garm_oracle.cpp"
+ORACLE_LIB = REPO / "oracle" / "liboracle.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+              "-Xptxas", "-warn-spills"]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd: list[str]) -> None:
+    res = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("build failed: " + " ".join(cmd) + "\n" + res.stdout)
+
+
+def _stale(target: Path, deps: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def build_library(force: bool = False, verbose: bool = False) -> Path:
+    nvcc = _nvcc()
+    BUILD_DIR.mkdir(exist_ok=True)
+    sources = sorted(CSRC.glob("*.cu"))
+    headers = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [REPO / "include" / "garm.h"]
+    objs = []
+    jobs = []
+    for src in sources:
+        obj = BUILD_DIR / (src.stem + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [src] + headers):
+            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, "-I", str(REPO / "include"), "-c", str(src), "-o", str(obj)])
+    if jobs:
+        workers = min(len(jobs), max(1, os.cpu_count() or 1))
+        with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+            for _ in ex.map(_run, jobs):
+                pass
+    if force or jobs or _stale(LIB_PATH, objs):
+        _run([nvcc, *ARCH, "-shared", "-o", str(LIB_PATH), *map(str, objs), "-lcudart"])
+    if verbose:
+        print(f"built {LIB_PATH}", file=sys.stderr)
+    return LIB_PATH
+
+
+def build_oracle(force: bool = False) -> Path:
+    if force or _stale(ORACLE_LIB, [ORACLE_SRC, REPO / "include" / "garm.h"]):
+        _run(["g++", "-std=c++20", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+              "-o", str(ORACLE_LIB), str(ORACLE_SRC)])
+    return ORACLE_LIB
+
+
+if __name__ == "__main__":
+    build_library(force="--force" in sys.argv, verbose=True)
+    build_oracle(force="--force" in sys.argv)

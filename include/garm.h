@@ -1,0 +1,170 @@
+/*
+ * garm.h — C ABI of the GB300 per-timestep GARM-LS grid pipeline.
+ *
+ * One opaque simulation handle owns the device state of one liquid scene on one
+ * GPU.  Every call returns a garm_status; nothing exits the process.  Host
+ * buffers passed to upload/download use the byte layout of the reference's
+ * frame files (`*.sav`): raw native-endian arrays written by
+ * GridBasedData::save (Source/Core/GridBasedData.h:102-103, Common/Util/IO.h:20-26),
+ * x-fastest cell order (Source/Core/Grid.h:40-44), vector fields interleaved
+ * per cell, matrices column-major per cell (Common/Util/Types.h:52-54), and the
+ * D face arrays of a staggered field in axis order (Source/Core/SGridBasedData.h:54-55).
+ *
+ * The entry points replace the stage methods of
+ * LevelSetLiquid<Dim> (Source/Core/LevelSetLiquid.h:125-169); the host C++
+ * class in garm-ls_gb300/host/GpuLevelSetLiquid.h wraps them behind the
+ * reference's Simulation interface (Common/Util/Simulation.h:10-34).
+ */
+#ifndef GARM_H
+#define GARM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GARM_ABI_VERSION 1
+
+typedef enum garm_status {
+    GARM_OK = 0,
+    GARM_INVALID = 1,        /* bad argument, size or field id */
+    GARM_OOM = 2,            /* device allocation failed */
+    GARM_NOT_CONVERGED = 3,  /* pressure PCG hit its iteration cap (reference: LinearSystem.h:33-36 exits) */
+    GARM_NUMERIC = 4,        /* NaN/Inf found in an input or in the state */
+    GARM_CUDA_ERROR = 5,     /* a CUDA runtime call failed */
+    GARM_TIMEOUT = 6,        /* a bounded device-side wait gave up (grid barrier) */
+    GARM_UNSUPPORTED = 7     /* feature not built into this library */
+} garm_status;
+
+typedef enum garm_precision {
+    GARM_PRECISION_FP64 = 0,  /* plain form: every stage in FP64, as the reference */
+    GARM_PRECISION_MIXED = 1  /* FP32 storage+math for advection/Hermite/WENO/matvec; FP64 dots,
+                                 residuals, iterative refinement and the reference-map test */
+} garm_precision;
+
+/* Field ids for upload/download.  Byte sizes follow the reference's .sav layout. */
+typedef enum garm_field {
+    GARM_FIELD_VELOCITY = 0,            /* D face arrays of double (LevelSetLiquid::_velocity)           */
+    GARM_FIELD_LEVEL_SET = 1,           /* cell double   (_levelSet)                                     */
+    GARM_FIELD_REF_MAP = 2,             /* cell double[D] (_refMap, refMap.sav)                          */
+    GARM_FIELD_REF_MAP_GRAD = 3,        /* cell double[D*D] column-major (_refMapGrad, refMapGrad.sav)   */
+    GARM_FIELD_REF_LEVEL_SET = 4,       /* cell double   (_refLevelSet, refLevelSet.sav)                 */
+    GARM_FIELD_REF_LEVEL_SET_GRAD = 5,  /* cell double[D] (_refLevelSetGrad)                             */
+    GARM_FIELD_ADV_REGION = 6,          /* cell uint8    (_advRegion, advRegion.sav)                     */
+    GARM_FIELD_ORI_LEVEL_SET = 7,       /* cell double   (_oriLevelSet)                                  */
+    GARM_FIELD_TMP_LEVEL_SET = 8,       /* cell double   (_tmpLevelSet)                                  */
+    GARM_FIELD_CELL_DIST = 9,           /* cell double   (Boundary::cellDist)                            */
+    GARM_FIELD_NODE_DIST = 10,          /* node double   (Boundary::nodeDist)                            */
+    GARM_FIELD_FRACTION = 11,           /* D face arrays (Boundary::fraction)                            */
+    GARM_FIELD_BOUNDARY_VELOCITY = 12,  /* D face arrays (Boundary::velocity)                            */
+    GARM_FIELD_BOUNDARY_NORMAL = 13,    /* D face arrays (Boundary::normal)                              */
+    GARM_FIELD_PRESSURE = 14,           /* cell double: last solved pressure, 0 off the unknown set      */
+    GARM_FIELD_COUNT = 15
+} garm_field;
+
+/* StaggeredGrid(boundaryWidth, spacing, resolution, center)
+ * (Source/Core/StaggeredGrid.h:27-36).  resolution counts cells including the
+ * solid ring; unused components of 2D grids are ignored. */
+typedef struct garm_grid_desc {
+    int dim;                 /* 2 or 3 */
+    int resolution[3];
+    int boundary_width;      /* 2 in every reference scene */
+    double spacing;          /* dx */
+    double center[3];
+} garm_grid_desc;
+
+/* Runtime knobs.  Defaults (garm_config_default) equal the reference constants. */
+typedef struct garm_config {
+    int precision;                    /* garm_precision */
+    int reinit_iters;                 /* 30   (LevelSetLiquid.cpp:1156) */
+    double reinit_cfl;                /* 0.9  (LevelSetLiquid.cpp:1156) */
+    int reinit_interval;              /* 1: reinitialise every step (LevelSetLiquid.cpp:625) */
+    double cg_tolerance;              /* 1e-8 relative residual (Jacobi-PCG; the reference's Eigen IC-PCG uses 1e-5) */
+    int cg_max_iters;                 /* 2000 (Projector.cpp:161) */
+    double boundary_extrap_radius;    /* 6    (LevelSetLiquid.h:92)  */
+    double air_extrap_radius;         /* 15   (LevelSetLiquid.h:93)  */
+    double rm_threshold;              /* 0.883022221559489 (LevelSetLiquid.cpp:631) */
+    double rm_band;                   /* 4   */
+    double rm_ratio;                  /* 1e-5 */
+    int enable_gravity;               /* 1   (LevelSetLiquid.h:72) */
+    double mixed_inner_tolerance;     /* inner FP32 PCG tolerance of one refinement sweep (mixed only) */
+    int mixed_max_refinements;        /* outer FP64 iterative-refinement sweeps (mixed only) */
+} garm_config;
+
+/* Per-step statistics returned by garm_sim_advance. */
+typedef struct garm_step_stats {
+    int restarted;            /* 1 when checkReferenceMap failed and restart() ran */
+    int cg_iterations;        /* total PCG iterations (inner iterations summed in mixed mode) */
+    int cg_refinements;       /* outer refinement sweeps (mixed); 1 in FP64 */
+    int unknowns;             /* pressure unknowns of this step */
+    double cg_residual;       /* final relative residual |b-Ax|/|b| */
+    int rm_total;             /* band cells inspected by checkReferenceMap */
+    int rm_bad;               /* band cells whose Jacobian columns are near-parallel */
+    double ms_total;          /* device time of the step (CUDA events) */
+    double ms_stage[8];       /* advect, compose, reinit, extrap_collider, rm_check+restart,
+                                 body_force, project, extrap_air+enforce_bc */
+} garm_step_stats;
+
+typedef struct garm_sim garm_sim;
+
+/* Library identity. */
+int garm_abi_version(void);
+const char *garm_status_string(garm_status s);
+garm_status garm_config_default(garm_config *cfg);
+
+/* Lifetime.  `stream` is a cudaStream_t (NULL: the library creates its own).
+ * Replaces LevelSetLiquid<Dim>::LevelSetLiquid(const StaggeredGrid<Dim>&)
+ * (Source/Core/LevelSetLiquid.cpp:46-77) plus Boundary::Boundary/reset
+ * (Source/Core/Boundary.cpp:8-35) for the domain box walls. */
+garm_status garm_sim_create(const garm_grid_desc *grid, const garm_config *cfg, void *stream, garm_sim **out);
+garm_status garm_sim_destroy(garm_sim *sim);
+garm_status garm_sim_device_bytes(const garm_sim *sim, size_t *bytes);
+/* Kernels launched by this simulation since creation (no reference counterpart: instrumentation). */
+garm_status garm_sim_launch_count(const garm_sim *sim, long long *count);
+
+/* Host <-> device transfer in the .sav layout.  Replaces GridBasedData::save/load
+ * (Source/Core/GridBasedData.h:102-103) as used by LevelSetLiquid::saveFrame/
+ * loadFrame (Source/Core/LevelSetLiquid.cpp:425-526). */
+garm_status garm_sim_field_bytes(const garm_sim *sim, int field, size_t *bytes);
+garm_status garm_sim_upload(garm_sim *sim, int field, const void *host, size_t bytes);
+garm_status garm_sim_download(garm_sim *sim, int field, void *host, size_t bytes);
+
+/* LevelSetLiquid::initialize (Source/Core/LevelSetLiquid.cpp:528-598), RM+GA,
+ * Newton/FMM off.  Expects the velocity and level set uploaded first. */
+garm_status garm_sim_initialize(garm_sim *sim);
+
+/* LevelSetLiquid::advance (Source/Core/LevelSetLiquid.cpp:608-698). `stats` may be NULL. */
+garm_status garm_sim_advance(garm_sim *sim, double dt, garm_step_stats *stats);
+
+/* max over faces of |u| (GridBasedData::normMax, Source/Core/GridBasedData.h:55-68). */
+garm_status garm_sim_max_speed(garm_sim *sim, double *out);
+/* LevelSetLiquid::getTimeStep (Source/Core/LevelSetLiquid.h:129): cfl*dx/max|u| (may be +inf). */
+garm_status garm_sim_time_step(garm_sim *sim, double cfl, double *dt);
+
+/* Single stages, for parity checks and for callers that drive the pipeline
+ * themselves.  Each mirrors one protected method of LevelSetLiquid<Dim>. */
+garm_status garm_stage_advect(garm_sim *sim, double dt);           /* advectFields       LevelSetLiquid.cpp:718-832  */
+garm_status garm_stage_compose(garm_sim *sim);                     /* generateCurrentFields        :1218-1244       */
+garm_status garm_stage_reinit(garm_sim *sim);                      /* reinitializeLevelSet         :1148-1160       */
+garm_status garm_stage_extrap_collider(garm_sim *sim);             /* extrapolateFieldsToCollider  :1086-1137       */
+garm_status garm_stage_rm_check(garm_sim *sim, int *keep, int *total, int *bad); /* checkReferenceMap :1246-1283 */
+garm_status garm_stage_restart(garm_sim *sim);                     /* restart (plain branch)       :1285-1352       */
+garm_status garm_stage_body_force(garm_sim *sim, double dt);       /* applyBodyForces              :834-877         */
+garm_status garm_stage_project(garm_sim *sim, garm_step_stats *stats); /* projectVelocity         :1019-1023       */
+garm_status garm_stage_extrap_air(garm_sim *sim);                  /* extrapolateFieldsToAir       :1059-1084       */
+garm_status garm_stage_enforce_bc(garm_sim *sim);                  /* enforceBoundaryConditions    :1139-1146       */
+garm_status garm_stage_enforce_boundary_level_set(garm_sim *sim, double tolerance); /* enforceBoundaryLevelSet :966-975 */
+
+/* Standalone WENO5 reinitialisation of one cell field held on the host
+ * (Reinitialization::solve<5>, Source/Core/Reinitialization.h:50-80), as the
+ * reference's TestReinit program calls it (Source/Test/TestReinit/TestReinit.cpp:225-236).
+ * `size` has `dim` entries; `phi` is updated in place. */
+garm_status garm_reinit_host(int dim, const int *size, double spacing, double *phi, int iters, double cfl, int precision);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GARM_H */

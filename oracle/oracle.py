@@ -1,0 +1,168 @@
+"""ctypes binding of the CPU oracle (oracle/garm_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the CPU
+baseline legs of bench.py as the checker — never by the library.  The oracle is
+a restatement of the reference's FP64 algorithm; see the header of
+garm_oracle.cpp for what it is pinned against.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(REPO / "garm-ls_gb300"))
+from garm.capi import (Config, GridDesc, StepStats, FIELD_ADV_REGION, FIELD_NAMES, OK, NOT_CONVERGED,  # noqa: E402
+                       field_shapes)
+
+LIB_PATH = REPO / "oracle" / "liboracle.so"
+
+STAGES = {"advect": 0, "compose": 1, "reinit": 2, "extrap_collider": 3, "rm_check": 4, "restart": 5,
+          "body_force": 6, "project": 7, "extrap_air": 8, "enforce_bc": 9, "enforce_boundary_level_set": 10}
+
+_LIB = None
+
+
+def load() -> C.CDLL:
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not LIB_PATH.exists():
+        from garm.build import build_oracle
+        build_oracle()
+    lib = C.CDLL(str(LIB_PATH))
+    lib.orc_create.restype = C.c_void_p
+    lib.orc_create.argtypes = [C.POINTER(GridDesc), C.POINTER(Config)]
+    lib.orc_destroy.argtypes = [C.c_void_p]
+    lib.orc_field_bytes.restype = C.c_size_t
+    lib.orc_field_bytes.argtypes = [C.c_void_p, C.c_int]
+    lib.orc_upload.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]
+    lib.orc_download.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]
+    lib.orc_initialize.argtypes = [C.c_void_p]
+    lib.orc_restart.argtypes = [C.c_void_p]
+    lib.orc_advance.argtypes = [C.c_void_p, C.c_double, C.POINTER(StepStats)]
+    lib.orc_stage.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(StepStats), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.orc_max_speed.restype = C.c_double
+    lib.orc_max_speed.argtypes = [C.c_void_p]
+    lib.orc_set_threads.argtypes = [C.c_int]
+    lib.orc_max_threads.restype = C.c_int
+    lib.orc_reinit.argtypes = [C.c_int, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int, C.c_double]
+    lib.orc_hermite_eval.argtypes = [C.c_int, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.orc_cubic_eval.argtypes = [C.c_int, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
+                                   C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    _LIB = lib
+    return lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class OracleSim:
+    """CPU FP64 LevelSetLiquid<Dim> with the same field/stage vocabulary as garm.capi.Simulation."""
+
+    def __init__(self, grid: GridDesc, cfg: Config):
+        self.lib = load()
+        self.grid = grid
+        self.cfg = cfg
+        self.h = self.lib.orc_create(C.byref(grid), C.byref(cfg))
+        if not self.h:
+            raise ValueError("orc_create failed")
+        self.shapes = field_shapes(grid)
+
+    def close(self):
+        if self.h:
+            self.lib.orc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, field: int, data: np.ndarray) -> None:
+        dtype = np.uint8 if field == FIELD_ADV_REGION else np.float64
+        a = np.ascontiguousarray(data, dtype=dtype)
+        if self.lib.orc_upload(self.h, field, a.ctypes.data, a.nbytes) != OK:
+            raise ValueError(f"orc_upload {FIELD_NAMES[field]}")
+
+    def download(self, field: int) -> np.ndarray:
+        n = self.lib.orc_field_bytes(self.h, field)
+        dtype = np.uint8 if field == FIELD_ADV_REGION else np.float64
+        out = np.empty(n // np.dtype(dtype).itemsize, dtype=dtype)
+        if self.lib.orc_download(self.h, field, out.ctypes.data, out.nbytes) != OK:
+            raise ValueError(f"orc_download {FIELD_NAMES[field]}")
+        return out
+
+    def initialize(self) -> int:
+        return self.lib.orc_initialize(self.h)
+
+    def advance(self, dt: float) -> dict:
+        st = StepStats()
+        rc = self.lib.orc_advance(self.h, float(dt), C.byref(st))
+        d = st.as_dict()
+        d["status"] = rc
+        return d
+
+    def max_speed(self) -> float:
+        return self.lib.orc_max_speed(self.h)
+
+    def stage(self, name: str, arg: float = 0.0):
+        st = StepStats()
+        keep, tot, bad = C.c_int(), C.c_int(), C.c_int()
+        rc = self.lib.orc_stage(self.h, STAGES[name], float(arg), C.byref(st), C.byref(keep), C.byref(tot), C.byref(bad))
+        if rc not in (OK, NOT_CONVERGED):
+            raise ValueError(f"orc_stage {name}: {rc}")
+        if name == "rm_check":
+            return keep.value, tot.value, bad.value
+        if name == "project":
+            d = st.as_dict()
+            d["status"] = rc
+            return d
+        return None
+
+
+def set_threads(n: int) -> None:
+    load().orc_set_threads(int(n))
+
+
+def max_threads() -> int:
+    return load().orc_max_threads()
+
+
+def reinit(phi: np.ndarray, spacing: float, iters: int, cfl: float) -> np.ndarray:
+    a = np.ascontiguousarray(phi, dtype=np.float64).copy()
+    size = (C.c_int * 3)(*([int(x) for x in reversed(a.shape)] + [1] * (3 - a.ndim)))
+    if load().orc_reinit(a.ndim, size, float(spacing), _dp(a), int(iters), float(cfl)) != OK:
+        raise ValueError("orc_reinit")
+    return a
+
+
+def hermite_eval(val: np.ndarray, grad: np.ndarray, spacing: float, origin, pts: np.ndarray):
+    """Scalar Hermite interpolation; grad has a trailing axis of size dim."""
+    dim = val.ndim
+    v = np.ascontiguousarray(val, dtype=np.float64)
+    g = np.ascontiguousarray(grad, dtype=np.float64)
+    size = (C.c_int * 3)(*([int(x) for x in reversed(v.shape)] + [1] * (3 - dim)))
+    o = np.ascontiguousarray(origin, dtype=np.float64)
+    p = np.ascontiguousarray(pts, dtype=np.float64)
+    ov = np.empty(len(p))
+    og = np.empty((len(p), dim))
+    load().orc_hermite_eval(dim, size, float(spacing), _dp(o), _dp(v), _dp(g), len(p), _dp(p), _dp(ov), _dp(og))
+    return ov, og
+
+
+def cubic_eval(val: np.ndarray, spacing: float, origin, pts: np.ndarray) -> np.ndarray:
+    dim = val.ndim
+    v = np.ascontiguousarray(val, dtype=np.float64)
+    size = (C.c_int * 3)(*([int(x) for x in reversed(v.shape)] + [1] * (3 - dim)))
+    o = np.ascontiguousarray(origin, dtype=np.float64)
+    p = np.ascontiguousarray(pts, dtype=np.float64)
+    out = np.empty(len(p))
+    load().orc_cubic_eval(dim, size, float(spacing), _dp(o), _dp(v), len(p), _dp(p), _dp(out))
+    return out

@@ -1,0 +1,76 @@
+"""The C ABI library loads and exports every entry point declared in include/garm.h,
+and its struct layouts and defaults agree with the host-side restatements
+(no GPU call is made)."""
+from __future__ import annotations
+
+import ctypes as C
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from garm import capi
+from helpers import host_default_config
+
+REPO = Path(__file__).resolve().parents[1]
+HEADER = REPO / "include" / "garm.h"
+
+
+def declared_functions() -> list[str]:
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(garm_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(garm_lib):
+    names = declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(garm_lib, n)]
+    assert not missing, missing
+    # and the Python binding declares a signature for each of them
+    assert set(names) <= set(capi._SIGS), set(names) - set(capi._SIGS)
+
+
+def test_nm_lists_symbols_as_extern_c(garm_lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(capi.LIB_PATH)], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (garm_\w+)", out))
+    assert set(declared_functions()) <= exported
+
+
+def test_struct_layout_matches_header(tmp_path):
+    probe = tmp_path / "probe.c"
+    probe.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "garm.h"\n'
+                     'int main(void){printf("%zu %zu %zu %zu %zu\\n", sizeof(garm_grid_desc), sizeof(garm_config),'
+                     ' sizeof(garm_step_stats), offsetof(garm_config, mixed_max_refinements), offsetof(garm_step_stats, ms_stage));return 0;}\n')
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-I", str(REPO / "include"), str(probe), "-o", str(exe)], check=True)
+    vals = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert vals == [C.sizeof(capi.GridDesc), C.sizeof(capi.Config), C.sizeof(capi.StepStats),
+                    capi.Config.mixed_max_refinements.offset, capi.StepStats.ms_stage.offset]
+
+
+def test_config_defaults_equal_reference_constants(garm_lib):
+    lib_cfg = capi.default_config()
+    host = host_default_config()
+    for name, _ in capi.Config._fields_:
+        assert getattr(lib_cfg, name) == getattr(host, name), name
+    assert lib_cfg.rm_threshold == 0.883022221559489  # LevelSetLiquid.cpp:631
+    assert lib_cfg.reinit_iters == 30 and lib_cfg.reinit_cfl == 0.9  # LevelSetLiquid.cpp:1156
+    assert lib_cfg.cg_max_iters == 2000  # Projector.cpp:161
+
+
+def test_status_strings_and_abi_version(garm_lib):
+    assert garm_lib.garm_abi_version() == 1
+    assert garm_lib.garm_status_string(capi.NOT_CONVERGED) == b"pressure solve did not converge"
+
+
+def test_null_arguments_are_rejected_without_a_gpu(garm_lib):
+    # argument validation happens before any CUDA call
+    assert garm_lib.garm_sim_create(None, None, None, None) == capi.INVALID
+    assert garm_lib.garm_sim_advance(None, 0.01, None) == capi.INVALID
+    assert garm_lib.garm_sim_upload(None, 0, None, 0) == capi.INVALID
+    assert garm_lib.garm_config_default(None) == capi.INVALID
+    bad = capi.grid_desc(3, [3, 3, 3], 0.1, [0, 0, 0])  # smaller than the solid ring
+    h = C.c_void_p()
+    assert garm_lib.garm_sim_create(C.byref(bad), None, None, C.byref(h)) == capi.INVALID

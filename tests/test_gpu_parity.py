@@ -1,0 +1,225 @@
+"""GPU parity: every stage of LevelSetLiquid::advance on the sm_103a kernels,
+called through the C ABI, against the FP64 CPU oracle on identical seeded inputs.
+
+Tolerances (FP64 plain form):
+  * boundary set-up, flags, counts, unknown numbering: exact;
+  * single stages: |gpu - oracle| <= 1e-11 (relative to the field's max) — the
+    kernels use FMA contraction and a tensor-product Hermite evaluation, so they
+    differ from the oracle by rounding only;
+  * projection: velocity within 1e-6 relative (both solve to |r| <= 1e-8 |b|);
+  * one full step: φ L∞ <= 1e-6·dx (the parity gate of the path).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from garm import capi, scenes
+from helpers import STATE_FIELDS, copy_state, host_default_config, linf, load_scene, rel
+
+pytestmark = pytest.mark.gpu
+
+STAGE_TOL = 1e-11
+
+
+def pair(oracle_mod, scene, **cfgkw):
+    cfg = host_default_config(**cfgkw)
+    g = capi.Simulation(scene.grid, cfg)
+    o = oracle_mod.OracleSim(scene.grid, cfg)
+    load_scene(g, scene)
+    load_scene(o, scene)
+    return g, o
+
+
+def advanced_state(oracle_mod, scene, steps, **cfgkw):
+    """Oracle state after initialize + restart + `steps` steps (gives non-trivial u, ξ, Π)."""
+    cfg = host_default_config(**cfgkw)
+    o = oracle_mod.OracleSim(scene.grid, cfg)
+    load_scene(o, scene)
+    o.initialize()
+    o.stage("restart")
+    for dt in scenes.frame_time_steps(o.max_speed, steps, 25, 1.0, scene.grid.spacing):
+        o.advance(dt)
+    return o
+
+
+SCENES = {
+    "dam2d": lambda: scenes.dam_break(2, 40),
+    "dam3d": lambda: scenes.dam_break(3, 20),
+    "drop3d": lambda: scenes.drop(20, seed=3),
+}
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+def test_boundary_and_initialize(oracle_mod, garm_lib, name):
+    sc = SCENES[name]()
+    g, o = pair(oracle_mod, sc)
+    for f in (capi.FIELD_CELL_DIST, capi.FIELD_NODE_DIST, capi.FIELD_BOUNDARY_NORMAL):
+        assert np.array_equal(g.download(f), o.download(f)), capi.FIELD_NAMES[f]
+    assert g.initialize() == capi.OK
+    assert o.initialize() == capi.OK
+    assert np.array_equal(g.download(capi.FIELD_FRACTION), o.download(capi.FIELD_FRACTION))
+    dx = sc.grid.spacing
+    assert linf(g.download(capi.FIELD_LEVEL_SET), o.download(capi.FIELD_LEVEL_SET)) <= 1e-9 * dx
+    assert np.array_equal(g.download(capi.FIELD_ADV_REGION), o.download(capi.FIELD_ADV_REGION))
+    assert linf(g.download(capi.FIELD_REF_MAP), o.download(capi.FIELD_REF_MAP)) == 0.0
+    ug, uo = g.download(capi.FIELD_VELOCITY), o.download(capi.FIELD_VELOCITY)
+    assert linf(ug, uo) <= 1e-6 * max(1.0, float(np.max(np.abs(uo))))
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+def test_single_stages(oracle_mod, garm_lib, name):
+    sc = SCENES[name]()
+    o = advanced_state(oracle_mod, sc, 3)
+    cfg = host_default_config()
+    g = capi.Simulation(sc.grid, cfg)
+    load_scene(g, sc)
+    g.initialize()  # boundary fractions
+    dt = 0.5 * sc.grid.spacing / max(o.max_speed(), 1e-3)
+
+    def sync():
+        copy_state(g, o)
+
+    checks = {
+        "advect": ([dt], [capi.FIELD_REF_MAP, capi.FIELD_REF_MAP_GRAD, capi.FIELD_VELOCITY]),
+        "compose": ([], [capi.FIELD_LEVEL_SET, capi.FIELD_TMP_LEVEL_SET, capi.FIELD_ORI_LEVEL_SET]),
+        "reinit": ([], [capi.FIELD_LEVEL_SET]),
+        "extrap_collider": ([], [capi.FIELD_LEVEL_SET, capi.FIELD_ORI_LEVEL_SET]),
+        "restart": ([], [capi.FIELD_REF_LEVEL_SET, capi.FIELD_REF_LEVEL_SET_GRAD, capi.FIELD_REF_MAP, capi.FIELD_REF_MAP_GRAD]),
+        "body_force": ([dt], [capi.FIELD_VELOCITY]),
+        "extrap_air": ([], [capi.FIELD_REF_MAP, capi.FIELD_ADV_REGION, capi.FIELD_VELOCITY]),
+        "enforce_bc": ([], [capi.FIELD_VELOCITY]),
+    }
+    snapshot = {f: o.download(f) for f in STATE_FIELDS}
+    for stage, (args, fields) in checks.items():
+        for f, v in snapshot.items():
+            o.upload(f, v)
+        sync()
+        g.stage(stage, *args)
+        o.stage(stage, *(args or [0.0]))
+        for f in fields:
+            a, b = g.download(f), o.download(f)
+            if f == capi.FIELD_ADV_REGION:
+                assert np.array_equal(a, b), f"{stage}: {capi.FIELD_NAMES[f]}"
+            else:
+                assert rel(a, b) <= STAGE_TOL, f"{stage}: {capi.FIELD_NAMES[f]} rel err {rel(a, b):.3e}"
+    # reference-map test: identical counts
+    for f, v in snapshot.items():
+        o.upload(f, v)
+    sync()
+    assert g.stage("rm_check") == o.stage("rm_check")
+    # projection: same unknown set, velocity within the solver tolerance
+    sg = g.stage("project")
+    so = o.stage("project")
+    assert sg["unknowns"] == so["unknowns"]
+    assert sg["cg_residual"] <= 1e-8 and so["cg_residual"] <= 1e-8
+    ug, uo = g.download(capi.FIELD_VELOCITY), o.download(capi.FIELD_VELOCITY)
+    assert rel(ug, uo) <= 1e-6, f"project: velocity rel err {rel(ug, uo):.3e}"
+    pg, po = g.download(capi.FIELD_PRESSURE), o.download(capi.FIELD_PRESSURE)
+    assert rel(pg, po) <= 1e-5
+    assert np.array_equal(pg != 0, po != 0) or so["unknowns"] == 0
+
+
+@pytest.mark.parametrize("name", list(SCENES))
+def test_one_step_parity_gate(oracle_mod, garm_lib, name):
+    """φ L∞ <= 1e-6·dx after initialize + restart + one advance (same dt on both)."""
+    sc = SCENES[name]()
+    g, o = pair(oracle_mod, sc)
+    g.initialize(); o.initialize()
+    g.stage("restart"); o.stage("restart")
+    dt = next(scenes.frame_time_steps(o.max_speed, 1, 25, 1.0, sc.grid.spacing))
+    sg = g.advance(dt)
+    so = o.advance(dt)
+    dx = sc.grid.spacing
+    err = linf(g.download(capi.FIELD_LEVEL_SET), o.download(capi.FIELD_LEVEL_SET))
+    assert err <= 1e-6 * dx, f"phi err {err / dx:.3e} dx"
+    assert sg["restarted"] == so["restarted"]
+    assert sg["unknowns"] == so["unknowns"]
+    assert rel(g.download(capi.FIELD_VELOCITY), o.download(capi.FIELD_VELOCITY)) <= 1e-5
+
+
+def test_restart_branch_every_step(oracle_mod, garm_lib):
+    """rm_threshold = -1 makes checkReferenceMap fail, so restart runs inside advance."""
+    sc = scenes.dam_break(3, 16)
+    g, o = pair(oracle_mod, sc, rm_threshold=-1.0)
+    g.initialize(); o.initialize()
+    g.stage("restart"); o.stage("restart")
+    for dt in [0.01, 0.01]:
+        sg, so = g.advance(dt), o.advance(dt)
+        assert sg["restarted"] == 1 and so["restarted"] == 1
+    dx = sc.grid.spacing
+    assert linf(g.download(capi.FIELD_LEVEL_SET), o.download(capi.FIELD_LEVEL_SET)) <= 1e-6 * dx
+
+
+def test_n_step_drift(oracle_mod, garm_lib, capsys):
+    """Drift of φ, u and ξ after 12 steps with each side choosing its own dt."""
+    sc = scenes.dam_break(3, 24)
+    g, o = pair(oracle_mod, sc)
+    g.initialize(); o.initialize()
+    g.stage("restart"); o.stage("restart")
+    dts_g = list(scenes.frame_time_steps(g.max_speed, 1, 25, 1.0, sc.grid.spacing))
+    steps = 12
+    gen_o = scenes.frame_time_steps(o.max_speed, steps, 25, 1.0, sc.grid.spacing)
+    gen_g = scenes.frame_time_steps(g.max_speed, steps, 25, 1.0, sc.grid.spacing)
+    for dto, dtg in zip(gen_o, gen_g):
+        o.advance(dto)
+        g.advance(dtg)
+    dx = sc.grid.spacing
+    ephi = linf(g.download(capi.FIELD_LEVEL_SET), o.download(capi.FIELD_LEVEL_SET)) / dx
+    eu = rel(g.download(capi.FIELD_VELOCITY), o.download(capi.FIELD_VELOCITY))
+    exi = linf(g.download(capi.FIELD_REF_MAP), o.download(capi.FIELD_REF_MAP)) / dx
+    with capsys.disabled():
+        print(f"\n[drift after {steps} steps, 24^3 dam break] phi {ephi:.3e} dx, u rel {eu:.3e}, xi {exi:.3e} dx")
+    assert ephi <= 1e-3
+    assert dts_g
+
+
+def test_empty_and_full_liquid(oracle_mod, garm_lib):
+    """No unknowns (all air) and all-liquid domains run and agree."""
+    for fill in (+1.0, -1.0):
+        sc = scenes.dam_break(3, 12)
+        sc.phi[...] = fill
+        g, o = pair(oracle_mod, sc)
+        g.initialize(); o.initialize()
+        g.stage("restart"); o.stage("restart")
+        sg, so = g.advance(0.01), o.advance(0.01)
+        assert sg["unknowns"] == so["unknowns"]
+        if fill > 0:
+            assert sg["unknowns"] == 0
+        dx = sc.grid.spacing
+        assert linf(g.download(capi.FIELD_LEVEL_SET), o.download(capi.FIELD_LEVEL_SET)) <= 1e-6 * dx
+
+
+def test_reinit_known_answer(oracle_mod, garm_lib):
+    """WENO5 reinitialisation of TestReinit case 0 (exp-distorted circle,
+    Source/Test/TestReinit/TestReinit.cpp:89-101): the GPU matches the oracle and
+    both approach the exact SDF in the |φ| <= 3dx band."""
+    n, length = 100, 10.0
+    dx = length / n
+    x = (np.arange(n) + 0.5) * dx - length / 2
+    X, Y = np.meshgrid(x, x, indexing="xy")
+    r = np.sqrt(X * X + Y * Y)
+    r0 = 0.2313 * length
+    maxd = length / np.sqrt(2) - r0
+    phi0 = (np.exp(r - r0) - 1) * (maxd / (np.exp(maxd) - 1))
+    sdf = r - r0
+    pg = capi.reinit_host(phi0, dx, 60, 0.5)
+    po = oracle_mod.reinit(phi0, dx, 60, 0.5)
+    assert linf(pg, po) <= 1e-10
+    band = np.abs(pg) <= 3 * dx
+    err0 = np.mean(np.abs(phi0 - sdf)[np.abs(phi0) <= 3 * dx])
+    err = np.mean(np.abs(pg - sdf)[band])
+    assert err < 0.05 * err0 and err < 0.02 * dx
+
+
+def test_invalid_arguments(garm_lib):
+    sc = scenes.dam_break(2, 16)
+    g = capi.Simulation(sc.grid, host_default_config())
+    with pytest.raises(capi.GarmError) as e:
+        g.upload(capi.FIELD_LEVEL_SET, np.zeros(5))
+    assert e.value.status == capi.INVALID
+    with pytest.raises(capi.GarmError):
+        g.download(capi.FIELD_COUNT if hasattr(capi, "FIELD_COUNT") else 99)
+    bad = capi.grid_desc(4, [8, 8, 8], 0.1, [0, 0, 0])
+    with pytest.raises(capi.GarmError):
+        capi.Simulation(bad, host_default_config())
