@@ -484,6 +484,14 @@ garm_status garm_sim_upload(garm_sim *sim, int field, const void *host, size_t b
 garm_status garm_sim_download(garm_sim *sim, int field, void *host, size_t bytes) { return sim ? download(sim->s, field, host, bytes) : GARM_INVALID; }
 garm_status garm_sim_initialize(garm_sim *sim) { return sim ? initialize(sim->s) : GARM_INVALID; }
 
+garm_status garm_sim_finish_load(garm_sim *sim) {
+	if (!sim) return GARM_INVALID;
+	State &s = sim->s;
+	GARM_TRY(GARM_DISPATCH(s, finishBoundary, s));
+	GARM_TRY(GARM_DISPATCH(s, refreshRefGradient, s));
+	return sync(s);
+}
+
 garm_status garm_sim_advance(garm_sim *sim, double dt, garm_step_stats *stats) {
 	if (!sim || !std::isfinite(dt) || dt < 0) return GARM_INVALID;
 	return advance(sim->s, dt, stats);

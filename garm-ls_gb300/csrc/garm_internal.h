@@ -94,6 +94,7 @@ template <int D, typename T> garm_status enforceBoundaryConditions(State &s);
 template <int D, typename T> garm_status enforceBoundaryLevelSet(State &s, void *field, double tol);
 template <int D, typename T> garm_status resetRefView(State &s);
 template <int D, typename T> garm_status initRefMap(State &s);
+template <int D, typename T> garm_status refreshRefGradient(State &s);
 template <int D, typename T> garm_status maxSpeed(State &s, double *out);
 template <int D, typename T> garm_status copyField(State &s, void *dst, const void *src, int64_t n);
 

@@ -91,32 +91,55 @@ garm_status generateCurrentFields(State &s) {
 // ---------------------------------------------------------------------------
 // WENO5 reinitialisation (Reinitialization.h:20-80)
 // ---------------------------------------------------------------------------
+// 2^-e for the binary exponent e of x > 0 (x normal): an exact power-of-two
+// scale built from the exponent bits, used to keep the WENO weights in range.
+__device__ __forceinline__ double pow2NegExp(double x) {
+	const int hi = __double2hiint(x);
+	const int e = ((hi >> 20) & 0x7ff) - 1023;
+	return __hiloint2double((1023 - e) << 20, 0);
+}
+__device__ __forceinline__ float pow2NegExp(float x) {
+	const int e = ((__float_as_int(x) >> 23) & 0xff) - 127;
+	return __int_as_float((127 - e) << 23);
+}
+
+// One one-sided WENO5 derivative from five differences (Derivatives.h:137-157),
+// returned without the 1/(6 dx) factor.  The three weights α_k = d_k/(s_k+ε)^2 are
+// normalised with a single division: with q_k = (s_k+ε)·2^-e (2^e ~ ε, an exact
+// scale) every q_k lies in [1/2, ~7e7], so d_k·q_i^2·q_j^2 neither overflows nor
+// underflows in FP32 or FP64, and Σα_k P_k / Σα_k = Σ w_k P_k / Σ w_k with
+// w_1 = .1 q_2^2 q_3^2, w_2 = .6 q_1^2 q_3^2, w_3 = .3 q_1^2 q_2^2.
+template <typename T>
+__device__ __forceinline__ T wenoSide(T d0, T d1, T d2, T d3, T d4, T sq0, T sq1, T sq2, T sq3, T sq4, T floorEps) {
+	const T m = fmax(fmax(fmax(sq0, sq1), fmax(sq2, sq3)), sq4);
+	const T eps = fma(m, T(1e-6), floorEps);
+	const T P1 = T(2) * d0 - T(7) * d1 + T(11) * d2;   // 6·phix1
+	const T P2 = -d1 + T(5) * d2 + T(2) * d3;           // 6·phix2
+	const T P3 = T(2) * d2 + T(5) * d3 - d4;            // 6·phix3
+	const T e1 = d0 - T(2) * d1 + d2, f1 = d0 - T(4) * d1 + T(3) * d2;
+	const T e2 = d1 - T(2) * d2 + d3, f2 = d1 - d3;
+	const T e3 = d2 - T(2) * d3 + d4, f3 = T(3) * d2 - T(4) * d3 + d4;
+	const T c13 = T(13.0 / 12.0);
+	const T s1 = fma(c13 * e1, e1, T(0.25) * f1 * f1);
+	const T s2 = fma(c13 * e2, e2, T(0.25) * f2 * f2);
+	const T s3 = fma(c13 * e3, e3, T(0.25) * f3 * f3);
+	const T sc = pow2NegExp(eps);
+	const T q1 = (s1 + eps) * sc, q2 = (s2 + eps) * sc, q3 = (s3 + eps) * sc;
+	const T t1 = q1 * q1, t2 = q2 * q2, t3 = q3 * q3;
+	const T w1 = T(0.1) * t2 * t3, w2 = T(0.6) * t1 * t3, w3 = T(0.3) * t1 * t2;
+	return (w1 * P1 + w2 * P2 + w3 * P3) / (w1 + w2 + w3);
+}
+
+// weno5 (Derivatives.h:134-159): one-sided derivatives (φ⁻, φ⁺) from seven values.
 template <typename T>
 __device__ __forceinline__ void weno5(const T v[7], T invDx, T &dm, T &dp) {
-#pragma unroll
-	for (int side = 0; side < 2; side++) {
-		T d0, d1, d2, d3, d4;
-		if (side) { d0 = v[6] - v[5]; d1 = v[5] - v[4]; d2 = v[4] - v[3]; d3 = v[3] - v[2]; d4 = v[2] - v[1]; }
-		else { d0 = v[1] - v[0]; d1 = v[2] - v[1]; d2 = v[3] - v[2]; d3 = v[4] - v[3]; d4 = v[5] - v[4]; }
-		T eps = fmax(fmax(fmax(d0 * d0, d1 * d1), fmax(d2 * d2, d3 * d3)), d4 * d4);
-		// 1e-99 in FP64 (Derivatives.h:144); FP32 needs a floor whose square stays normal
-		eps = eps * T(1e-6) + (sizeof(T) == 8 ? T(1e-99) : T(1e-18));
-		const T phix1 = d0 / T(3) - d1 * T(7) / T(6) + d2 * T(11) / T(6);
-		const T phix2 = -d1 / T(6) + d2 * T(5) / T(6) + d3 / T(3);
-		const T phix3 = d2 / T(3) + d3 * T(5) / T(6) - d4 / T(6);
-		const T e1 = d0 - T(2) * d1 + d2, f1 = d0 - T(4) * d1 + T(3) * d2;
-		const T e2 = d1 - T(2) * d2 + d3, f2 = d1 - d3;
-		const T e3 = d2 - T(2) * d3 + d4, f3 = T(3) * d2 - T(4) * d3 + d4;
-		const T s1 = e1 * e1 * T(13) / T(12) + f1 * f1 / T(4);
-		const T s2 = e2 * e2 * T(13) / T(12) + f2 * f2 / T(4);
-		const T s3 = e3 * e3 * T(13) / T(12) + f3 * f3 / T(4);
-		const T q1 = s1 + eps, q2 = s2 + eps, q3 = s3 + eps;
-		const T a1 = T(0.1) / (q1 * q1);
-		const T a2 = T(0.6) / (q2 * q2);
-		const T a3 = T(0.3) / (q3 * q3);
-		const T r = (a1 * phix1 + a2 * phix2 + a3 * phix3) / (a1 + a2 + a3) * invDx;
-		if (side) dp = r; else dm = r;
-	}
+	// 1e-99 in FP64 (Derivatives.h:144); FP32 takes the smallest comparable normal number
+	const T floorEps = sizeof(T) == 8 ? T(1e-99) : T(1e-30);
+	const T D1 = v[1] - v[0], D2 = v[2] - v[1], D3 = v[3] - v[2], D4 = v[4] - v[3], D5 = v[5] - v[4], D6 = v[6] - v[5];
+	const T Q1 = D1 * D1, Q2 = D2 * D2, Q3 = D3 * D3, Q4 = D4 * D4, Q5 = D5 * D5, Q6 = D6 * D6;
+	const T k = invDx * T(1.0 / 6.0);
+	dm = wenoSide<T>(D1, D2, D3, D4, D5, Q1, Q2, Q3, Q4, Q5, floorEps) * k;
+	dp = wenoSide<T>(D6, D5, D4, D3, D2, Q6, Q5, Q4, Q3, Q2, floorEps) * k;
 }
 
 // One TVD-RK3 sub-stage: out = lin(base, in + dt*L(in)).
@@ -144,7 +167,7 @@ __global__ void __launch_bounds__(kBlock) kReinitStage(G<D, T> g, const T *__res
 	}
 	sum = sqrt(sum);
 	const T sp = g.dx * sum;
-	const T sgn = f / sqrt(f * f + sp * sp);
+	const T sgn = f * rsqrt(f * f + sp * sp);  // smoothed sign (Reinitialization.h:26)
 	const T adv = f + dt * sgn * (T(1) - sum);
 	T r;
 	if (Mode == 0) r = adv;
@@ -294,6 +317,34 @@ garm_status restart(State &s) {
 	return resetRefView<D, T>(s);
 }
 
+// ψ0 = computeFirst<4>(φ0) as loadFrame does without Newton (LevelSetLiquid.cpp:507-509)
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kRefGrad4(Geom geom, const T *ref, T *g0, T *g1, T *g2) {
+	const G<D, T> g = cellGrid<D, T>(geom);
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= g.count()) return;
+	int i, j, k;
+	g.coord(id, i, j, k);
+	T *out[3] = {g0, g1, g2};
+	const T h = g.inv / T(12);
+#pragma unroll
+	for (int a = 0; a < D; a++) {
+		const int ex = a == 0, ey = a == 1, ez = a == 2;
+		const T v0 = ldg(ref + g.cidx(i - 2 * ex, j - 2 * ey, k - 2 * ez));
+		const T v1 = ldg(ref + g.cidx(i - ex, j - ey, k - ez));
+		const T v3 = ldg(ref + g.cidx(i + ex, j + ey, k + ez));
+		const T v4 = ldg(ref + g.cidx(i + 2 * ex, j + 2 * ey, k + 2 * ez));
+		out[a][id] = (v0 - T(8) * v1 + T(8) * v3 - v4) * h;
+	}
+}
+
+template <int D, typename T>
+garm_status refreshRefGradient(State &s) {
+	kRefGrad4<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, (const T *)s.ref, (T *)s.refGrad[0], (T *)s.refGrad[1], (T *)(D == 3 ? s.refGrad[2] : nullptr)); s.launches++;
+	GARM_CHECK_LAUNCH();
+	return resetRefView<D, T>(s);
+}
+
 // ξ = x, advRegion = 1, Π = I (LevelSetLiquid.cpp:560-566)
 template <int D, typename T>
 __global__ void __launch_bounds__(kBlock) kInitRefMap(Geom geom, RestartIO<D, T> io, uint8_t *adv) {
@@ -345,6 +396,7 @@ garm_status enforceBoundaryLevelSet(State &s, void *field, double tol) {
 	template garm_status checkReferenceMap<D, T>(State &, int *, int *, int *); \
 	template garm_status restart<D, T>(State &); \
 	template garm_status initRefMap<D, T>(State &); \
+	template garm_status refreshRefGradient<D, T>(State &); \
 	template garm_status enforceBoundaryLevelSet<D, T>(State &, void *, double);
 GARM_INST(2, double)
 GARM_INST(3, double)

@@ -71,6 +71,19 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     return LIB_PATH
 
 
+DEMO_SRC = PKG_DIR / "host" / "garm_demo.cpp"
+DEMO_BIN = PKG_DIR / "garm_demo"
+
+
+def build_demo(force: bool = False) -> Path:
+    """The C++ host drop-in (host/GpuLevelSetLiquid.h) exercised by a demo driver."""
+    deps = [DEMO_SRC, PKG_DIR / "host" / "GpuLevelSetLiquid.h", REPO / "include" / "garm.h", LIB_PATH]
+    if force or _stale(DEMO_BIN, deps):
+        _run(["g++", "-std=c++17", "-O2", "-Wall", "-I", str(REPO / "include"), "-I", str(PKG_DIR / "host"),
+              str(DEMO_SRC), "-o", str(DEMO_BIN), "-L", str(PKG_DIR), "-lgarm", "-Wl,-rpath,$ORIGIN"])
+    return DEMO_BIN
+
+
 def build_oracle(force: bool = False) -> Path:
     if force or _stale(ORACLE_LIB, [ORACLE_SRC, REPO / "include" / "garm.h"]):
         _run(["g++", "-std=c++20", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
@@ -80,4 +93,5 @@ def build_oracle(force: bool = False) -> Path:
 
 if __name__ == "__main__":
     build_library(force="--force" in sys.argv, verbose=True)
+    build_demo(force="--force" in sys.argv)
     build_oracle(force="--force" in sys.argv)

@@ -81,6 +81,7 @@ _SIGS = {
     "garm_sim_upload": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),
     "garm_sim_download": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),
     "garm_sim_initialize": (C.c_int, [C.c_void_p]),
+    "garm_sim_finish_load": (C.c_int, [C.c_void_p]),
     "garm_sim_advance": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(StepStats)]),
     "garm_sim_max_speed": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "garm_sim_time_step": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_double)]),
@@ -222,6 +223,9 @@ class Simulation:
             check(st, "garm_sim_initialize")
         return st
 
+    def finish_load(self) -> None:
+        check(self.lib.garm_sim_finish_load(self.handle), "garm_sim_finish_load")
+
     def advance(self, dt: float, allow_not_converged: bool = True) -> dict:
         stats = StepStats()
         st = self.lib.garm_sim_advance(self.handle, float(dt), C.byref(stats))
@@ -265,7 +269,9 @@ class Simulation:
             st = lib.garm_stage_project(h, C.byref(stats))
             if st not in (OK, NOT_CONVERGED):
                 check(st, name)
-            return stats.as_dict()
+            d = stats.as_dict()
+            d["status"] = st
+            return d
         elif name == "extrap_air":
             check(lib.garm_stage_extrap_air(h), name)
         elif name == "enforce_bc":

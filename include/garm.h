@@ -135,6 +135,11 @@ garm_status garm_sim_download(garm_sim *sim, int field, void *host, size_t bytes
  * Newton/FMM off.  Expects the velocity and level set uploaded first. */
 garm_status garm_sim_initialize(garm_sim *sim);
 
+/* The non-I/O part of LevelSetLiquid::loadFrame (Source/Core/LevelSetLiquid.cpp:474-526),
+ * to call after uploading velocity, refMap, refLevelSet, advRegion and refMapGrad:
+ * Boundary::finish, ψ0 = computeFirst<4>(φ0) and the Hermite view reset. */
+garm_status garm_sim_finish_load(garm_sim *sim);
+
 /* LevelSetLiquid::advance (Source/Core/LevelSetLiquid.cpp:608-698). `stats` may be NULL. */
 garm_status garm_sim_advance(garm_sim *sim, double dt, garm_step_stats *stats);
 

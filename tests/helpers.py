@@ -53,3 +53,36 @@ def linf(a, b) -> float:
 def rel(a, b) -> float:
     scale = max(float(np.max(np.abs(np.asarray(b, dtype=np.float64)))), 1e-300)
     return linf(a, b) / scale
+
+
+def velocity_check(g_u, o_u, fraction, rtol: float):
+    """Compare staggered velocities.  Faces of the fluid domain (fraction < 1)
+    must agree to `rtol` of max|u|.  On solid faces (fraction == 1) the wall
+    condition of Boundary::enforce (Boundary.cpp:98-110) branches on the sign of
+    the normal velocity vn; where vn is zero up to rounding the two sides may take
+    different branches, which leaves one at u and the other at 0.2·u (the 0.8
+    tangential damping).  Those faces are counted, every other solid-face
+    mismatch fails.  Returns (interior relative error, number of tie faces)."""
+    g_u = np.asarray(g_u, dtype=np.float64)
+    o_u = np.asarray(o_u, dtype=np.float64)
+    scale = max(float(np.max(np.abs(o_u))), 1e-300)
+    diff = np.abs(g_u - o_u)
+    fluid = fraction < 1
+    inner = float(np.max(diff[fluid], initial=0.0)) / scale
+    bad = (~fluid) & (diff > rtol * scale)
+    ties = 0
+    for gv, ov in zip(g_u[bad], o_u[bad]):
+        if abs(gv - 0.2 * ov) <= rtol * scale + 1e-6 * abs(ov) or abs(ov - 0.2 * gv) <= rtol * scale + 1e-6 * abs(gv):
+            ties += 1
+        else:
+            raise AssertionError(f"solid-face velocity mismatch not explained by the wall-condition tie: {gv} vs {ov}")
+    return inner, ties
+
+
+def band_error(a, b, ref_phi, dx: float, band: float = 3.0) -> float:
+    """L∞ of a-b over cells with |ref_phi| <= band·dx (the accuracy band of the
+    reference's own error measure, TestReinit.cpp:162-171 and TestAdvect2D.cpp:250-264)."""
+    m = np.abs(np.asarray(ref_phi)) <= band * dx
+    if not np.any(m):
+        return 0.0
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))[m]))
