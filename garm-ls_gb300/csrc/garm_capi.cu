@@ -122,6 +122,7 @@ garm_status allocState(State &s) {
 	} else {
 		GARM_TRY(dalloc(s, &s.wts32, N * 4 * 2 * D));
 		GARM_TRY(dalloc(s, &s.diag32, N * 4));
+		GARM_TRY(dalloc(s, &s.invd32, N * 4));
 		GARM_TRY(dalloc(s, &s.fR, N * 4));
 		GARM_TRY(dalloc(s, &s.fZ, N * 4));
 		GARM_TRY(dalloc(s, &s.fP0, N * 4));
@@ -129,7 +130,7 @@ garm_status allocState(State &s) {
 		GARM_TRY(dalloc(s, &s.fQ, N * 4));
 		GARM_TRY(dalloc(s, &s.fE, N * 4));
 	}
-	s.maxBlocks = s.numSMs * 2;
+	s.maxBlocks = s.numSMs;
 	GARM_TRY(dalloc(s, &s.partials, size_t(s.maxBlocks) * 4 * 8));
 	GARM_TRY(dalloc(s, &s.barrier, 64));
 	GARM_TRY(dalloc(s, &s.cgScalars, 64));
@@ -435,6 +436,8 @@ garm_status garm_sim_create(const garm_grid_desc *gd, const garm_config *cfg, vo
 		} else s.F[a] = 0;
 		s.Ftot += s.F[a];
 	}
+	// every grid (cells, nodes, faces) must index with 32-bit integers
+	if (s.NN >= (int64_t(1) << 31) || s.Ftot >= (int64_t(1) << 31)) { freeAll(s); delete sim; return GARM_INVALID; }
 	garm_status r = allocState(s);
 	if (r == GARM_OK) r = GARM_DISPATCH(s, initBoundary, s);           // Boundary ctor → reset()
 	if (r == GARM_OK) {

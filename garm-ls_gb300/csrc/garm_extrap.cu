@@ -201,22 +201,27 @@ __global__ void kCellMask(int64_t N, int kind, const T *cellDist, const uint8_t 
 // Kind 0: NS scalar planes (cell double, Extrapolation.h:86-126)
 // Kind 1: D-vector reference map; unreached cells get their position (Extrapolation.h:176-218)
 // Kind 2: flag (uchar) (Extrapolation.h:128-174)
+// Neighbours are visited in the reference's order -x,+x,-y,+y,-z,+z (Grid.h:59-60).
 template <int D, typename T, int Kind, int NS>
 __global__ void __launch_bounds__(kBlock) kExtrapCellPass(Geom geom, T *f0, T *f1, T *f2, uint8_t *flag, const uint8_t *__restrict__ vis0, uint8_t *vis1) {
-	const G<D, T> g = cellGrid<D, T>(geom);
-	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-	if (id >= g.count()) return;
+	const int sx = geom.n[0], sy = geom.n[1], sz = D == 3 ? geom.n[2] : 1;
+	const int N = sx * sy * sz;
+	const int id = int(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= N) return;
 	if (vis0[id]) { vis1[id] = 1; return; }
-	int i, j, k;
-	g.coord(id, i, j, k);
+	const unsigned r = unsigned(id) / unsigned(sx);
+	const int i = id - int(r) * sx;
+	const int j = D == 3 ? int(r % unsigned(sy)) : int(r);
+	const int k = D == 3 ? int(r / unsigned(sy)) : 0;
+	const int sxy = sx * sy;
+	const int off[6] = {-1, 1, -sx, sx, -sxy, sxy};
+	const bool ok[6] = {i > 0, i < sx - 1, j > 0, j < sy - 1, k > 0, k < sz - 1};
 	int cnt = 0;
 	T s0 = T(0), s1 = T(0), s2 = T(0);
 #pragma unroll
 	for (int q = 0; q < 2 * D; q++) {
-		const int a = q >> 1, sd = (q & 1) ? 1 : -1;
-		const int ni = i + (a == 0 ? sd : 0), nj = j + (a == 1 ? sd : 0), nk = k + (a == 2 ? sd : 0);
-		if (!g.valid(ni, nj, nk)) continue;
-		const int64_t n = g.idx(ni, nj, nk);
+		if (!ok[q]) continue;
+		const int n = id + off[q];
 		if (!vis0[n]) continue;
 		cnt++;
 		if (Kind == 0) { s0 += f0[n]; if (NS > 1) s1 += f1[n]; }
@@ -229,7 +234,10 @@ __global__ void __launch_bounds__(kBlock) kExtrapCellPass(Geom geom, T *f0, T *f
 		else flag[id] = 1;
 		vis1[id] = 1;
 	} else {
-		if (Kind == 1) { f0[id] = g.pos(0, i); f1[id] = g.pos(1, j); if (D == 3) f2[id] = g.pos(2, k); }
+		if (Kind == 1) {
+			const G<D, T> g = cellGrid<D, T>(geom);
+			f0[id] = g.pos(0, i); f1[id] = g.pos(1, j); if (D == 3) f2[id] = g.pos(2, k);
+		}
 		vis1[id] = 0;
 	}
 }
@@ -268,22 +276,25 @@ __global__ void kFaceMask(Geom geom, const T *fr0, const T *fr1, const T *fr2, c
 
 template <int D, typename T>
 __global__ void __launch_bounds__(kBlock) kExtrapFacePass(Geom geom, T *u0, T *u1, T *u2, const uint8_t *__restrict__ vis0, uint8_t *vis1, int64_t F0, int64_t F1, int64_t Ftot) {
-	int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-	if (id >= Ftot) return;
-	const int64_t gid = id;
+	const int gid = int(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (gid >= int(Ftot)) return;
 	if (vis0[gid]) { vis1[gid] = 1; return; }
-	int axis = 0; int64_t base = 0;
-	if (id >= F0) { id -= F0; axis = 1; base = F0; if (id >= F1) { id -= F1; axis = 2; base = F0 + F1; } }
-	const G<D, T> g = faceGrid<D, T>(geom, axis);
+	int id = gid, axis = 0, base = 0;
+	if (id >= int(F0)) { id -= int(F0); axis = 1; base = int(F0); if (id >= int(F1)) { id -= int(F1); axis = 2; base = int(F0 + F1); } }
+	const int sx = geom.n[0] + (axis == 0), sy = geom.n[1] + (axis == 1), sz = D == 3 ? geom.n[2] + (axis == 2) : 1;
 	T *u = axis == 0 ? u0 : (axis == 1 ? u1 : u2);
-	int i, j, k; g.coord(id, i, j, k);
+	const unsigned r = unsigned(id) / unsigned(sx);
+	const int i = id - int(r) * sx;
+	const int j = D == 3 ? int(r % unsigned(sy)) : int(r);
+	const int k = D == 3 ? int(r / unsigned(sy)) : 0;
+	const int sxy = sx * sy;
+	const int off[6] = {-1, 1, -sx, sx, -sxy, sxy};
+	const bool ok[6] = {i > 0, i < sx - 1, j > 0, j < sy - 1, k > 0, k < sz - 1};
 	int cnt = 0; T s = T(0);
 #pragma unroll
 	for (int q = 0; q < 2 * D; q++) {
-		const int a = q >> 1, sd = (q & 1) ? 1 : -1;
-		const int ni = i + (a == 0 ? sd : 0), nj = j + (a == 1 ? sd : 0), nk = k + (a == 2 ? sd : 0);
-		if (!g.valid(ni, nj, nk)) continue;
-		const int64_t n = g.idx(ni, nj, nk);
+		if (!ok[q]) continue;
+		const int n = id + off[q];
 		if (!vis0[base + n]) continue;
 		cnt++; s += u[n];
 	}

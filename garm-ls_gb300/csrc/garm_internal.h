@@ -59,7 +59,7 @@ struct State {
 	int *nbr = nullptr;        // [2D][N] neighbour unknown id, -1 if none
 	double *wts = nullptr;     // [2D][N] off-diagonal weights (positive w; matrix entry is -w)
 	double *diag = nullptr, *invd = nullptr, *rhs = nullptr, *pres = nullptr;
-	float *wts32 = nullptr, *diag32 = nullptr;
+	float *wts32 = nullptr, *diag32 = nullptr, *invd32 = nullptr;
 	// PCG work vectors (FP64) and the FP32 inner vectors of the mixed form
 	double *cgX = nullptr, *cgR = nullptr, *cgZ = nullptr, *cgP0 = nullptr, *cgP1 = nullptr, *cgQ = nullptr;
 	float *fR = nullptr, *fZ = nullptr, *fP0 = nullptr, *fP1 = nullptr, *fQ = nullptr, *fE = nullptr;

@@ -151,15 +151,20 @@ __global__ void __launch_bounds__(kBlock) kReinitStage(G<D, T> g, const T *__res
 	int i, j, k;
 	g.coord(id, i, j, k);
 	const T f = ldg(in + id);
+	// Stencil addressing: the base of the line through the cell along each axis,
+	// plus one clamped coordinate per load (clamp-to-edge, GridBasedData.h:47).
+	const int sx = g.s[0], sy = g.s[1], sz = D == 3 ? g.s[2] : 1;
+	const int sxy = sx * sy;
+	const T *line[3] = {in + (id - i), in + (id - j * sx), in + (id - k * sxy)};
+	const int lim[3] = {sx - 1, sy - 1, sz - 1};
+	const int pos[3] = {i, j, k};
+	const int str[3] = {1, sx, sxy};
 	T sum = T(0);
 #pragma unroll
 	for (int a = 0; a < D; a++) {
 		T v[7];
 #pragma unroll
-		for (int t = 0; t < 7; t++) {
-			const int o = t - 3;
-			v[t] = ldg(in + g.cidx(i + (a == 0 ? o : 0), j + (a == 1 ? o : 0), k + (a == 2 ? o : 0)));
-		}
+		for (int t = 0; t < 7; t++) v[t] = ldg(line[a] + min(max(pos[a] + t - 3, 0), lim[a]) * str[a]);
 		T dm, dp;
 		weno5<T>(v, g.inv, dm, dp);
 		if (f < T(0)) { const T x = fmin(dm, T(0)), y = fmax(dp, T(0)); sum += x * x; sum += y * y; }

@@ -13,7 +13,7 @@
 
 namespace garm {
 
-constexpr int kCgBlock = 256;
+constexpr int kCgBlock = 512;
 constexpr unsigned long long kBarrierSpinLimit = 20000000ull;  // x ~100 ns sleep: ~2 s, then GARM_TIMEOUT
 
 // ---------------------------------------------------------------------------
@@ -88,7 +88,7 @@ struct BuildIO {
 	const int *grid2mat;
 	int *nbr;
 	double *wts, *diag, *invd, *rhs;
-	float *wts32, *diag32;
+	float *wts32, *diag32, *invd32;
 	int64_t stride;
 };
 
@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(kBlock) kBuildSystem(Geom geom, BuildIO<D, T> 
 	io.rhs[r] = div;
 	io.diag[r] = dg;
 	io.invd[r] = dg != 0 ? 1 / dg : 1;  // Eigen DiagonalPreconditioner
-	if (io.diag32) io.diag32[r] = float(dg);
+	if (io.diag32) { io.diag32[r] = float(dg); io.invd32[r] = dg != 0 ? float(1 / dg) : 1.0f; }
 }
 
 // ---------------------------------------------------------------------------
@@ -141,7 +141,7 @@ struct CgArgs {
 	const int *nDev;
 	const int *nbr;
 	const double *w, *diag, *invd;
-	const float *w32, *diag32;
+	const float *w32, *diag32, *invd32;
 	int64_t stride;
 	const double *b;
 	double *x, *r, *z, *p0, *p1, *q;
@@ -158,8 +158,11 @@ struct CgArgs {
 	int *ints;     // [0] matvecs, [1] refinements
 };
 
-__device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
-__device__ __forceinline__ float ldcg(const float *p) { return __ldcg(p); }
+// Vectors written by other blocks in the previous phase.  gridSync() ends with
+// fences of GPU scope, which order these plain (L1-cacheable) loads after the
+// other blocks' stores; the read-only texture path (__ldg) is never used for them.
+__device__ __forceinline__ double ldcg(const double *p) { return *p; }
+__device__ __forceinline__ float ldcg(const float *p) { return *p; }
 
 // Grid-wide barrier with a bounded wait.  Returns false when any block gave up.
 __device__ bool gridSync(unsigned *bar, int *err) {
@@ -205,48 +208,63 @@ __device__ __forceinline__ void blockPartials(double (&acc)[NV], double *partial
 	__syncthreads();
 }
 
-// Sum of the gridDim partials of slot v, identical in every block.
-template <int NV>
-__device__ __forceinline__ void gridTotals(const double *partials, int maxBlocks, double (&out)[NV], double *sh) {
+// Sum of the gridDim partials of slot v, identical in every block (fixed lane
+// partition and shuffle tree: deterministic).  Lane 0 then runs `fin` on the
+// totals (scalar work done once per block) and the results are broadcast.
+template <int NV, int NOUT, typename Fin>
+__device__ __forceinline__ void gridTotals(const double *partials, int maxBlocks, double (&out)[NOUT], double *sh, Fin fin) {
+	static_assert(NOUT >= NV, "outputs include the sums");
 	const int lane = threadIdx.x & 31;
 	if (threadIdx.x < 32) {
+		double t[NOUT];
 #pragma unroll
 		for (int v = 0; v < NV; v++) {
 			double s = 0;
 			for (int b = lane; b < (int)gridDim.x; b += 32) s += ldcg(partials + v * maxBlocks + b);
-			s = warpSum(s);
-			if (lane == 0) sh[v] = s;
+			t[v] = warpSum(s);
+		}
+		if (lane == 0) {
+			fin(t);
+#pragma unroll
+			for (int v = 0; v < NOUT; v++) sh[v] = t[v];
 		}
 	}
 	__syncthreads();
 #pragma unroll
-	for (int v = 0; v < NV; v++) out[v] = sh[v];
+	for (int v = 0; v < NOUT; v++) out[v] = sh[v];
 	__syncthreads();
 }
 
-// Inner PCG over vectors of type V with operator (A_V = diag - Σ w·neighbour):
-//   solve A e = rhs, e starts at 0.  Dot products in FP64.  Returns matvecs;
-//   `rr`/`rhsNorm2` of the final iterate in *outRR/*outB2.
+struct NoFin { __device__ void operator()(double *) const {} };
+
+// Inner PCG over vectors of type V with the operator A_V = diag - Σ w·neighbour:
+//   solve A e = rhs, e starts at 0.  Element-wise arithmetic is in V (FP32 in the
+//   mixed form); each thread's partial dot product is promoted to FP64 and the
+//   block and grid reductions run in FP64 in a fixed order; α and β are formed
+//   in FP64 once per block.  Returns the number of matvecs; the final |r|^2 and
+//   |rhs|^2 are left in *outRR / *outB2.
 template <int NB, typename V>
-__device__ int pcgCore(const CgArgs &a, int n, const V *w, const V *dg, const double *invd, const V *rhsV, const double *rhsD,
+__device__ int pcgCore(const CgArgs &a, int n, const V *w, const V *dg, const V *invd, const double *rhsD,
                        V *x, V *r, V *z, V *p0, V *p1, V *q, double tolRel, int maxIter, double *sh, double *outRR, double *outB2, bool *ok) {
 	const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x, nthr = int64_t(gridDim.x) * blockDim.x;
-	double acc[2] = {0, 0};
+	V acc0 = V(0), acc1 = V(0);
 	for (int64_t i = tid; i < n; i += nthr) {
-		const double bi = rhsD ? rhsD[i] : double(rhsV[i]);
-		const V bv = V(bi);
+		const V bv = V(rhsD[i]);
 		x[i] = V(0);
 		r[i] = bv;
-		const V zi = V(double(bv) * invd[i]);
+		const V zi = bv * invd[i];
 		z[i] = zi;
 		p0[i] = zi;
-		acc[0] += double(bv) * double(bv);
-		acc[1] += double(bv) * double(zi);
+		acc0 = fma(bv, bv, acc0);
+		acc1 = fma(bv, zi, acc1);
 	}
-	blockPartials<2>(acc, a.partials, a.maxBlocks, sh);
+	{
+		double acc[2] = {double(acc0), double(acc1)};
+		blockPartials<2>(acc, a.partials, a.maxBlocks, sh);
+	}
 	if (!gridSync(a.bar, a.err)) { *ok = false; return 0; }
 	double tot[2];
-	gridTotals<2>(a.partials, a.maxBlocks, tot, sh);
+	gridTotals<2, 2>(a.partials, a.maxBlocks, tot, sh, NoFin{});
 	const double rhsNorm2 = tot[0];
 	double rz = tot[1];
 	*outB2 = rhsNorm2;
@@ -258,53 +276,55 @@ __device__ int pcgCore(const CgArgs &a, int n, const V *w, const V *dg, const do
 
 	V *pc = p0, *po = p1;
 	bool first = true;
-	double beta = 0;
+	V beta = V(0);
 	int it = 0;
 	while (it < maxIter) {
 		// Phase A: p' = z + beta p (first: p' = p0), q = A p', partial p'·q
-		double pq = 0;
+		V pq = V(0);
 		for (int64_t i = tid; i < n; i += nthr) {
-			const V pi = first ? ldcg(pc + i) : V(fma(V(beta), ldcg(pc + i), ldcg(z + i)));
+			const V pi = first ? ldcg(pc + i) : fma(beta, ldcg(pc + i), ldcg(z + i));
 			if (!first) po[i] = pi;
 			V qi = dg[i] * pi;
 #pragma unroll
 			for (int k = 0; k < NB; k++) {
 				const int nb = a.nbr[k * a.stride + i];
 				if (nb >= 0) {
-					const V pn = first ? ldcg(pc + nb) : V(fma(V(beta), ldcg(pc + nb), ldcg(z + nb)));
-					qi -= w[k * a.stride + i] * pn;
+					const V pn = first ? ldcg(pc + nb) : fma(beta, ldcg(pc + nb), ldcg(z + nb));
+					qi = fma(-w[k * a.stride + i], pn, qi);
 				}
 			}
 			q[i] = qi;
-			pq += double(pi) * double(qi);
+			pq = fma(pi, qi, pq);
 		}
 		if (!first) { V *t = pc; pc = po; po = t; }
 		first = false;
-		double acc1[1] = {pq};
+		double acc1[1] = {double(pq)};
 		blockPartials<1>(acc1, a.partials, a.maxBlocks, sh);
 		if (!gridSync(a.bar, a.err)) { *ok = false; return it; }
 		double t1[1];
-		gridTotals<1>(a.partials, a.maxBlocks, t1, sh);
-		const double alpha = rz / t1[0];
+		const double rzc = rz;
+		gridTotals<1, 1>(a.partials, a.maxBlocks, t1, sh, [rzc](double *t) { t[0] = rzc / t[0]; });  // α = rz / p·q
+		const V alpha = V(t1[0]);
 		// Phase B: x += alpha p; r -= alpha q; z = M^-1 r; partial r·r, r·z
-		double a2[2] = {0, 0};
+		V rr = V(0), rzn = V(0);
 		for (int64_t i = tid; i < n; i += nthr) {
-			x[i] = V(double(x[i]) + alpha * double(ldcg(pc + i)));
-			const V ri = V(double(r[i]) - alpha * double(q[i]));
+			x[i] = fma(alpha, ldcg(pc + i), x[i]);
+			const V ri = fma(-alpha, q[i], r[i]);
 			r[i] = ri;
-			const V zi = V(double(ri) * invd[i]);
+			const V zi = ri * invd[i];
 			z[i] = zi;
-			a2[0] += double(ri) * double(ri);
-			a2[1] += double(ri) * double(zi);
+			rr = fma(ri, ri, rr);
+			rzn = fma(ri, zi, rzn);
 		}
+		double a2[2] = {double(rr), double(rzn)};
 		blockPartials<2>(a2, a.partials, a.maxBlocks, sh);
 		if (!gridSync(a.bar, a.err)) { *ok = false; return it + 1; }
-		double t2[2];
-		gridTotals<2>(a.partials, a.maxBlocks, t2, sh);
+		double t2[3];
+		gridTotals<2, 3>(a.partials, a.maxBlocks, t2, sh, [rzc](double *u) { u[2] = u[1] / rzc; });  // β = rz_new / rz
 		it++;
 		*outRR = t2[0];
 		if (t2[0] < threshold) break;
-		beta = t2[1] / rz;
+		beta = V(t2[2]);
 		rz = t2[1];
 	}
 	return it;
@@ -313,11 +333,11 @@ __device__ int pcgCore(const CgArgs &a, int n, const V *w, const V *dg, const do
 // FP64 form: one PCG on the FP64 operator.
 template <int NB>
 __global__ void __launch_bounds__(kCgBlock) kPcgFp64(CgArgs a) {
-	__shared__ double sh[64];
+	__shared__ double sh[2 * 32];
 	const int n = *a.nDev;
 	double rr = 0, b2 = 0;
 	bool ok = true;
-	const int mv = pcgCore<NB, double>(a, n, a.w, a.diag, a.invd, nullptr, a.b, a.x, a.r, a.z, a.p0, a.p1, a.q, a.tol, a.maxIter, sh, &rr, &b2, &ok);
+	const int mv = pcgCore<NB, double>(a, n, a.w, a.diag, a.invd, a.b, a.x, a.r, a.z, a.p0, a.p1, a.q, a.tol, a.maxIter, sh, &rr, &b2, &ok);
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		a.ints[0] = mv;
 		a.ints[1] = 1;
@@ -356,14 +376,14 @@ __global__ void __launch_bounds__(kCgBlock) kPcgMixed(CgArgs a) {
 		blockPartials<2>(acc, a.partials, a.maxBlocks, sh);
 		if (!gridSync(a.bar, a.err)) break;
 		double t[2];
-		gridTotals<2>(a.partials, a.maxBlocks, t, sh);
+		gridTotals<2, 2>(a.partials, a.maxBlocks, t, sh, NoFin{});
 		if (t[0] == 0) { relres = 0; break; }
 		tolUsed = fmax(a.tol, DBL_EPSILON / sqrt(t[0]));
 		relres = sqrt(t[1] / t[0]);
 		if (relres <= tolUsed || sweeps >= a.maxRefine) break;
 		double rr = 0, b2 = 0;
 		bool ok = true;
-		mvTotal += pcgCore<NB, float>(a, n, a.w32, a.diag32, a.invd, nullptr, a.r, a.fe, a.fr, a.fz, a.fp0, a.fp1, a.fq, a.innerTol, a.maxIter, sh, &rr, &b2, &ok);
+		mvTotal += pcgCore<NB, float>(a, n, a.w32, a.diag32, a.invd32, a.r, a.fe, a.fr, a.fz, a.fp0, a.fp1, a.fq, a.innerTol, a.maxIter, sh, &rr, &b2, &ok);
 		if (!ok) break;
 		for (int64_t i = tid; i < n; i += nthr) a.x[i] += double(a.fe[i]);
 		sweeps++;
@@ -421,7 +441,7 @@ garm_status project(State &s, garm_step_stats *st) {
 	for (int a = 0; a < 3; a++) { bio.fr[a] = (const T *)s.fraction[a]; bio.u[a] = (const T *)s.u[a]; bio.bv[a] = (const T *)s.bvel[a]; }
 	bio.grid2mat = s.grid2mat;
 	bio.nbr = s.nbr; bio.wts = s.wts; bio.diag = s.diag; bio.invd = s.invd; bio.rhs = s.rhs;
-	bio.wts32 = s.mixed ? s.wts32 : nullptr; bio.diag32 = s.mixed ? s.diag32 : nullptr;
+	bio.wts32 = s.mixed ? s.wts32 : nullptr; bio.diag32 = s.mixed ? s.diag32 : nullptr; bio.invd32 = s.mixed ? s.invd32 : nullptr;
 	bio.stride = s.N;
 	kBuildSystem<D, T><<<nbC, kBlock, 0, s.stream>>>(s.geom, bio); s.launches++;
 	GARM_CHECK_LAUNCH();
@@ -429,7 +449,7 @@ garm_status project(State &s, garm_step_stats *st) {
 	CgArgs a{};
 	a.nDev = s.nUnknownsDev;
 	a.nbr = s.nbr; a.w = s.wts; a.diag = s.diag; a.invd = s.invd;
-	a.w32 = s.wts32; a.diag32 = s.diag32;
+	a.w32 = s.wts32; a.diag32 = s.diag32; a.invd32 = s.invd32;
 	a.stride = s.N;
 	a.b = s.rhs;
 	a.x = s.pres; a.r = s.cgR; a.z = s.cgZ; a.p0 = s.cgP0; a.p1 = s.cgP1; a.q = s.cgQ;
@@ -450,7 +470,8 @@ garm_status project(State &s, garm_step_stats *st) {
 	int perSM = 0;
 	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kfn, kCgBlock, 0);
 	if (e != cudaSuccess || perSM <= 0) return GARM_CUDA_ERROR;
-	int blocks = s.numSMs * (perSM < 2 ? perSM : 2);
+	int blocks = s.numSMs;  // one resident block per SM (occupancy permitting)
+	if (perSM < 1) return GARM_CUDA_ERROR;
 	if (blocks > s.maxBlocks) blocks = s.maxBlocks;
 	void *args[] = {&a};
 	e = cudaLaunchCooperativeKernel(kfn, dim3(blocks), dim3(kCgBlock), args, 0, s.stream);
