@@ -262,3 +262,17 @@ def test_mixed_precision_within_1e3_dx(oracle_mod, garm_lib, capsys, name):
     assert sg["status"] == capi.OK
     assert sg["cg_residual"] <= 1e-8
     assert ephi <= 1e-3
+
+
+def test_not_converged_is_reported_not_fatal(oracle_mod, garm_lib):
+    """cg_max_iters = 1: the reference would exit (LinearSystem.h:33-36); here the step
+    completes and reports GARM_NOT_CONVERGED, like the oracle."""
+    sc = scenes.drop(16, seed=1)
+    g, o = pair(oracle_mod, sc, cg_max_iters=1)
+    assert g.initialize() == capi.NOT_CONVERGED
+    assert o.initialize() == capi.NOT_CONVERGED
+    g.stage("restart"); o.stage("restart")
+    sg, so = g.advance(0.01), o.advance(0.01)
+    assert sg["status"] == capi.NOT_CONVERGED and so["status"] == capi.NOT_CONVERGED
+    assert sg["cg_iterations"] == 1 and so["cg_iterations"] == 1
+    assert np.all(np.isfinite(g.download(capi.FIELD_VELOCITY)))

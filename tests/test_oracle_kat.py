@@ -165,3 +165,10 @@ def test_dam_break_steps_are_deterministic_and_bounded(oracle_mod):
     oracle_mod.set_threads(0)
     assert np.array_equal(res[0], res[1])  # fixed-order reductions: thread-count independent
     assert np.all(np.isfinite(res[0]))
+
+
+def test_oracle_reports_not_converged(oracle_mod):
+    sc = scenes.drop(12, seed=2)
+    o = oracle_mod.OracleSim(sc.grid, host_default_config(cg_max_iters=1))
+    load_scene(o, sc)
+    assert o.initialize() == capi.NOT_CONVERGED
