@@ -97,7 +97,10 @@ _SIGS = {
     "garm_stage_enforce_bc": (C.c_int, [C.c_void_p]),
     "garm_stage_enforce_boundary_level_set": (C.c_int, [C.c_void_p, C.c_double]),
     "garm_reinit_host": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int, C.c_double, C.c_int]),
+    "garm_reinit_device_noalloc": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.c_double, C.c_void_p, C.c_int, C.c_double, C.c_void_p]),
 }
+
+NOALLOC_MAX_CELLS = 1 << 19
 
 _LIB = None
 

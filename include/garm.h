@@ -168,6 +168,25 @@ garm_status garm_stage_enforce_boundary_level_set(garm_sim *sim, double toleranc
  * `size` has `dim` entries; `phi` is updated in place. */
 garm_status garm_reinit_host(int dim, const int *size, double spacing, double *phi, int iters, double cfl, int precision);
 
+/* WENO5 reinitialisation of a cell field that is already in device memory, for
+ * callers that may not allocate device memory: a plug-in whose host application
+ * owns all GPU memory, or a real-time loop that cannot afford the implicit
+ * synchronisation of cudaMalloc/cudaFree.  This entry point has no counterpart in
+ * the reference; it runs the same kernels as garm_reinit_host.
+ *
+ * `phi` is a device pointer to size[0]*...*size[dim-1] doubles (x fastest),
+ * updated in place on `stream` (a cudaStream_t; NULL = legacy default stream).
+ * It calls no cudaMalloc, cudaFree or allocating library routine: its two stage
+ * planes live in one fixed device array of 2*GARM_NOALLOC_MAX_CELLS doubles
+ * (8 MiB), held by every GPU that loads the library until the process exits.
+ * Grids of more than GARM_NOALLOC_MAX_CELLS cells return GARM_INVALID.
+ * The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call before
+ * any stream capture.  All calls share the one array, so calls whose work
+ * overlaps on the GPU race; the array needs no clearing between calls. */
+#define GARM_NOALLOC_MAX_CELLS (1 << 19)
+garm_status garm_reinit_device_noalloc(int dim, const int *size, double spacing, double *phi, int iters, double cfl, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
