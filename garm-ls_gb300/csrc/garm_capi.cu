@@ -107,30 +107,24 @@ garm_status allocState(State &s) {
 	GARM_TRY(dalloc(s, &s.mat2grid, N * 4));
 	GARM_TRY(dalloc(s, &s.scanBlock, size_t(gridFor(s.N)) * 4 + 64));
 	GARM_TRY(dalloc(s, &s.nUnknownsDev, 64));
-	GARM_TRY(dalloc(s, &s.nbr, N * 4 * 2 * D));
-	GARM_TRY(dalloc(s, &s.wts, N * 8 * 2 * D));
+	GARM_TRY(dalloc(s, &s.ent64, N * 16 * 2 * D));
 	GARM_TRY(dalloc(s, &s.diag, N * 8));
 	GARM_TRY(dalloc(s, &s.invd, N * 8));
 	GARM_TRY(dalloc(s, &s.rhs, N * 8));
 	GARM_TRY(dalloc(s, &s.pres, N * 8));
 	GARM_TRY(dalloc(s, &s.cgR, N * 8));
+	GARM_TRY(dalloc(s, &s.cgPack[0], N * 4 * e));
+	GARM_TRY(dalloc(s, &s.cgPack[1], N * 4 * e));
 	if (!s.mixed) {
-		GARM_TRY(dalloc(s, &s.cgZ, N * 8));
-		GARM_TRY(dalloc(s, &s.cgP0, N * 8));
-		GARM_TRY(dalloc(s, &s.cgP1, N * 8));
-		GARM_TRY(dalloc(s, &s.cgQ, N * 8));
+		GARM_TRY(dalloc(s, &s.cgP64, N * 8));
 	} else {
-		GARM_TRY(dalloc(s, &s.wts32, N * 4 * 2 * D));
+		GARM_TRY(dalloc(s, &s.ent32, N * 8 * 2 * D));
 		GARM_TRY(dalloc(s, &s.diag32, N * 4));
 		GARM_TRY(dalloc(s, &s.invd32, N * 4));
-		GARM_TRY(dalloc(s, &s.fR, N * 4));
-		GARM_TRY(dalloc(s, &s.fZ, N * 4));
-		GARM_TRY(dalloc(s, &s.fP0, N * 4));
-		GARM_TRY(dalloc(s, &s.fP1, N * 4));
-		GARM_TRY(dalloc(s, &s.fQ, N * 4));
-		GARM_TRY(dalloc(s, &s.fE, N * 4));
+		GARM_TRY(dalloc(s, &s.cgP32, N * 4));
+		GARM_TRY(dalloc(s, &s.cgE32, N * 4));
 	}
-	s.maxBlocks = s.numSMs;
+	s.maxBlocks = s.numSMs * 2;
 	GARM_TRY(dalloc(s, &s.partials, size_t(s.maxBlocks) * 4 * 8));
 	GARM_TRY(dalloc(s, &s.barrier, 64));
 	GARM_TRY(dalloc(s, &s.cgScalars, 64));

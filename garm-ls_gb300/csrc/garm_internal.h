@@ -56,13 +56,17 @@ struct State {
 	int *scanBlock = nullptr;  // per-block counts for the compaction scan
 	int *nUnknownsDev = nullptr;
 	int nUnknowns = 0;
-	int *nbr = nullptr;        // [2D][N] neighbour unknown id, -1 if none
-	double *wts = nullptr;     // [2D][N] off-diagonal weights (positive w; matrix entry is -w)
+	void *ent64 = nullptr;      // [2D][N] {neighbour unknown id (-1: none), weight w}, matrix entry -w (FP64)
+	void *ent32 = nullptr;      // the same entries with FP32 weights (mixed)
 	double *diag = nullptr, *invd = nullptr, *rhs = nullptr, *pres = nullptr;
-	float *wts32 = nullptr, *diag32 = nullptr, *invd32 = nullptr;
-	// PCG work vectors (FP64) and the FP32 inner vectors of the mixed form
-	double *cgX = nullptr, *cgR = nullptr, *cgZ = nullptr, *cgP0 = nullptr, *cgP1 = nullptr, *cgQ = nullptr;
-	float *fR = nullptr, *fZ = nullptr, *fP0 = nullptr, *fP1 = nullptr, *fQ = nullptr, *fE = nullptr;
+	float *diag32 = nullptr, *invd32 = nullptr;
+	// PCG work vectors: packed {r, w, s, 1/diag} per unknown (double-buffered, in the
+	// solve's element type), the search direction, the mixed form's FP32 correction
+	// and its FP64 refinement residual cgR
+	double *cgR = nullptr;
+	void *cgPack[2] = {};
+	double *cgP64 = nullptr;
+	float *cgP32 = nullptr, *cgE32 = nullptr;
 	double *partials = nullptr; int maxBlocks = 0;
 	unsigned *barrier = nullptr;   // [count, generation]
 	double *cgScalars = nullptr;   // device-side scalars written by the persistent solver

@@ -14,7 +14,8 @@
 namespace garm {
 
 constexpr int kCgBlock = 512;
-constexpr unsigned long long kBarrierSpinLimit = 20000000ull;  // x ~100 ns sleep: ~2 s, then GARM_TIMEOUT
+constexpr int kRegUnknowns = 4;  // unknowns per thread held in registers by the PCG
+constexpr unsigned long long kBarrierSpinLimit = 200000000ull;  // acquire polls (~2 s), then GARM_TIMEOUT
 
 // ---------------------------------------------------------------------------
 // unknown set and numbering
@@ -76,6 +77,11 @@ __global__ void __launch_bounds__(kBlock) kScatterUnknowns(int64_t N, const int 
 	}
 }
 
+// One off-diagonal entry: neighbour unknown id (-1: none) and weight w (the
+// matrix entry is -w), stored [k][unknown] so a warp reads one coalesced record.
+struct __align__(16) NbW64 { int nb; int pad; double w; };
+struct __align__(8) NbW32 { int nb; float w; };
+
 // ---------------------------------------------------------------------------
 // rows of the ghost-fluid Poisson matrix
 // ---------------------------------------------------------------------------
@@ -86,9 +92,10 @@ struct BuildIO {
 	const T *u[3];
 	const T *bv[3];
 	const int *grid2mat;
-	int *nbr;
-	double *wts, *diag, *invd, *rhs;
-	float *wts32, *diag32, *invd32;
+	NbW64 *ent;
+	double *diag, *invd, *rhs;
+	NbW32 *ent32;
+	float *diag32, *invd32;
 	int64_t stride;
 };
 
@@ -124,9 +131,8 @@ __global__ void __launch_bounds__(kBlock) kBuildSystem(Geom geom, BuildIO<D, T> 
 			div += side * w * double(io.u[a][fid]);
 		}
 		if (w < 1) div += side * (1 - w) * double(io.bv[a][fid]);
-		io.nbr[q * io.stride + r] = nb;
-		io.wts[q * io.stride + r] = wt;
-		if (io.wts32) io.wts32[q * io.stride + r] = float(wt);
+		io.ent[q * io.stride + r] = NbW64{nb, 0, wt};
+		if (io.ent32) io.ent32[q * io.stride + r] = NbW32{nb, float(wt)};
 	}
 	io.rhs[r] = div;
 	io.diag[r] = dg;
@@ -139,13 +145,18 @@ __global__ void __launch_bounds__(kBlock) kBuildSystem(Geom geom, BuildIO<D, T> 
 // ---------------------------------------------------------------------------
 struct CgArgs {
 	const int *nDev;
-	const int *nbr;
-	const double *w, *diag, *invd;
-	const float *w32, *diag32, *invd32;
+	const NbW64 *ent;
+	const double *diag, *invd;
+	const NbW32 *ent32;
+	const float *diag32, *invd32;
 	int64_t stride;
 	const double *b;
-	double *x, *r, *z, *p0, *p1, *q;
-	float *fr, *fz, *fp0, *fp1, *fq, *fe;
+	double *x;       // FP64 solution (pressure)
+	double *r64;     // FP64 residual of the refinement loop (mixed)
+	double *p64;          // FP64 form: search direction
+	void *pack64[2];      // FP64 form: {r, w, s, 1/diag} per unknown, double-buffered
+	float *e32, *p32;     // mixed inner solve: correction and search direction
+	void *pack32[2];      // mixed inner solve: {r, w, s, 1/diag} in FP32
 	double *partials;
 	int maxBlocks;
 	unsigned *bar;
@@ -164,27 +175,32 @@ struct CgArgs {
 __device__ __forceinline__ double ldcg(const double *p) { return *p; }
 __device__ __forceinline__ float ldcg(const float *p) { return *p; }
 
-// Grid-wide barrier with a bounded wait.  Returns false when any block gave up.
-__device__ bool gridSync(unsigned *bar, int *err) {
+__device__ __forceinline__ unsigned ldAcquire(const unsigned *ptr) {
+	unsigned v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ptr) : "memory");
+	return v;
+}
+__device__ __forceinline__ void addRelease(unsigned *ptr, unsigned v) {
+	asm volatile("red.release.gpu.global.add.u32 [%0], %1;" :: "l"(ptr), "r"(v) : "memory");
+}
+
+// Grid-wide barrier with a bounded wait.  Each block adds 1 to a counter with
+// release semantics once its threads have passed __syncthreads; a block waits
+// (acquire loads) until the counter reaches gridDim.x times the number of
+// barriers passed so far.  The spin is capped: past the cap the block sets the
+// error flag and every block leaves at its next barrier.  Returns false then.
+__device__ bool gridSync(unsigned *bar, int *err, unsigned &epoch) {
 	__syncthreads();
 	if (threadIdx.x == 0) {
-		volatile unsigned *vgen = bar + 1;
-		const unsigned gen = *vgen;
-		__threadfence();
-		const unsigned prev = atomicAdd(bar, 1u);
-		if (prev == gridDim.x - 1) {
-			atomicExch(bar, 0u);
-			__threadfence();
-			atomicAdd(bar + 1, 1u);
-		} else {
-			unsigned long long spins = 0;
-			while (*vgen == gen) {
-				__nanosleep(100);
-				if (++spins > kBarrierSpinLimit) { atomicExch(err, 1); break; }
+		epoch += gridDim.x;
+		addRelease(bar, 1u);
+		unsigned long long spins = 0;
+		while (ldAcquire(bar) < epoch) {
+			if ((++spins & 1023ull) == 0) {
 				if (*(volatile int *)err) break;
+				if (spins > kBarrierSpinLimit) { atomicExch(err, 1); break; }
 			}
 		}
-		__threadfence();
 	}
 	__syncthreads();
 	return *(volatile int *)err == 0;
@@ -197,12 +213,12 @@ __device__ __forceinline__ void blockPartials(double (&acc)[NV], double *partial
 #pragma unroll
 	for (int v = 0; v < NV; v++) {
 		double x = warpSum(acc[v]);
-		if (lane == 0) sh[v * 32 + w] = x;
+		if (lane == 0) sh[v * 16 + w] = x;
 	}
 	__syncthreads();
 	if (threadIdx.x < NV) {
 		double s = 0;
-		for (int q = 0; q < (int)(blockDim.x >> 5); q++) s += sh[threadIdx.x * 32 + q];
+		for (int q = 0; q < (int)(blockDim.x >> 5); q++) s += sh[threadIdx.x * 16 + q];
 		partials[threadIdx.x * maxBlocks + blockIdx.x] = s;
 	}
 	__syncthreads();
@@ -237,36 +253,67 @@ __device__ __forceinline__ void gridTotals(const double *partials, int maxBlocks
 
 struct NoFin { __device__ void operator()(double *) const {} };
 
-// Inner PCG over vectors of type V with the operator A_V = diag - Σ w·neighbour:
-//   solve A e = rhs, e starts at 0.  Element-wise arithmetic is in V (FP32 in the
-//   mixed form); each thread's partial dot product is promoted to FP64 and the
-//   block and grid reductions run in FP64 in a fixed order; α and β are formed
-//   in FP64 once per block.  Returns the number of matvecs; the final |r|^2 and
-//   |rhs|^2 are left in *outRR / *outB2.
+__device__ __forceinline__ double mulRn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mulRn(float a, float b) { return __fmul_rn(a, b); }
+
+// Per-unknown solver state gathered by neighbours: residual r, w = A M^-1 r,
+// s = A p and the Jacobi scale 1/diag, packed so one gather touches one sector.
+template <typename V> struct Pack;
+template <> struct __align__(16) Pack<float> { float r, w, s, d; };
+template <> struct __align__(32) Pack<double> { double r, w, s, d; };
+
+// Preconditioned CG in the Chronopoulos–Gear arrangement (one global reduction
+// per iteration), solving A e = rhs from e = 0 with the Jacobi preconditioner.
+// Mathematically it is the PCG of LinearSystem.h:23-39 (Eigen's algorithm, the
+// same stopping rule |r|^2 < max(tol^2 |b|^2, DBL_MIN), tol = max(tol, eps/|b|)):
+//     u = M^-1 r, w = A u,  γ = r·u,  δ = w·u,
+//     β = γ/γ_old, α = γ / (δ - β γ / α_old),
+//     p = u + β p,  s = w + β s,  x += α p,  r -= α s.
+// One iteration is one fused phase plus one grid barrier: a thread updates its
+// own unknowns and recomputes, from last iteration's {r, w, s} of its
+// neighbours, their new u (the same fma/mul sequence as the owner, so
+// bit-identical), which gives w_new = A u_new without a second barrier.  The
+// packed state is double-buffered.  Element arithmetic is in V; per-thread
+// partial dots are promoted to FP64 and reduced in a fixed order; α and β are
+// formed in FP64 (uniformly in every block).  Returns the number of matvecs.
+template <typename V> struct EntOf;
+template <> struct EntOf<double> { using T = NbW64; };
+template <> struct EntOf<float> { using T = NbW32; };
+
 template <int NB, typename V>
-__device__ int pcgCore(const CgArgs &a, int n, const V *w, const V *dg, const V *invd, const double *rhsD,
-                       V *x, V *r, V *z, V *p0, V *p1, V *q, double tolRel, int maxIter, double *sh, double *outRR, double *outB2, bool *ok) {
+__device__ int pcgCore(const CgArgs &a, int n, const typename EntOf<V>::T *__restrict__ ent, const V *__restrict__ dg, const V *__restrict__ invd, const double *rhsD,
+                       V *__restrict__ x, V *__restrict__ p, Pack<V> *st0, Pack<V> *st1, double tolRel, int maxIter, double *sh, unsigned &epoch,
+                       double *outRR, double *outB2, bool *ok) {
 	const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x, nthr = int64_t(gridDim.x) * blockDim.x;
-	V acc0 = V(0), acc1 = V(0);
+	const int64_t S = a.stride;
+	Pack<V> *stb[2] = {st0, st1};
+	// set-up: x = 0, r = b, s = 0, p = 0, w = A M^-1 b; partial r·u, w·u, r·r
+	V acc0 = V(0), acc1 = V(0), acc2 = V(0);
 	for (int64_t i = tid; i < n; i += nthr) {
-		const V bv = V(rhsD[i]);
-		x[i] = V(0);
-		r[i] = bv;
-		const V zi = bv * invd[i];
-		z[i] = zi;
-		p0[i] = zi;
-		acc0 = fma(bv, bv, acc0);
-		acc1 = fma(bv, zi, acc1);
+		const V bi = V(rhsD[i]), di = invd[i];
+		const V ui = mulRn(bi, di);
+		V wi = dg[i] * ui;
+#pragma unroll
+		for (int k = 0; k < NB; k++) {
+			const auto e = ent[k * S + i];
+			if (e.nb >= 0) wi = fma(-V(e.w), mulRn(V(rhsD[e.nb]), invd[e.nb]), wi);
+		}
+		x[i] = V(0); p[i] = V(0);
+		st0[i] = Pack<V>{bi, wi, V(0), di};
+		acc0 = fma(bi, ui, acc0);
+		acc1 = fma(wi, ui, acc1);
+		acc2 = fma(bi, bi, acc2);
 	}
 	{
-		double acc[2] = {double(acc0), double(acc1)};
-		blockPartials<2>(acc, a.partials, a.maxBlocks, sh);
+		double acc[3] = {double(acc0), double(acc1), double(acc2)};
+		blockPartials<3>(acc, a.partials, a.maxBlocks, sh);
 	}
-	if (!gridSync(a.bar, a.err)) { *ok = false; return 0; }
-	double tot[2];
-	gridTotals<2, 2>(a.partials, a.maxBlocks, tot, sh, NoFin{});
-	const double rhsNorm2 = tot[0];
-	double rz = tot[1];
+	if (!gridSync(a.bar, a.err, epoch)) { *ok = false; return 0; }
+	// totals γ, δ, |r|^2, then (lane 0 only) β = 0 and α = γ/δ for the first iteration
+	double tot[5];
+	gridTotals<3, 5>(a.partials, a.maxBlocks, tot, sh, [](double *t) { t[3] = 0; t[4] = t[0] / t[1]; });
+	double gamma = tot[0];
+	const double rhsNorm2 = tot[2];
 	*outB2 = rhsNorm2;
 	*outRR = rhsNorm2;
 	if (rhsNorm2 == 0) return 0;
@@ -274,58 +321,130 @@ __device__ int pcgCore(const CgArgs &a, int n, const V *w, const V *dg, const V 
 	const double threshold = fmax(tol * tol * rhsNorm2, DBL_MIN);
 	if (rhsNorm2 < threshold) return 0;
 
-	V *pc = p0, *po = p1;
-	bool first = true;
-	V beta = V(0);
-	int it = 0;
+	int cur = 0, it = 0;
+	if (n <= kRegUnknowns * nthr) {
+		// Register-resident path: each thread owns at most kRegUnknowns unknowns and
+		// keeps their neighbour entries, diagonal, p, x and packed state in registers
+		// for the whole solve; an iteration is the neighbour gathers, one packed store
+		// per unknown, the reduction and one barrier.
+		using E = typename EntOf<V>::T;
+		E en[kRegUnknowns][NB];
+		V dgi[kRegUnknowns], pp[kRegUnknowns], xx[kRegUnknowns];
+		Pack<V> me[kRegUnknowns];
+		bool own[kRegUnknowns];
+#pragma unroll
+		for (int c = 0; c < kRegUnknowns; c++) {
+			const int64_t i = tid + c * nthr;
+			own[c] = i < n;
+			pp[c] = V(0); xx[c] = V(0);
+			if (own[c]) {
+				dgi[c] = dg[i];
+				me[c] = st0[i];
+#pragma unroll
+				for (int k = 0; k < NB; k++) en[c][k] = ent[k * S + i];
+			} else {
+				dgi[c] = V(0);
+				me[c] = Pack<V>{V(0), V(0), V(0), V(0)};
+#pragma unroll
+				for (int k = 0; k < NB; k++) { en[c][k] = E{}; en[c][k].nb = -1; }
+			}
+		}
+		while (it < maxIter) {
+			const double alpha = tot[4];
+			const V bV = V(tot[3]), aV = V(alpha);
+			const Pack<V> *__restrict__ sc = stb[cur];
+			Pack<V> *__restrict__ sn = stb[cur ^ 1];
+			V g = V(0), d = V(0), rr = V(0);
+#pragma unroll
+			for (int c = 0; c < kRegUnknowns; c++) {
+				if (!own[c]) continue;
+				const V ui = mulRn(me[c].r, me[c].d);
+				const V pi = fma(bV, pp[c], ui);
+				const V si = fma(bV, me[c].s, me[c].w);
+				const V rni = fma(-aV, si, me[c].r);
+				const V uni = mulRn(rni, me[c].d);
+				V wni = dgi[c] * uni;
+#pragma unroll
+				for (int k = 0; k < NB; k++) {
+					if (en[c][k].nb >= 0) {
+						const Pack<V> q = sc[en[c][k].nb];
+						const V snb = fma(bV, q.s, q.w);
+						const V rnb = fma(-aV, snb, q.r);
+						wni = fma(-V(en[c][k].w), mulRn(rnb, q.d), wni);
+					}
+				}
+				pp[c] = pi;
+				xx[c] = fma(aV, pi, xx[c]);
+				me[c] = Pack<V>{rni, wni, si, me[c].d};
+				sn[tid + c * nthr] = me[c];
+				g = fma(rni, uni, g);
+				d = fma(wni, uni, d);
+				rr = fma(rni, rni, rr);
+			}
+			cur ^= 1;
+			double acc[3] = {double(g), double(d), double(rr)};
+			blockPartials<3>(acc, a.partials, a.maxBlocks, sh);
+			if (!gridSync(a.bar, a.err, epoch)) { *ok = false; it++; break; }
+			const double gOld = gamma;
+			gridTotals<3, 5>(a.partials, a.maxBlocks, tot, sh, [gOld, alpha](double *t) {
+				t[3] = t[0] / gOld;
+				t[4] = t[0] / (t[1] - t[3] * t[0] / alpha);
+			});
+			it++;
+			*outRR = tot[2];
+			if (tot[2] < threshold) break;
+			gamma = tot[0];
+		}
+#pragma unroll
+		for (int c = 0; c < kRegUnknowns; c++)
+			if (own[c]) x[tid + c * nthr] = xx[c];
+		return it;
+	}
 	while (it < maxIter) {
-		// Phase A: p' = z + beta p (first: p' = p0), q = A p', partial p'·q
-		V pq = V(0);
+		const double alpha = tot[4];
+		const V bV = V(tot[3]), aV = V(alpha);
+		const Pack<V> *__restrict__ sc = stb[cur];
+		Pack<V> *__restrict__ sn = stb[cur ^ 1];
+		V g = V(0), d = V(0), rr = V(0);
 		for (int64_t i = tid; i < n; i += nthr) {
-			const V pi = first ? ldcg(pc + i) : fma(beta, ldcg(pc + i), ldcg(z + i));
-			if (!first) po[i] = pi;
-			V qi = dg[i] * pi;
+			const Pack<V> me = sc[i];
+			const V ui = mulRn(me.r, me.d);
+			const V pi = fma(bV, p[i], ui);
+			const V si = fma(bV, me.s, me.w);
+			const V rni = fma(-aV, si, me.r);
+			const V uni = mulRn(rni, me.d);
+			V wni = dg[i] * uni;
 #pragma unroll
 			for (int k = 0; k < NB; k++) {
-				const int nb = a.nbr[k * a.stride + i];
-				if (nb >= 0) {
-					const V pn = first ? ldcg(pc + nb) : fma(beta, ldcg(pc + nb), ldcg(z + nb));
-					qi = fma(-w[k * a.stride + i], pn, qi);
+				const auto e = ent[k * S + i];
+				if (e.nb >= 0) {
+					const Pack<V> q = sc[e.nb];
+					const V snb = fma(bV, q.s, q.w);
+					const V rnb = fma(-aV, snb, q.r);
+					wni = fma(-V(e.w), mulRn(rnb, q.d), wni);
 				}
 			}
-			q[i] = qi;
-			pq = fma(pi, qi, pq);
+			p[i] = pi;
+			x[i] = fma(aV, pi, x[i]);
+			sn[i] = Pack<V>{rni, wni, si, me.d};
+			g = fma(rni, uni, g);
+			d = fma(wni, uni, d);
+			rr = fma(rni, rni, rr);
 		}
-		if (!first) { V *t = pc; pc = po; po = t; }
-		first = false;
-		double acc1[1] = {double(pq)};
-		blockPartials<1>(acc1, a.partials, a.maxBlocks, sh);
-		if (!gridSync(a.bar, a.err)) { *ok = false; return it; }
-		double t1[1];
-		const double rzc = rz;
-		gridTotals<1, 1>(a.partials, a.maxBlocks, t1, sh, [rzc](double *t) { t[0] = rzc / t[0]; });  // α = rz / p·q
-		const V alpha = V(t1[0]);
-		// Phase B: x += alpha p; r -= alpha q; z = M^-1 r; partial r·r, r·z
-		V rr = V(0), rzn = V(0);
-		for (int64_t i = tid; i < n; i += nthr) {
-			x[i] = fma(alpha, ldcg(pc + i), x[i]);
-			const V ri = fma(-alpha, q[i], r[i]);
-			r[i] = ri;
-			const V zi = ri * invd[i];
-			z[i] = zi;
-			rr = fma(ri, ri, rr);
-			rzn = fma(ri, zi, rzn);
-		}
-		double a2[2] = {double(rr), double(rzn)};
-		blockPartials<2>(a2, a.partials, a.maxBlocks, sh);
-		if (!gridSync(a.bar, a.err)) { *ok = false; return it + 1; }
-		double t2[3];
-		gridTotals<2, 3>(a.partials, a.maxBlocks, t2, sh, [rzc](double *u) { u[2] = u[1] / rzc; });  // β = rz_new / rz
+		cur ^= 1;
+		double acc[3] = {double(g), double(d), double(rr)};
+		blockPartials<3>(acc, a.partials, a.maxBlocks, sh);
+		if (!gridSync(a.bar, a.err, epoch)) { *ok = false; return it + 1; }
+		// lane 0: β = γ_new/γ, α = γ_new / (δ_new - β γ_new / α_old); broadcast to the block
+		const double gOld = gamma;
+		gridTotals<3, 5>(a.partials, a.maxBlocks, tot, sh, [gOld, alpha](double *t) {
+			t[3] = t[0] / gOld;
+			t[4] = t[0] / (t[1] - t[3] * t[0] / alpha);
+		});
 		it++;
-		*outRR = t2[0];
-		if (t2[0] < threshold) break;
-		beta = V(t2[2]);
-		rz = t2[1];
+		*outRR = tot[2];
+		if (tot[2] < threshold) break;
+		gamma = tot[0];
 	}
 	return it;
 }
@@ -333,11 +452,12 @@ __device__ int pcgCore(const CgArgs &a, int n, const V *w, const V *dg, const V 
 // FP64 form: one PCG on the FP64 operator.
 template <int NB>
 __global__ void __launch_bounds__(kCgBlock) kPcgFp64(CgArgs a) {
-	__shared__ double sh[2 * 32];
+	__shared__ double sh[3 * 16];
 	const int n = *a.nDev;
 	double rr = 0, b2 = 0;
 	bool ok = true;
-	const int mv = pcgCore<NB, double>(a, n, a.w, a.diag, a.invd, a.b, a.x, a.r, a.z, a.p0, a.p1, a.q, a.tol, a.maxIter, sh, &rr, &b2, &ok);
+	unsigned epoch = 0;
+	const int mv = pcgCore<NB, double>(a, n, a.ent, a.diag, a.invd, a.b, a.x, a.p64, (Pack<double> *)a.pack64[0], (Pack<double> *)a.pack64[1], a.tol, a.maxIter, sh, epoch, &rr, &b2, &ok);
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		a.ints[0] = mv;
 		a.ints[1] = 1;
@@ -348,33 +468,35 @@ __global__ void __launch_bounds__(kCgBlock) kPcgFp64(CgArgs a) {
 
 // Mixed form: FP64 iterative refinement around FP32 inner PCG sweeps.
 //   x64 = 0; repeat: r64 = b - A64 x64 (FP64); stop when |r64| <= tol |b|;
-//   solve A32 e = r64 (FP32 vectors, FP64 dots) to innerTol; x64 += e.
+//   solve A32 e = r64 (FP32 vectors, FP64 reductions) to innerTol; x64 += e.
 template <int NB>
 __global__ void __launch_bounds__(kCgBlock) kPcgMixed(CgArgs a) {
-	__shared__ double sh[64];
+	__shared__ double sh[3 * 32];
 	const int n = *a.nDev;
 	const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x, nthr = int64_t(gridDim.x) * blockDim.x;
+	unsigned epoch = 0;
 	for (int64_t i = tid; i < n; i += nthr) a.x[i] = 0;
 	int mvTotal = 0, sweeps = 0;
 	double relres = 0, tolUsed = a.tol;
-	for (;;) {
+	const bool alive = gridSync(a.bar, a.err, epoch);  // x = 0 everywhere before the first residual
+	while (alive) {
 		// r64 = b - A64 x64 and |b|^2, |r64|^2 in FP64
 		double acc[2] = {0, 0};
 		for (int64_t i = tid; i < n; i += nthr) {
-			double ax = a.diag[i] * ldcg(a.x + i);
+			double ax = a.diag[i] * a.x[i];
 #pragma unroll
 			for (int k = 0; k < NB; k++) {
-				const int nb = a.nbr[k * a.stride + i];
-				if (nb >= 0) ax -= a.w[k * a.stride + i] * ldcg(a.x + nb);
+				const NbW64 e = a.ent[k * a.stride + i];
+				if (e.nb >= 0) ax -= e.w * a.x[e.nb];
 			}
 			const double bi = a.b[i];
 			const double ri = bi - ax;
-			a.r[i] = ri;
+			a.r64[i] = ri;
 			acc[0] += bi * bi;
 			acc[1] += ri * ri;
 		}
 		blockPartials<2>(acc, a.partials, a.maxBlocks, sh);
-		if (!gridSync(a.bar, a.err)) break;
+		if (!gridSync(a.bar, a.err, epoch)) break;
 		double t[2];
 		gridTotals<2, 2>(a.partials, a.maxBlocks, t, sh, NoFin{});
 		if (t[0] == 0) { relres = 0; break; }
@@ -383,11 +505,11 @@ __global__ void __launch_bounds__(kCgBlock) kPcgMixed(CgArgs a) {
 		if (relres <= tolUsed || sweeps >= a.maxRefine) break;
 		double rr = 0, b2 = 0;
 		bool ok = true;
-		mvTotal += pcgCore<NB, float>(a, n, a.w32, a.diag32, a.invd32, a.r, a.fe, a.fr, a.fz, a.fp0, a.fp1, a.fq, a.innerTol, a.maxIter, sh, &rr, &b2, &ok);
+		mvTotal += pcgCore<NB, float>(a, n, a.ent32, a.diag32, a.invd32, a.r64, a.e32, a.p32, (Pack<float> *)a.pack32[0], (Pack<float> *)a.pack32[1], a.innerTol, a.maxIter, sh, epoch, &rr, &b2, &ok);
 		if (!ok) break;
-		for (int64_t i = tid; i < n; i += nthr) a.x[i] += double(a.fe[i]);
+		for (int64_t i = tid; i < n; i += nthr) a.x[i] += double(a.e32[i]);
 		sweeps++;
-		if (!gridSync(a.bar, a.err)) break;
+		if (!gridSync(a.bar, a.err, epoch)) break;
 	}
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		a.ints[0] = mvTotal;
@@ -440,20 +562,22 @@ garm_status project(State &s, garm_step_stats *st) {
 	bio.phi = (const T *)s.phi;
 	for (int a = 0; a < 3; a++) { bio.fr[a] = (const T *)s.fraction[a]; bio.u[a] = (const T *)s.u[a]; bio.bv[a] = (const T *)s.bvel[a]; }
 	bio.grid2mat = s.grid2mat;
-	bio.nbr = s.nbr; bio.wts = s.wts; bio.diag = s.diag; bio.invd = s.invd; bio.rhs = s.rhs;
-	bio.wts32 = s.mixed ? s.wts32 : nullptr; bio.diag32 = s.mixed ? s.diag32 : nullptr; bio.invd32 = s.mixed ? s.invd32 : nullptr;
+	bio.ent = (NbW64 *)s.ent64; bio.diag = s.diag; bio.invd = s.invd; bio.rhs = s.rhs;
+	bio.ent32 = s.mixed ? (NbW32 *)s.ent32 : nullptr; bio.diag32 = s.mixed ? s.diag32 : nullptr; bio.invd32 = s.mixed ? s.invd32 : nullptr;
 	bio.stride = s.N;
 	kBuildSystem<D, T><<<nbC, kBlock, 0, s.stream>>>(s.geom, bio); s.launches++;
 	GARM_CHECK_LAUNCH();
 
 	CgArgs a{};
 	a.nDev = s.nUnknownsDev;
-	a.nbr = s.nbr; a.w = s.wts; a.diag = s.diag; a.invd = s.invd;
-	a.w32 = s.wts32; a.diag32 = s.diag32; a.invd32 = s.invd32;
+	a.ent = (const NbW64 *)s.ent64; a.diag = s.diag; a.invd = s.invd;
+	a.ent32 = (const NbW32 *)s.ent32; a.diag32 = s.diag32; a.invd32 = s.invd32;
 	a.stride = s.N;
 	a.b = s.rhs;
-	a.x = s.pres; a.r = s.cgR; a.z = s.cgZ; a.p0 = s.cgP0; a.p1 = s.cgP1; a.q = s.cgQ;
-	a.fr = s.fR; a.fz = s.fZ; a.fp0 = s.fP0; a.fp1 = s.fP1; a.fq = s.fQ; a.fe = s.fE;
+	a.x = s.pres;
+	a.r64 = s.cgR;
+	a.p64 = s.cgP64; a.pack64[0] = s.cgPack[0]; a.pack64[1] = s.cgPack[1];
+	a.e32 = s.cgE32; a.p32 = s.cgP32; a.pack32[0] = s.cgPack[0]; a.pack32[1] = s.cgPack[1];
 	a.partials = s.partials; a.maxBlocks = s.maxBlocks;
 	a.bar = s.barrier; a.err = s.cgInts + 4;
 	a.tol = s.cfg.cg_tolerance; a.maxIter = s.cfg.cg_max_iters;
@@ -470,8 +594,9 @@ garm_status project(State &s, garm_step_stats *st) {
 	int perSM = 0;
 	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kfn, kCgBlock, 0);
 	if (e != cudaSuccess || perSM <= 0) return GARM_CUDA_ERROR;
-	int blocks = s.numSMs;  // one resident block per SM (occupancy permitting)
-	if (perSM < 1) return GARM_CUDA_ERROR;
+	// one resident 512-thread block per SM; the cooperative launch verifies co-residency
+	int blocks = s.numSMs;
+	if (blocks > s.maxBlocks) blocks = s.maxBlocks;
 	if (blocks > s.maxBlocks) blocks = s.maxBlocks;
 	void *args[] = {&a};
 	e = cudaLaunchCooperativeKernel(kfn, dim3(blocks), dim3(kCgBlock), args, 0, s.stream);
