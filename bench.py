@@ -140,6 +140,18 @@ def state_fields():
             capi.FIELD_REF_LEVEL_SET_GRAD, capi.FIELD_ADV_REGION]
 
 
+def profiled_traffic(name: str, n: int):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of one ncu
+    capture summarised under profiles/, when it was taken on this workload size."""
+    p = REPO / "profiles" / name
+    if n != 128 or not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        if ln.startswith("traffic_bytes_per_launch:"):
+            return int(ln.split(":")[1])
+    return None
+
+
 def reinit_roofline(sim, torch, stream, n_cells: int, esz: int, iters: int, peaks: dict) -> dict:
     """Time the WENO5 reinitialisation stage alone with CUDA events on the sim's stream
     and express its algorithmic bytes per launch against the measured HBM peak."""
@@ -234,6 +246,8 @@ def run_garm(args) -> None:
     }
     if rank == 0:
         out["roofline"] = reinit_roofline(sim, torch, stream, int(scene.phi.size), 8 if args.precision == "fp64" else 4, 30, peaks)
+        out["roofline"]["traffic"] = profiled_traffic(
+            "reinit_stage_fp64_dam_break_128.txt" if args.precision == "fp64" else "reinit_stage_f32_dam_break_128.txt", n)
 
     # end to end through the C ABI with host buffers: upload the step's input state
     # from pinned memory, advance, download the state and the level set
@@ -280,19 +294,23 @@ def run_garm(args) -> None:
         barrier(world)
         torch.cuda.synchronize()
         m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        mms = []
+        mms, mcg = [], []
         m0.record(stream)
         for _ in range(K):
-            mms.append(mix.advance(next(g2))["ms_total"])
+            st = mix.advance(next(g2))
+            mms.append(st["ms_total"])
+            mcg.append(st["cg_iterations"])
         m1.record(stream)
         torch.cuda.synchronize()
         mix_ms = reduce_max(m0.elapsed_time(m1), world)
         mval = world * interior * K / (mix_ms * 1e-3)
         out["mixed"] = {"value": mval, "unit": UNIT, "ms_per_step": mix_ms / K, "p50_step_ms": statistics.median(mms),
                         "p99_step_ms": float(np.percentile(mms, 99)), "phi_err_dx_band3dx_after_1_step_vs_fp64": phi_err_band, "phi_err_dx_all_cells_after_1_step_vs_fp64": phi_err,
-                        "speedup_vs_fp64": mval / value, "dtype": "f32 storage+math, f64 dots/residual/refinement/RM test"}
+                        "speedup_vs_fp64": mval / value, "cg_iterations_mean": statistics.mean(mcg),
+                        "dtype": "f32 storage+math, f64 dots/residual/refinement/RM test"}
         if rank == 0:
             out["mixed"]["roofline"] = reinit_roofline(mix, torch, stream, int(scene.phi.size), 4, 30, peaks)
+            out["mixed"]["roofline"]["traffic"] = profiled_traffic("reinit_stage_f32_dam_break_128.txt", n)
         mix.close()
 
     # CPU baseline: the oracle (a CPU port of the reference's FP64 path) on this host,
