@@ -39,7 +39,8 @@ template <int D, typename T>
 struct OutPlanes { T *p[12]; };
 
 template <int D, typename T>
-__global__ void __launch_bounds__(kBlock) kMixedVec(Geom geom, Planes<D, T> grad, OutPlanes<D, T> mixed, int ncomp) {
+__global__ void __launch_bounds__(kBlock) kMixedVec(Geom geom, Planes<D, T> grad, OutPlanes<D, T> mixed, int ncomp, const int *gate) {
+	if (gate && !*gate) return;
 	const G<D, T> g = cellGrid<D, T>(geom);
 	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
 	if (id >= g.count()) return;
@@ -99,7 +100,8 @@ struct RefMapIO {
 };
 
 template <int D, typename T>
-__global__ void __launch_bounds__(kBlock) kAdvectRefMap(Geom geom, VelView<D, T> vv, RefMapIO<D, T> io, T mdt) {
+__global__ void __launch_bounds__(kBlock) kAdvectRefMap(Geom geom, VelView<D, T> vv, RefMapIO<D, T> io, const double *dtp) {
+	const T mdt = T(-*dtp);
 	const G<D, T> g = cellGrid<D, T>(geom);
 	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
 	if (id >= g.count()) return;
@@ -232,7 +234,8 @@ __global__ void __launch_bounds__(kBlock) kAdvectRefMap(Geom geom, VelView<D, T>
 
 // ---- 4. velocity advection: RK2 trace with trilinear u, cubic Lagrange sample of u_axis
 template <int D, typename T>
-__global__ void __launch_bounds__(kBlock) kAdvectVelocity(Geom geom, VelView<D, T> vv, T *o0, T *o1, T *o2, int64_t F0, int64_t F1, int64_t Ftot, T mdt) {
+__global__ void __launch_bounds__(kBlock) kAdvectVelocity(Geom geom, VelView<D, T> vv, T *o0, T *o1, T *o2, int64_t F0, int64_t F1, int64_t Ftot, const double *dtp) {
+	const T mdt = T(-*dtp);
 	int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
 	if (id >= Ftot) return;
 	int axis = 0;
@@ -307,7 +310,7 @@ static VelView<D, T> makeVelView(State &s) {
 }
 
 template <int D, typename T>
-garm_status advectFields(State &s, double dt) {
+garm_status advectFields(State &s) {
 	const int64_t F0 = s.F[0], F1 = s.F[1];
 	// 1. ∇u
 	kVelocityGrad<D, T><<<gridFor(s.Ftot), kBlock, 0, s.stream>>>(s.geom, (const T *)s.u[0], (const T *)s.u[1], (const T *)s.u[2],
@@ -319,7 +322,7 @@ garm_status advectFields(State &s, double dt) {
 	for (int q = 0; q < D * D; q++) pg.p[q] = (const T *)s.Pi[q];
 	OutPlanes<D, T> mo{};
 	for (int q = 0; q < 12; q++) mo.p[q] = (T *)s.xiMixed[q];
-	kMixedVec<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, pg, mo, D); s.launches++;
+	kMixedVec<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, pg, mo, D, nullptr); s.launches++;
 	GARM_CHECK_LAUNCH();
 	// 3. ξ, Π
 	VelView<D, T> vv = makeVelView<D, T>(s);
@@ -327,10 +330,10 @@ garm_status advectFields(State &s, double dt) {
 	for (int c = 0; c < D; c++) { io.xi[c] = (const T *)s.xi[c]; io.xiOut[c] = (T *)s.xiNew[c]; }
 	for (int q = 0; q < D * D; q++) { io.Pi[q] = (const T *)s.Pi[q]; io.PiOut[q] = (T *)s.PiNew[q]; }
 	for (int q = 0; q < 12; q++) io.mixed[q] = (const T *)s.xiMixed[q];
-	kAdvectRefMap<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, vv, io, T(-dt)); s.launches++;
+	kAdvectRefMap<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, vv, io, s.dtDev); s.launches++;
 	GARM_CHECK_LAUNCH();
 	// 4. u (reads the old velocity for every axis: Advection.h:15-22)
-	kAdvectVelocity<D, T><<<gridFor(s.Ftot), kBlock, 0, s.stream>>>(s.geom, vv, (T *)s.uNew[0], (T *)s.uNew[1], (T *)s.uNew[2], F0, F1, s.Ftot, T(-dt)); s.launches++;
+	kAdvectVelocity<D, T><<<gridFor(s.Ftot), kBlock, 0, s.stream>>>(s.geom, vv, (T *)s.uNew[0], (T *)s.uNew[1], (T *)s.uNew[2], F0, F1, s.Ftot, s.dtDev); s.launches++;
 	GARM_CHECK_LAUNCH();
 	for (int c = 0; c < D; c++) { void *t = s.xi[c]; s.xi[c] = s.xiNew[c]; s.xiNew[c] = t; }
 	for (int q = 0; q < D * D; q++) { void *t = s.Pi[q]; s.Pi[q] = s.PiNew[q]; s.PiNew[q] = t; }
@@ -345,13 +348,13 @@ garm_status resetRefView(State &s) {
 	for (int a = 0; a < D; a++) pg.p[a] = (const T *)s.refGrad[a];
 	OutPlanes<D, T> mo{};
 	for (int q = 0; q < 4; q++) mo.p[q] = (T *)s.refMixed[q];
-	kMixedVec<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, pg, mo, 1); s.launches++;
+	kMixedVec<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, pg, mo, 1, s.gate); s.launches++;
 	GARM_CHECK_LAUNCH();
 	return GARM_OK;
 }
 
 #define GARM_INST(D, T) \
-	template garm_status advectFields<D, T>(State &, double); \
+	template garm_status advectFields<D, T>(State &); \
 	template garm_status resetRefView<D, T>(State &);
 GARM_INST(2, double)
 GARM_INST(3, double)

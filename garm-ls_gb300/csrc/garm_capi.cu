@@ -33,6 +33,14 @@ __global__ void kInterleave(double *dst, int ncomp, int64_t n, const T *d0, cons
 	for (int c = 0; c < ncomp; c++) dst[i * ncomp + c] = double(d[c][i]);
 }
 
+__global__ void kSetScalar(double *p, double v) { *p = v; }
+__global__ void kSetClock(double *clock, double frameLength, double cfl) { clock[0] = 0; clock[1] = frameLength; clock[2] = cfl; }
+__global__ void kBeginStep(unsigned long long *counter, double *stats) {
+	const unsigned long long c = ++*counter;
+	double *rec = stats + ((c + kStatsCap - 1) % kStatsCap) * kStatsSlots;
+	for (int q = 0; q < kStatsSlots; q++) rec[q] = 0;
+}
+
 __global__ void kPressureToCells(int64_t N, const int *grid2mat, const double *p, double *out) {
 	const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
 	if (i >= N) return;
@@ -58,7 +66,11 @@ garm_status dalloc(State &s, P **p, size_t bytes) {
 	return r;
 }
 
+void dropGraphs(State &s);
+
 void freeAll(State &s) {
+	for (auto &g : s.stepGraph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+	if (s.statsHost) { cudaFreeHost(s.statsHost); s.statsHost = nullptr; }
 	for (int i = 0; i < s.nAllocs; i++) cudaFree(s.allocs[i]);
 	s.nAllocs = 0;
 	for (auto &e : s.ev) if (e) { cudaEventDestroy(e); e = nullptr; }
@@ -131,6 +143,12 @@ garm_status allocState(State &s) {
 	GARM_TRY(dalloc(s, &s.cgInts, 64));
 	GARM_TRY(dalloc(s, &s.redU64, 64));
 	GARM_TRY(dalloc(s, &s.redI32, 64));
+	GARM_TRY(dalloc(s, &s.dtDev, 64));
+	GARM_TRY(dalloc(s, &s.clockDev, 64));
+	GARM_TRY(dalloc(s, &s.restartFlag, 64));
+	GARM_TRY(dalloc(s, &s.stepCounter, 64));
+	GARM_TRY(dalloc(s, &s.statsDev, size_t(kStatsCap) * kStatsSlots * 8));
+	if (cudaMallocHost(&s.statsHost, size_t(kStatsCap) * kStatsSlots * 8) != cudaSuccess) { cudaGetLastError(); s.statsHost = nullptr; return GARM_OOM; }
 	// staging: the largest .sav field (Π: D*D doubles per cell)
 	size_t big = N * 8 * size_t(D * D);
 	if (size_t(s.Ftot) * 8 > big) big = size_t(s.Ftot) * 8;
@@ -271,6 +289,7 @@ garm_status download(State &s, int field, void *host, size_t bytes) {
 
 // LevelSetLiquid::initialize (LevelSetLiquid.cpp:528-598)
 garm_status initialize(State &s) {
+	dropGraphs(s);  // boundary work lists are baked into captured steps
 	GARM_TRY(GARM_DISPATCH(s, finishBoundary, s));                       // _boundary.finish
 	GARM_TRY(GARM_DISPATCH(s, enforceBoundaryLevelSet, s, s.phi, 0.0));  // enforceBoundaryLevelSet(_levelSet)
 	GARM_TRY(GARM_DISPATCH(s, reinitialize, s));                         // reinitializeLevelSet
@@ -291,38 +310,90 @@ garm_status initialize(State &s) {
 
 garm_status record(State &s, int i) { return cudaEventRecord(s.ev[i], s.stream) == cudaSuccess ? GARM_OK : GARM_CUDA_ERROR; }
 
-// LevelSetLiquid::advance (LevelSetLiquid.cpp:608-698)
+// Enqueue one LevelSetLiquid::advance (LevelSetLiquid.cpp:608-698) with dt already in
+// s.dtDev.  No host synchronisation: the reference-map decision is a device flag
+// that gates the restart branch, and statistics go to the step's device record.
+// `timed` records the stage events (not allowed inside a graph capture).
+garm_status enqueueStep(State &s, bool timed) {
+	if (timed) GARM_TRY(record(s, 0));
+	GARM_TRY(GARM_DISPATCH(s, advectFields, s));
+	if (timed) GARM_TRY(record(s, 1));
+	GARM_TRY(GARM_DISPATCH(s, generateCurrentFields, s));
+	if (timed) GARM_TRY(record(s, 2));
+	const bool doReinit = s.cfg.reinit_interval <= 1 || (s.stepIndex % s.cfg.reinit_interval) == 0;
+	if (doReinit) GARM_TRY(GARM_DISPATCH(s, reinitialize, s));
+	if (timed) GARM_TRY(record(s, 3));
+	GARM_TRY(GARM_DISPATCH(s, extrapolateToCollider, s));
+	if (timed) GARM_TRY(record(s, 4));
+	GARM_TRY(GARM_DISPATCH(s, checkReferenceMapAsync, s, true));
+	s.gate = s.restartFlag;  // restart(); generateCurrentFields(); extrapolateFieldsToCollider()  (:631-640)
+	garm_status r = GARM_DISPATCH(s, restart, s);
+	if (r == GARM_OK) r = GARM_DISPATCH(s, generateCurrentFields, s);
+	if (r == GARM_OK) r = GARM_DISPATCH(s, extrapolateToCollider, s);
+	s.gate = nullptr;
+	GARM_TRY(r);
+	if (timed) GARM_TRY(record(s, 5));
+	GARM_TRY(GARM_DISPATCH(s, bodyForce, s));
+	if (timed) GARM_TRY(record(s, 6));
+	GARM_TRY(GARM_DISPATCH(s, projectAsync, s, true));
+	if (timed) GARM_TRY(record(s, 7));
+	GARM_TRY(GARM_DISPATCH(s, extrapolateToAir, s));
+	GARM_TRY(GARM_DISPATCH(s, enforceBoundaryConditions, s));
+	if (timed) GARM_TRY(record(s, 8));
+	s.stepIndex++;
+	return GARM_OK;
+}
+
+garm_status beginStep(State &s) {
+	kBeginStep<<<1, 1, 0, s.stream>>>(s.stepCounter, s.statsDev); s.launches++;
+	s.hostSteps++;
+	GARM_CHECK_LAUNCH();
+	return GARM_OK;
+}
+
+// dt of the step computed on the device from max|u| and the frame clock.
+garm_status enqueueAutoDt(State &s) {
+	GARM_TRY(GARM_DISPATCH(s, maxSpeedAsync, s));
+	kStepDt<<<1, 1, 0, s.stream>>>(s.redU64, s.geom.dx, s.clockDev, s.dtDev, s.statsDev, s.stepCounter); s.launches++;
+	GARM_CHECK_LAUNCH();
+	return GARM_OK;
+}
+
+// Read the records of the last `k` steps into stats (the last step's record).
+garm_status readRecords(State &s, int k, garm_step_stats *S) {
+	if (cudaMemcpyAsync(s.statsHost, s.statsDev, size_t(kStatsCap) * kStatsSlots * 8, cudaMemcpyDeviceToHost, s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
+	if (cudaStreamSynchronize(s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
+	garm_status worst = GARM_OK;
+	for (int q = 0; q < k; q++) {
+		const double *rec = s.statsHost + ((s.hostSteps - 1 - q + kStatsCap) % kStatsCap) * kStatsSlots;
+		if (rec[kStCgErr] != 0) return GARM_TIMEOUT;
+		if (rec[kStUnknowns] > 0 && !(rec[kStCgResidual] <= rec[kStCgTol])) worst = GARM_NOT_CONVERGED;
+	}
+	if (S) {
+		const double *rec = s.statsHost + ((s.hostSteps - 1 + kStatsCap) % kStatsCap) * kStatsSlots;
+		S->restarted = int(rec[kStRestarted]);
+		S->rm_total = int(rec[kStRmTotal]);
+		S->rm_bad = int(rec[kStRmBad]);
+		S->unknowns = int(rec[kStUnknowns]);
+		S->cg_iterations = int(rec[kStCgIters]);
+		S->cg_refinements = int(rec[kStCgRefine]);
+		S->cg_residual = rec[kStCgResidual];
+		s.nUnknowns = S->unknowns;
+	}
+	return worst;
+}
+
+// LevelSetLiquid::advance (LevelSetLiquid.cpp:608-698) with a host-given dt.
 garm_status advance(State &s, double dt, garm_step_stats *st) {
 	garm_step_stats local{};
 	garm_step_stats &S = st ? *st : local;
 	std::memset(&S, 0, sizeof(S));
-	GARM_TRY(record(s, 0));
-	GARM_TRY(GARM_DISPATCH(s, advectFields, s, dt));
-	GARM_TRY(record(s, 1));
-	GARM_TRY(GARM_DISPATCH(s, generateCurrentFields, s));
-	GARM_TRY(record(s, 2));
-	const bool doReinit = s.cfg.reinit_interval <= 1 || (s.stepIndex % s.cfg.reinit_interval) == 0;
-	if (doReinit) GARM_TRY(GARM_DISPATCH(s, reinitialize, s));
-	GARM_TRY(record(s, 3));
-	GARM_TRY(GARM_DISPATCH(s, extrapolateToCollider, s));
-	GARM_TRY(record(s, 4));
-	int keep = 1, tot = 0, bad = 0;
-	GARM_TRY(GARM_DISPATCH(s, checkReferenceMap, s, &keep, &tot, &bad));
-	if (!keep) {
-		GARM_TRY(GARM_DISPATCH(s, restart, s));
-		GARM_TRY(GARM_DISPATCH(s, generateCurrentFields, s));
-		GARM_TRY(GARM_DISPATCH(s, extrapolateToCollider, s));
-	}
-	GARM_TRY(record(s, 5));
-	GARM_TRY(GARM_DISPATCH(s, bodyForce, s, dt));
-	GARM_TRY(record(s, 6));
-	const garm_status pr = GARM_DISPATCH(s, project, s, &S);
+	GARM_TRY(beginStep(s));
+	kSetScalar<<<1, 1, 0, s.stream>>>(s.dtDev, dt); s.launches++;
+	GARM_CHECK_LAUNCH();
+	GARM_TRY(enqueueStep(s, true));
+	const garm_status pr = readRecords(s, 1, &S);
 	if (pr != GARM_OK && pr != GARM_NOT_CONVERGED) return pr;
-	GARM_TRY(record(s, 7));
-	GARM_TRY(GARM_DISPATCH(s, extrapolateToAir, s));
-	GARM_TRY(GARM_DISPATCH(s, enforceBoundaryConditions, s));
-	GARM_TRY(record(s, 8));
-	GARM_TRY(sync(s));
 	float ms = 0;
 	for (int i = 0; i < 8; i++) {
 		cudaEventElapsedTime(&ms, s.ev[i], s.ev[i + 1]);
@@ -330,10 +401,102 @@ garm_status advance(State &s, double dt, garm_step_stats *st) {
 	}
 	cudaEventElapsedTime(&ms, s.ev[0], s.ev[8]);
 	S.ms_total = ms;
-	S.restarted = keep ? 0 : 1;
-	S.rm_total = tot;
-	S.rm_bad = bad;
-	s.stepIndex++;
+	return pr;
+}
+
+struct BufferRoles {
+	void *u[3], *uNew[3], *xi[3], *xiNew[3], *Pi[9], *PiNew[9];
+};
+BufferRoles saveRoles(const State &s) {
+	BufferRoles b;
+	for (int a = 0; a < 3; a++) { b.u[a] = s.u[a]; b.uNew[a] = s.uNew[a]; b.xi[a] = s.xi[a]; b.xiNew[a] = s.xiNew[a]; }
+	for (int q = 0; q < 9; q++) { b.Pi[q] = s.Pi[q]; b.PiNew[q] = s.PiNew[q]; }
+	return b;
+}
+void restoreRoles(State &s, const BufferRoles &b) {
+	for (int a = 0; a < 3; a++) { s.u[a] = b.u[a]; s.uNew[a] = b.uNew[a]; s.xi[a] = b.xi[a]; s.xiNew[a] = b.xiNew[a]; }
+	for (int q = 0; q < 9; q++) { s.Pi[q] = b.Pi[q]; s.PiNew[q] = b.PiNew[q]; }
+}
+void swapRoles(State &s) {
+	for (int a = 0; a < 3; a++) { std::swap(s.u[a], s.uNew[a]); std::swap(s.xi[a], s.xiNew[a]); }
+	for (int q = 0; q < 9; q++) std::swap(s.Pi[q], s.PiNew[q]);
+}
+
+void dropGraphs(State &s) {
+	for (auto &g : s.stepGraph) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+	s.graphTried = false;
+	s.graphOk = false;
+}
+
+// Capture the two single-step graphs (even and odd step: the advected fields'
+// ping-pong buffers alternate).  If the step cannot be captured (for example a
+// cooperative launch refused in capture) the buffer roles are restored and the
+// steps run as direct launches instead.
+garm_status buildStepGraphs(State &s) {
+	dropGraphs(s);
+	s.graphTried = true;
+	if (s.cfg.reinit_interval > 1) return GARM_OK;  // the captured step always reinitialises
+	const BufferRoles even = saveRoles(s);
+	s.evenU0 = s.u[0];
+	for (int g = 0; g < 2; g++) {
+		cudaGraph_t graph = nullptr;
+		const long long launches = s.launches;
+		const long long stepIndex = s.stepIndex;
+		garm_status r = GARM_OK;
+		if (cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) r = GARM_CUDA_ERROR;
+		else {
+			kBeginStep<<<1, 1, 0, s.stream>>>(s.stepCounter, s.statsDev);
+			s.launches++;
+			if (cudaGetLastError() != cudaSuccess) r = GARM_CUDA_ERROR;
+			if (r == GARM_OK) r = enqueueAutoDt(s);
+			if (r == GARM_OK) r = enqueueStep(s, false);
+			if (cudaStreamEndCapture(s.stream, &graph) != cudaSuccess) r = GARM_CUDA_ERROR;
+		}
+		s.graphLaunches = s.launches - launches;
+		s.launches = launches;
+		s.stepIndex = stepIndex;
+		if (r == GARM_OK && graph && cudaGraphInstantiate(&s.stepGraph[g], graph, 0) != cudaSuccess) r = GARM_CUDA_ERROR;
+		if (graph) cudaGraphDestroy(graph);
+		if (r != GARM_OK) {
+			cudaGetLastError();
+			restoreRoles(s, even);
+			dropGraphs(s);
+			s.graphTried = true;
+			return GARM_OK;
+		}
+	}
+	restoreRoles(s, even);  // two captured steps swapped the roles twice
+	s.graphOk = true;
+	return GARM_OK;
+}
+
+// `steps` steps with dt from the device (Simulator::advanceTimeBySteps policy).
+garm_status advanceAuto(State &s, int steps, garm_step_stats *st) {
+	if (!s.graphTried) GARM_TRY(buildStepGraphs(s));
+	GARM_TRY(record(s, 0));
+	for (int k = 0; k < steps; k++) {
+		if (s.graphOk) {
+			// graph 0 was captured with the buffer roles of s.evenU0, graph 1 with the swapped ones
+			const int parity = (s.u[0] == s.evenU0) ? 0 : 1;
+			if (cudaGraphLaunch(s.stepGraph[parity], s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
+			s.hostSteps++;
+			s.stepIndex++;
+			s.launches += s.graphLaunches;
+			swapRoles(s);  // the host's view follows the graph's alternation
+		} else {
+			GARM_TRY(beginStep(s));
+			GARM_TRY(enqueueAutoDt(s));
+			GARM_TRY(enqueueStep(s, false));
+		}
+	}
+	GARM_TRY(record(s, 8));
+	garm_step_stats local{};
+	garm_step_stats &S = st ? *st : local;
+	std::memset(&S, 0, sizeof(S));
+	const garm_status pr = readRecords(s, steps < kStatsCap ? steps : kStatsCap, &S);
+	float ms = 0;
+	cudaEventElapsedTime(&ms, s.ev[0], s.ev[8]);
+	S.ms_total = ms;
 	return pr;
 }
 
@@ -484,6 +647,7 @@ garm_status garm_sim_initialize(garm_sim *sim) { return sim ? initialize(sim->s)
 garm_status garm_sim_finish_load(garm_sim *sim) {
 	if (!sim) return GARM_INVALID;
 	State &s = sim->s;
+	dropGraphs(s);
 	GARM_TRY(GARM_DISPATCH(s, finishBoundary, s));
 	GARM_TRY(GARM_DISPATCH(s, refreshRefGradient, s));
 	return sync(s);
@@ -492,6 +656,25 @@ garm_status garm_sim_finish_load(garm_sim *sim) {
 garm_status garm_sim_advance(garm_sim *sim, double dt, garm_step_stats *stats) {
 	if (!sim || !std::isfinite(dt) || dt < 0) return GARM_INVALID;
 	return advance(sim->s, dt, stats);
+}
+
+garm_status garm_sim_set_clock(garm_sim *sim, unsigned frame_rate, double cfl) {
+	if (!sim || frame_rate == 0 || !(cfl > 0)) return GARM_INVALID;
+	State &s = sim->s;
+	kSetClock<<<1, 1, 0, s.stream>>>(s.clockDev, 1.0 / frame_rate, cfl); s.launches++;
+	if (cudaGetLastError() != cudaSuccess) return GARM_CUDA_ERROR;
+	return sync(s);
+}
+
+garm_status garm_sim_advance_auto(garm_sim *sim, int steps, garm_step_stats *stats) {
+	if (!sim || steps < 1) return GARM_INVALID;
+	return advanceAuto(sim->s, steps, stats);
+}
+
+garm_status garm_sim_graph_active(const garm_sim *sim, int *active) {
+	if (!sim || !active) return GARM_INVALID;
+	*active = sim->s.graphOk ? 1 : 0;
+	return GARM_OK;
 }
 
 garm_status garm_sim_max_speed(garm_sim *sim, double *out) {
@@ -509,13 +692,21 @@ garm_status garm_sim_time_step(garm_sim *sim, double cfl, double *dt) {
 
 #define STAGE_BODY(expr) do { if (!sim) return GARM_INVALID; State &s = sim->s; garm_status r_ = (expr); if (r_ == GARM_OK || r_ == GARM_NOT_CONVERGED) { garm_status q_ = sync(s); if (q_ != GARM_OK) return q_; } return r_; } while (0)
 
-garm_status garm_stage_advect(garm_sim *sim, double dt) { STAGE_BODY(GARM_DISPATCH(s, advectFields, s, dt)); }
+garm_status garm_stage_advect(garm_sim *sim, double dt) {
+	if (!sim) return GARM_INVALID;
+	kSetScalar<<<1, 1, 0, sim->s.stream>>>(sim->s.dtDev, dt);
+	STAGE_BODY(GARM_DISPATCH(s, advectFields, s));
+}
 garm_status garm_stage_compose(garm_sim *sim) { STAGE_BODY(GARM_DISPATCH(s, generateCurrentFields, s)); }
 garm_status garm_stage_reinit(garm_sim *sim) { STAGE_BODY(GARM_DISPATCH(s, reinitialize, s)); }
 garm_status garm_stage_extrap_collider(garm_sim *sim) { STAGE_BODY(GARM_DISPATCH(s, extrapolateToCollider, s)); }
 garm_status garm_stage_rm_check(garm_sim *sim, int *keep, int *total, int *bad) { STAGE_BODY(GARM_DISPATCH(s, checkReferenceMap, s, keep, total, bad)); }
 garm_status garm_stage_restart(garm_sim *sim) { STAGE_BODY(GARM_DISPATCH(s, restart, s)); }
-garm_status garm_stage_body_force(garm_sim *sim, double dt) { STAGE_BODY(GARM_DISPATCH(s, bodyForce, s, dt)); }
+garm_status garm_stage_body_force(garm_sim *sim, double dt) {
+	if (!sim) return GARM_INVALID;
+	kSetScalar<<<1, 1, 0, sim->s.stream>>>(sim->s.dtDev, dt);
+	STAGE_BODY(GARM_DISPATCH(s, bodyForce, s));
+}
 garm_status garm_stage_project(garm_sim *sim, garm_step_stats *stats) {
 	garm_step_stats local{};
 	garm_step_stats *st = stats ? stats : &local;

@@ -188,7 +188,8 @@ garm_status finishBoundary(State &s) {
 enum FixedKind { kFixedCellDistPos = 0, kFixedAdvPos = 1, kFixedOriNonPos = 2 };
 
 template <typename T>
-__global__ void kCellMask(int64_t N, int kind, const T *cellDist, const uint8_t *adv, const T *ori, uint8_t *vis) {
+__global__ void kCellMask(int64_t N, int kind, const T *cellDist, const uint8_t *adv, const T *ori, uint8_t *vis, const int *gate) {
+	if (gate && !*gate) return;
 	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
 	if (id >= N) return;
 	bool f;
@@ -203,7 +204,8 @@ __global__ void kCellMask(int64_t N, int kind, const T *cellDist, const uint8_t 
 // Kind 2: flag (uchar) (Extrapolation.h:128-174)
 // Neighbours are visited in the reference's order -x,+x,-y,+y,-z,+z (Grid.h:59-60).
 template <int D, typename T, int Kind, int NS>
-__global__ void __launch_bounds__(kBlock) kExtrapCellPass(Geom geom, T *f0, T *f1, T *f2, uint8_t *flag, const uint8_t *__restrict__ vis0, uint8_t *vis1) {
+__global__ void __launch_bounds__(kBlock) kExtrapCellPass(Geom geom, T *f0, T *f1, T *f2, uint8_t *flag, const uint8_t *__restrict__ vis0, uint8_t *vis1, const int *gate) {
+	if (gate && !*gate) return;
 	const int sx = geom.n[0], sy = geom.n[1], sz = D == 3 ? geom.n[2] : 1;
 	const int N = sx * sy * sz;
 	const int id = int(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -306,7 +308,7 @@ template <int D, typename T, int Kind, int NS>
 static garm_status cellExtrap(State &s, T *f0, T *f1, T *f2, uint8_t *flag, int passes) {
 	uint8_t *v0 = s.vis0, *v1 = s.vis1;
 	for (int it = 0; it < passes; it++) {
-		kExtrapCellPass<D, T, Kind, NS><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, f0, f1, f2, flag, v0, v1); s.launches++;
+		kExtrapCellPass<D, T, Kind, NS><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, f0, f1, f2, flag, v0, v1, s.gate); s.launches++;
 		uint8_t *t = v0; v0 = v1; v1 = t;
 	}
 	GARM_CHECK_LAUNCH();
@@ -318,7 +320,7 @@ static inline int passCount(double r) { int n = 0; while (n < r) n++; return n; 
 
 template <int D, typename T>
 garm_status extrapolateToCollider(State &s) {
-	kCellMask<T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, kFixedCellDistPos, (const T *)s.cellDist, s.adv, (const T *)s.ori, s.vis0); s.launches++;
+	kCellMask<T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, kFixedCellDistPos, (const T *)s.cellDist, s.adv, (const T *)s.ori, s.vis0, s.gate); s.launches++;
 	GARM_CHECK_LAUNCH();
 	// ori and φ share the fixed set cellDist > 0, so one pass extrapolates both
 	return cellExtrap<D, T, 0, 2>(s, (T *)s.ori, (T *)s.phi, nullptr, nullptr, passCount(s.cfg.boundary_extrap_radius));
@@ -328,12 +330,12 @@ template <int D, typename T>
 garm_status extrapolateToAir(State &s) {
 	const int R = passCount(s.cfg.air_extrap_radius);
 	// ξ from cells with advRegion > 0
-	kCellMask<T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, kFixedAdvPos, (const T *)s.cellDist, s.adv, (const T *)s.ori, s.vis0); s.launches++;
+	kCellMask<T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, kFixedAdvPos, (const T *)s.cellDist, s.adv, (const T *)s.ori, s.vis0, s.gate); s.launches++;
 	GARM_CHECK_LAUNCH();
 	GARM_TRY((cellExtrap<D, T, 1, 1>(s, (T *)s.xi[0], (T *)s.xi[1], (T *)(D == 3 ? s.xi[2] : nullptr), nullptr, R)));
 	// advRegion = (ori <= 0), then dilate
 	kAdvFromOri<T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, (const T *)s.ori, s.adv); s.launches++;
-	kCellMask<T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, kFixedOriNonPos, (const T *)s.cellDist, s.adv, (const T *)s.ori, s.vis0); s.launches++;
+	kCellMask<T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, kFixedOriNonPos, (const T *)s.cellDist, s.adv, (const T *)s.ori, s.vis0, s.gate); s.launches++;
 	GARM_CHECK_LAUNCH();
 	GARM_TRY((cellExtrap<D, T, 2, 1>(s, nullptr, nullptr, nullptr, s.adv, R)));
 	// velocity, airExtrapolationRadius + 2 passes
@@ -354,15 +356,15 @@ garm_status extrapolateToAir(State &s) {
 // Body force: u_y -= 9.8 dt on every y-face
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void kAddConst(int64_t n, T *u, T v) {
+__global__ void kGravity(int64_t n, T *u, const double *dtp) {
 	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-	if (id < n) u[id] -= v;
+	if (id < n) u[id] -= T(9.8 * *dtp);  // kGravity * dt (Constants.h:9)
 }
 
 template <int D, typename T>
-garm_status bodyForce(State &s, double dt) {
+garm_status bodyForce(State &s) {
 	if (!s.cfg.enable_gravity) return GARM_OK;
-	kAddConst<T><<<gridFor(s.F[1]), kBlock, 0, s.stream>>>(s.F[1], (T *)s.u[1], T(9.8 * dt)); s.launches++;
+	kGravity<T><<<gridFor(s.F[1]), kBlock, 0, s.stream>>>(s.F[1], (T *)s.u[1], s.dtDev); s.launches++;
 	GARM_CHECK_LAUNCH();
 	return GARM_OK;
 }
@@ -453,6 +455,32 @@ __global__ void __launch_bounds__(kBlock) kMaxAbs(const T *u0, const T *u1, cons
 	}
 }
 
+// dt of the next step from max|u| on the device: stepRate*dx/max|u| (LevelSetLiquid.h:129)
+// clamped to the end of the frame and halved when two steps remain (Simulator.cpp:110-117).
+// clock = {time within the frame, frame length, cfl}.
+__global__ void kStepDt(const unsigned long long *maxBits, double dx, double *clock, double *dt, double *stats, const unsigned long long *counter) {
+	double *rec = stepRecord(stats, counter);
+	const double m = __longlong_as_double((long long)*maxBits);
+	const double target = clock[1];
+	double time = clock[0];
+	double d = clock[2] * dx / m;  // +inf at rest, as the reference
+	if (time + d >= target) { d = target - time; time = 0; }
+	else { if (time + 2 * d >= target) d = (target - time) / 2; time += d; }
+	clock[0] = time;
+	*dt = d;
+	if (rec) rec[kStDt] = d;
+}
+
+template <int D, typename T>
+garm_status maxSpeedAsync(State &s) {
+	cudaError_t e = cudaMemsetAsync(s.redU64, 0, sizeof(unsigned long long), s.stream);
+	if (e != cudaSuccess) return GARM_CUDA_ERROR;
+	const unsigned nb = unsigned(s.numSMs > 0 ? s.numSMs * 8 : 1024);
+	kMaxAbs<T><<<nb, kBlock, 0, s.stream>>>((const T *)s.u[0], (const T *)s.u[1], (const T *)(D == 3 ? s.u[2] : s.u[0]), s.F[0], s.F[1], s.Ftot, s.redU64); s.launches++;
+	GARM_CHECK_LAUNCH();
+	return GARM_OK;
+}
+
 template <int D, typename T>
 garm_status maxSpeed(State &s, double *out) {
 	cudaError_t e = cudaMemsetAsync(s.redU64, 0, sizeof(unsigned long long), s.stream);
@@ -489,9 +517,10 @@ garm_status copyField(State &s, void *dst, const void *src, int64_t n) {
 	template garm_status finishBoundary<D, T>(State &); \
 	template garm_status extrapolateToCollider<D, T>(State &); \
 	template garm_status extrapolateToAir<D, T>(State &); \
-	template garm_status bodyForce<D, T>(State &, double); \
+	template garm_status bodyForce<D, T>(State &); \
 	template garm_status enforceBoundaryConditions<D, T>(State &); \
 	template garm_status maxSpeed<D, T>(State &, double *); \
+	template garm_status maxSpeedAsync<D, T>(State &); \
 	template garm_status copyField<D, T>(State &, void *, const void *, int64_t);
 GARM_INST(2, double)
 GARM_INST(3, double)

@@ -80,19 +80,49 @@ struct State {
 	void *allocs[160] = {}; int nAllocs = 0; size_t deviceBytes = 0;
 	// timing events
 	cudaEvent_t ev[10] = {};
+	// device-resident stepping: dt of the current step, the Simulator frame clock
+	// {time in frame, frame length, cfl}, the restart decision (gates the restart
+	// branch when non-null) and per-step statistics written on the device
+	double *dtDev = nullptr;
+	double *clockDev = nullptr;
+	int *restartFlag = nullptr;
+	const int *gate = nullptr;
+	double *statsDev = nullptr;        // kStatsSlots doubles per recorded step
+	unsigned long long *stepCounter = nullptr;  // device count of started steps
+	unsigned long long hostSteps = 0;           // host mirror of the counter
+	double *statsHost = nullptr;       // pinned mirror
+	int statsCap = 0;
+	// captured single-step graphs (even / odd step: the ping-pong buffers alternate)
+	cudaGraphExec_t stepGraph[2] = {nullptr, nullptr};
+	bool graphTried = false, graphOk = false;
+	void *evenU0 = nullptr;            // u[0] buffer of the even-step graph
+	long long graphLaunches = 0;       // kernels in one captured step
 };
+
+// Per-step records live in a device ring indexed by a device step counter, so a
+// captured step graph writes the record of whichever step it is replaying.
+constexpr int kStatsCap = 256;
+__device__ __forceinline__ double *stepRecord(double *base, const unsigned long long *counter) {
+	return base ? base + ((*counter + kStatsCap - 1) % kStatsCap) * 12 : nullptr;
+}
+
+// Layout of one per-step statistics record on the device.
+enum StatSlot { kStDt = 0, kStRestarted, kStRmTotal, kStRmBad, kStUnknowns, kStCgIters, kStCgRefine, kStCgResidual, kStCgTol, kStCgErr, kStatsSlots = 12 };
 
 // Stage entry points (templated on dimension D and working type T).
 template <int D, typename T> garm_status initBoundary(State &s);
 template <int D, typename T> garm_status finishBoundary(State &s);
-template <int D, typename T> garm_status advectFields(State &s, double dt);
+template <int D, typename T> garm_status advectFields(State &s);
 template <int D, typename T> garm_status generateCurrentFields(State &s);
 template <int D, typename T> garm_status reinitialize(State &s);
 template <int D, typename T> garm_status extrapolateToCollider(State &s);
 template <int D, typename T> garm_status checkReferenceMap(State &s, int *keep, int *tot, int *bad);
+template <int D, typename T> garm_status checkReferenceMapAsync(State &s, bool record);
 template <int D, typename T> garm_status restart(State &s);
-template <int D, typename T> garm_status bodyForce(State &s, double dt);
+template <int D, typename T> garm_status bodyForce(State &s);
 template <int D, typename T> garm_status project(State &s, garm_step_stats *st);
+template <int D, typename T> garm_status projectAsync(State &s, bool record);
+garm_status projectStats(State &s, garm_step_stats *st);
 template <int D, typename T> garm_status extrapolateToAir(State &s);
 template <int D, typename T> garm_status enforceBoundaryConditions(State &s);
 template <int D, typename T> garm_status enforceBoundaryLevelSet(State &s, void *field, double tol);
@@ -100,6 +130,8 @@ template <int D, typename T> garm_status resetRefView(State &s);
 template <int D, typename T> garm_status initRefMap(State &s);
 template <int D, typename T> garm_status refreshRefGradient(State &s);
 template <int D, typename T> garm_status maxSpeed(State &s, double *out);
+template <int D, typename T> garm_status maxSpeedAsync(State &s);
+__global__ void kStepDt(const unsigned long long *maxBits, double dx, double *clock, double *dt, double *stats, const unsigned long long *counter);
 template <int D, typename T> garm_status copyField(State &s, void *dst, const void *src, int64_t n);
 
 // Standalone WENO5 reinitialisation on raw device planes.

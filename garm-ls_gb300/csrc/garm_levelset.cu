@@ -57,7 +57,8 @@ __device__ __forceinline__ T hermiteScalar(const G<D, T> &g, const T *p, const T
 }
 
 template <int D, typename T>
-__global__ void __launch_bounds__(kBlock) kCompose(Geom geom, ComposeIO<D, T> io, T airClamp, T solidTol) {
+__global__ void __launch_bounds__(kBlock) kCompose(Geom geom, ComposeIO<D, T> io, T airClamp, T solidTol, const int *gate) {
+	if (gate && !*gate) return;
 	const G<D, T> g = cellGrid<D, T>(geom);
 	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
 	if (id >= g.count()) return;
@@ -83,7 +84,7 @@ garm_status generateCurrentFields(State &s) {
 	io.cellDist = (const T *)s.cellDist;
 	io.phi = (T *)s.phi; io.tmp = (T *)s.tmp; io.ori = (T *)s.ori;
 	const double airClamp = s.cfg.air_extrap_radius * s.geom.dx;
-	kCompose<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, io, T(airClamp), T(3.0 * s.geom.dx)); s.launches++;
+	kCompose<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, io, T(airClamp), T(3.0 * s.geom.dx), s.gate); s.launches++;
 	GARM_CHECK_LAUNCH();
 	return GARM_OK;
 }
@@ -252,23 +253,40 @@ __global__ void __launch_bounds__(kBlock) kCheckRefMap(int64_t N, const T *ori, 
 	}
 }
 
+// restartFlag = !(bad <= ratio * tot): the decision of advance (LevelSetLiquid.cpp:631)
+__global__ void kRestartDecision(const int *counts, double ratio, int *flag, double *stats, const unsigned long long *counter) {
+	double *rec = stepRecord(stats, counter);
+	const int tot = counts[0], bad = counts[1];
+	const int restart = (1.0 * bad <= ratio * tot) ? 0 : 1;
+	*flag = restart;
+	if (rec) { rec[kStRestarted] = restart; rec[kStRmTotal] = tot; rec[kStRmBad] = bad; }
+}
+
+// Counts and decision on the device, no host synchronisation.
 template <int D, typename T>
-garm_status checkReferenceMap(State &s, int *keep, int *tot, int *bad) {
+garm_status checkReferenceMapAsync(State &s, bool record) {
 	cudaError_t e = cudaMemsetAsync(s.redI32, 0, 2 * sizeof(int), s.stream);
 	if (e != cudaSuccess) return GARM_CUDA_ERROR;
 	PiPtrs<D, T> pp{};
 	for (int q = 0; q < D * D; q++) pp.p[q] = (const T *)s.Pi[q];
 	kCheckRefMap<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, (const T *)s.ori, (const T *)s.cellDist, pp,
 		s.cfg.rm_band * s.geom.dx, s.cfg.rm_threshold, s.redI32); s.launches++;
+	kRestartDecision<<<1, 1, 0, s.stream>>>(s.redI32, s.cfg.rm_ratio, s.restartFlag, record ? s.statsDev : nullptr, s.stepCounter); s.launches++;
 	GARM_CHECK_LAUNCH();
-	int h[2] = {0, 0};
-	e = cudaMemcpyAsync(h, s.redI32, sizeof(h), cudaMemcpyDeviceToHost, s.stream);
-	if (e != cudaSuccess) return GARM_CUDA_ERROR;
-	e = cudaStreamSynchronize(s.stream);
+	return GARM_OK;
+}
+
+template <int D, typename T>
+garm_status checkReferenceMap(State &s, int *keep, int *tot, int *bad) {
+	GARM_TRY((checkReferenceMapAsync<D, T>(s, false)));
+	int h[2] = {0, 0}, f = 0;
+	cudaError_t e = cudaMemcpyAsync(h, s.redI32, sizeof(h), cudaMemcpyDeviceToHost, s.stream);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(&f, s.restartFlag, sizeof(int), cudaMemcpyDeviceToHost, s.stream);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
 	if (e != cudaSuccess) return GARM_CUDA_ERROR;
 	if (tot) *tot = h[0];
 	if (bad) *bad = h[1];
-	if (keep) *keep = (1.0 * h[1] <= s.cfg.rm_ratio * h[0]) ? 1 : 0;
+	if (keep) *keep = f ? 0 : 1;
 	return GARM_OK;
 }
 
@@ -285,7 +303,8 @@ struct RestartIO {
 };
 
 template <int D, typename T>
-__global__ void __launch_bounds__(kBlock) kRestart(Geom geom, RestartIO<D, T> io) {
+__global__ void __launch_bounds__(kBlock) kRestart(Geom geom, RestartIO<D, T> io, const int *gate) {
+	if (gate && !*gate) return;
 	const G<D, T> g = cellGrid<D, T>(geom);
 	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
 	if (id >= g.count()) return;
@@ -317,7 +336,7 @@ garm_status restart(State &s) {
 	io.ref = (T *)s.ref;
 	for (int a = 0; a < D; a++) { io.refGrad[a] = (T *)s.refGrad[a]; io.xi[a] = (T *)s.xi[a]; }
 	for (int q = 0; q < D * D; q++) io.Pi[q] = (T *)s.Pi[q];
-	kRestart<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, io); s.launches++;
+	kRestart<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, io, s.gate); s.launches++;
 	GARM_CHECK_LAUNCH();
 	return resetRefView<D, T>(s);
 }
@@ -399,6 +418,7 @@ garm_status enforceBoundaryLevelSet(State &s, void *field, double tol) {
 	template garm_status reinitialize<D, T>(State &); \
 	template garm_status reinitRaw<D, T>(cudaStream_t, const int *, double, T *, T *, T *, int, double); \
 	template garm_status checkReferenceMap<D, T>(State &, int *, int *, int *); \
+	template garm_status checkReferenceMapAsync<D, T>(State &, bool); \
 	template garm_status restart<D, T>(State &); \
 	template garm_status initRefMap<D, T>(State &); \
 	template garm_status refreshRefGradient<D, T>(State &); \

@@ -547,8 +547,20 @@ __global__ void __launch_bounds__(kBlock) kApplyPressure(Geom geom, T *u0, T *u1
 	u[id] = T(double(u[id]) + (p1 - p0) * coef);
 }
 
+// Copy the solve's statistics into the step record on the device.
+__global__ void kRecordCg(const int *ints, const double *scal, const int *n, double *stats, const unsigned long long *counter) {
+	double *rec = stepRecord(stats, counter);
+	if (!rec) return;
+	rec[kStUnknowns] = *n;
+	rec[kStCgIters] = ints[0];
+	rec[kStCgRefine] = ints[1];
+	rec[kStCgResidual] = scal[0];
+	rec[kStCgTol] = scal[1];
+	rec[kStCgErr] = ints[4];
+}
+
 template <int D, typename T>
-garm_status project(State &s, garm_step_stats *st) {
+garm_status projectAsync(State &s, bool record) {
 	const unsigned nbC = gridFor(s.N);
 	kUnknownFlags<D, T><<<nbC, kBlock, 0, s.stream>>>(s.geom, (const T *)s.phi, (const T *)s.fraction[0], (const T *)s.fraction[1], (const T *)s.fraction[2],
 		s.grid2mat, s.scanBlock); s.launches++;
@@ -594,8 +606,14 @@ garm_status project(State &s, garm_step_stats *st) {
 	int perSM = 0;
 	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kfn, kCgBlock, 0);
 	if (e != cudaSuccess || perSM <= 0) return GARM_CUDA_ERROR;
-	// one resident 512-thread block per SM; the cooperative launch verifies co-residency
-	int blocks = s.numSMs;
+	// one resident 512-thread block per SM for large scenes; small scenes take one
+	// block per 4096 interior cells so that several scenes' solves can share the GPU.
+	// The cooperative launch verifies co-residency.
+	int64_t interior = 1;
+	for (int q = 0; q < D; q++) interior *= (s.geom.n[q] - 2 * s.geom.bw);
+	int blocks = int((interior + 4095) / 4096);
+	if (blocks < 1) blocks = 1;
+	if (blocks > s.numSMs) blocks = s.numSMs;
 	if (blocks > s.maxBlocks) blocks = s.maxBlocks;
 	if (blocks > s.maxBlocks) blocks = s.maxBlocks;
 	void *args[] = {&a};
@@ -607,8 +625,15 @@ garm_status project(State &s, garm_step_stats *st) {
 		s.F[0], s.F[1], s.Ftot); s.launches++;
 	GARM_CHECK_LAUNCH();
 
+	kRecordCg<<<1, 1, 0, s.stream>>>(s.cgInts, s.cgScalars, s.nUnknownsDev, record ? s.statsDev : nullptr, s.stepCounter); s.launches++;
+	GARM_CHECK_LAUNCH();
+	return GARM_OK;
+}
+
+// Statistics of the last solve (host readback; synchronises the stream).
+garm_status projectStats(State &s, garm_step_stats *st) {
 	int hi[8] = {}; double hs[2] = {}; int n = 0;
-	e = cudaMemcpyAsync(hi, s.cgInts, sizeof(hi), cudaMemcpyDeviceToHost, s.stream);
+	cudaError_t e = cudaMemcpyAsync(hi, s.cgInts, sizeof(hi), cudaMemcpyDeviceToHost, s.stream);
 	if (e == cudaSuccess) e = cudaMemcpyAsync(hs, s.cgScalars, sizeof(hs), cudaMemcpyDeviceToHost, s.stream);
 	if (e == cudaSuccess) e = cudaMemcpyAsync(&n, s.nUnknownsDev, sizeof(int), cudaMemcpyDeviceToHost, s.stream);
 	if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
@@ -625,7 +650,13 @@ garm_status project(State &s, garm_step_stats *st) {
 	return GARM_OK;
 }
 
-#define GARM_INST(D, T) template garm_status project<D, T>(State &, garm_step_stats *);
+template <int D, typename T>
+garm_status project(State &s, garm_step_stats *st) {
+	GARM_TRY((projectAsync<D, T>(s, false)));
+	return projectStats(s, st);
+}
+
+#define GARM_INST(D, T) template garm_status project<D, T>(State &, garm_step_stats *); template garm_status projectAsync<D, T>(State &, bool);
 GARM_INST(2, double)
 GARM_INST(3, double)
 GARM_INST(2, float)

@@ -83,6 +83,9 @@ _SIGS = {
     "garm_sim_initialize": (C.c_int, [C.c_void_p]),
     "garm_sim_finish_load": (C.c_int, [C.c_void_p]),
     "garm_sim_advance": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(StepStats)]),
+    "garm_sim_set_clock": (C.c_int, [C.c_void_p, C.c_uint, C.c_double]),
+    "garm_sim_advance_auto": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(StepStats)]),
+    "garm_sim_graph_active": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "garm_sim_max_speed": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "garm_sim_time_step": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_double)]),
     "garm_stage_advect": (C.c_int, [C.c_void_p, C.c_double]),
@@ -237,6 +240,23 @@ class Simulation:
         d = stats.as_dict()
         d["status"] = st
         return d
+
+    def set_clock(self, frame_rate: int = 25, cfl: float = 1.0) -> None:
+        check(self.lib.garm_sim_set_clock(self.handle, int(frame_rate), float(cfl)), "garm_sim_set_clock")
+
+    def advance_auto(self, steps: int, allow_not_converged: bool = True) -> dict:
+        stats = StepStats()
+        st = self.lib.garm_sim_advance_auto(self.handle, int(steps), C.byref(stats))
+        if st != OK and not (allow_not_converged and st == NOT_CONVERGED):
+            check(st, "garm_sim_advance_auto")
+        d = stats.as_dict()
+        d["status"] = st
+        return d
+
+    def graph_active(self) -> bool:
+        v = C.c_int()
+        check(self.lib.garm_sim_graph_active(self.handle, C.byref(v)), "garm_sim_graph_active")
+        return bool(v.value)
 
     def max_speed(self) -> float:
         v = C.c_double()

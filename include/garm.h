@@ -143,6 +143,18 @@ garm_status garm_sim_finish_load(garm_sim *sim);
 /* LevelSetLiquid::advance (Source/Core/LevelSetLiquid.cpp:608-698). `stats` may be NULL. */
 garm_status garm_sim_advance(garm_sim *sim, double dt, garm_step_stats *stats);
 
+/* Device-resident stepping.  garm_sim_set_clock starts a frame clock for the
+ * Simulator's dt policy (Common/Util/Simulator.cpp:102-128): dt = cfl*dx/max|u|,
+ * clamped to the end of a frame of 1/frame_rate seconds and halved when two steps
+ * remain.  garm_sim_advance_auto then runs `steps` advance() calls with dt computed
+ * on the device, replaying a captured CUDA graph of one step when the device
+ * allows it, and synchronises once at the end; `stats` describes the last step and
+ * ms_total the whole call.  Replaces the Simulator loop around advance(). */
+garm_status garm_sim_set_clock(garm_sim *sim, unsigned frame_rate, double cfl);
+garm_status garm_sim_advance_auto(garm_sim *sim, int steps, garm_step_stats *stats);
+/* 1 when garm_sim_advance_auto replays captured step graphs (no reference counterpart). */
+garm_status garm_sim_graph_active(const garm_sim *sim, int *active);
+
 /* max over faces of |u| (GridBasedData::normMax, Source/Core/GridBasedData.h:55-68). */
 garm_status garm_sim_max_speed(garm_sim *sim, double *out);
 /* LevelSetLiquid::getTimeStep (Source/Core/LevelSetLiquid.h:129): cfl*dx/max|u| (may be +inf). */
