@@ -44,6 +44,12 @@ def parse():
     p.add_argument("--no-mixed", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--workload", choices=["dam", "batch", "serve"], default="dam",
+                   help="dam: the 128^3 dam break (default line, with mixed and batch sub-objects); "
+                        "batch: 48 uneven pool scenes only; serve: the Poisson request stream only")
+    p.add_argument("--batch-scenes", type=int, default=48)
+    p.add_argument("--requests", type=int, default=48, help="serve: number of requests")
     return p.parse_args()
 
 
@@ -177,6 +183,80 @@ def reinit_roofline(sim, torch, stream, n_cells: int, esz: int, iters: int, peak
             "traffic": None, "ms_per_launch": round(ms_per_launch, 4), "algorithmic_bytes_per_launch": int(bytes_per_launch)}
 
 
+def batch_scenes(count: int, seed: int = 0):
+    """`count` independent pool scenes: n drawn uniformly from {64, 96, 128, 160},
+    1-3 seed-placed spheres of radius 0.05-0.15 over a pool of depth 0.1-0.4."""
+    import numpy as np
+    from garm import scenes
+    rng = np.random.default_rng(seed)
+    sizes = rng.choice([64, 96, 128, 160], size=count)
+    return [scenes.random_pool_scene(int(n), seed=1000 + i) for i, n in enumerate(sizes)]
+
+
+def run_batch(args, torch, world: int, W: int, K: int) -> dict:
+    """Mixed-precision steps of a batch of uneven scenes, one stream per scene, each
+    batch step one replay of every scene's captured step graph (garm_batch_advance_auto).
+    Timed with events on one stream joined to every scene stream on both sides."""
+    from garm import capi
+    scs = batch_scenes(args.batch_scenes)
+    cfg = capi.default_config(precision=capi.PRECISION_MIXED)
+    streams = [torch.cuda.Stream() for _ in scs]
+    sims = []
+    for sc, st in zip(scs, streams):
+        sim = capi.Simulation(sc.grid, cfg, stream=st.cuda_stream)
+        sim.upload(capi.FIELD_LEVEL_SET, sc.phi.ravel())
+        sim.upload(capi.FIELD_VELOCITY, sc.velocity)
+        sim.initialize()
+        sim.stage("restart")
+        sim.set_clock(25, 1.0)
+        sims.append(sim)
+    cells = sum(sc.interior_cells for sc in scs)
+    resident = sum(s.device_bytes() for s in sims)
+    capi.batch_advance_auto(sims, W)  # warm-up, captures every scene's step graphs
+    l0 = sum(s.launch_count() for s in sims)
+    main = torch.cuda.current_stream()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(main)
+    for st in streams:
+        st.wait_event(e0)
+    stats = capi.batch_advance_auto(sims, K)
+    for st in streams:
+        ev = torch.cuda.Event()
+        ev.record(st)
+        main.wait_event(ev)
+    e1.record(main)
+    torch.cuda.synchronize()
+    ms = reduce_max(e0.elapsed_time(e1), world)
+    launches = sum(s.launch_count() for s in sims) - l0
+    per_step = [st["ms_total"] / K for st in stats]
+    graphs = all(s.graph_active() for s in sims)
+    for s in sims:
+        s.close()
+    import numpy as np
+    return {"value": world * cells * K / (ms * 1e-3), "unit": UNIT, "ms_per_batch_step": ms / K, "scenes": len(scs),
+            "interior_cells": cells, "sizes": sorted({int(round(sc.interior_cells ** (1 / 3))) for sc in scs}),
+            "resident_bytes": resident, "graph_replay": graphs, "gpu_launches": launches,
+            "p50_scene_step_ms": float(np.percentile(per_step, 50)), "p99_scene_step_ms": float(np.percentile(per_step, 99)),
+            "dtype": "f32 storage+math, f64 dots/residual/refinement/RM test",
+            "workload": f"{len(scs)} pool scenes, n uniform in {{64,96,128,160}}, 1-3 spheres, mixed, "
+                        f"one stream and one step graph per scene, {K} steps each"}
+
+
+def run_serve(args, world: int) -> dict:
+    """The Poisson request stream served with HBM-budget admission and continuous batching."""
+    from garm import serving
+    reqs = serving.make_requests(args.requests, rate=20.0, seed=11)
+    out = serving.Server(budget_bytes=150e9).run(reqs)
+    res = out.pop("results")
+    out.update({"unit": UNIT, "value": world * out["cell_steps_per_s"],
+                "workload": f"{len(reqs)} requests, Poisson 20/s, n log-uniform in [48,192], 20-200 steps, "
+                            "dam break or drop, mixed, 150 GB budget",
+                "restarts": sum(r.restarts for r in res)})
+    return out
+
+
 def run_garm(args) -> None:
     import numpy as np
     import torch
@@ -191,6 +271,26 @@ def run_garm(args) -> None:
     stream = torch.cuda.current_stream()
     capi.load()
     n, K, W = args.n, args.steps, args.warmup
+    if args.workload in ("batch", "serve"):
+        clocks = Clocks(local)
+        clocks.start()
+        sub = run_batch(args, torch, world, W, K) if args.workload == "batch" else run_serve(args, world)
+        clk = clocks.stop()
+        if rank == 0:
+            line = {"metric": METRIC, "value": sub.pop("value"), "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+                    "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                    "data": "synthetic", "config": {"workload": sub.pop("workload"), "replicas": world,
+                                                    "l2": "no flush: device state larger than L2"},
+                    "clocks": clk}
+            if "ms_per_batch_step" in sub:
+                line["ms_per_step"] = sub["ms_per_batch_step"]
+                line["gpu_launches"] = sub["gpu_launches"]
+            line[args.workload] = sub
+            print(json.dumps(line), flush=True)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
     scene = scenes.dam_break(3, n)
     dx = scene.grid.spacing
     interior = n ** 3
@@ -206,29 +306,28 @@ def run_garm(args) -> None:
 
     main_prec = capi.PRECISION_MIXED if args.precision == "mixed" else capi.PRECISION_FP64
     sim = make(main_prec)
-    gen = scenes.frame_time_steps(sim.max_speed, W + K, 25, 1.0, dx)
-    for _ in range(W):
-        sim.advance(next(gen))
+    sim.set_clock(25, 1.0)  # Simulator dt policy on the device: CFL 1, 25 frames/s
+    sim.advance_auto(W)     # warm-up (also captures the step graphs)
     barrier(world)
     torch.cuda.synchronize()
     clocks = Clocks(local)
     clocks.start()
     l0 = sim.launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    step_ms, cg_it, restarts, dts = [], [], 0, []
     ev0.record(stream)
-    for _ in range(K):
-        dt = next(gen)
-        st = sim.advance(dt)
-        dts.append(dt)
-        step_ms.append(st["ms_total"])
-        cg_it.append(st["cg_iterations"])
-        restarts += st["restarted"]
+    sim.advance_auto(K)     # K steps, dt from max|u| on the device, one synchronisation
     ev1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
     launches = sim.launch_count() - l0
     elapsed_ms = reduce_max(ev0.elapsed_time(ev1), world)
+    # per-step latency: the same loop one step per call (each call synchronises)
+    step_ms, cg_it, restarts = [], [], 0
+    for _ in range(K):
+        st = sim.advance_auto(1)
+        step_ms.append(st["ms_total"])
+        cg_it.append(st["cg_iterations"])
+        restarts += st["restarted"]
     barrier(world)
     value = replica_value(world, interior, K, elapsed_ms)
     peaks = measured_peaks()
@@ -236,12 +335,12 @@ def run_garm(args) -> None:
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": elapsed_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
-        "config": {"workload": f"3D dam break {n}^3 MAC grid, {'plain FP64' if args.precision == 'fp64' else 'mixed FP32/FP64'} form (BASELINE config C2)", "n": n,
+        "config": {"workload": f"3D dam break {n}^3 MAC grid, {'plain FP64' if args.precision == 'fp64' else 'mixed FP32/FP64'} form", "n": n,
                    "interior_cells": interior, "storage_cells": (n + 4) ** 3, "cfl": 1.0, "frame_rate": 25,
                    "reinit": "WENO5 x30 every step", "pcg_tol": 1e-8, "replicas": world,
                    "l2": "no flush: device state > 1 GB, larger than L2"},
         "p50_step_ms": statistics.median(step_ms), "p99_step_ms": float(np.percentile(step_ms, 99)),
-        "cg_iterations_mean": statistics.mean(cg_it), "restarts": restarts,
+        "cg_iterations_mean": statistics.mean(cg_it), "restarts": restarts, "graph_replay": sim.graph_active(),
         "clocks": clk, "gpu_launches": launches,
     }
     if rank == 0:
@@ -288,21 +387,21 @@ def run_garm(args) -> None:
         band = np.abs(pr) <= 3 * dx
         phi_err_band = float(np.max(np.abs(pr - pm)[band])) / dx
         ref.close()
-        g2 = scenes.frame_time_steps(mix.max_speed, W + K, 25, 1.0, dx)
-        for _ in range(W):
-            mix.advance(next(g2))
+        mix.set_clock(25, 1.0)
+        mix.advance_auto(W)
         barrier(world)
         torch.cuda.synchronize()
         m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        mms, mcg = [], []
         m0.record(stream)
-        for _ in range(K):
-            st = mix.advance(next(g2))
-            mms.append(st["ms_total"])
-            mcg.append(st["cg_iterations"])
+        mix.advance_auto(K)
         m1.record(stream)
         torch.cuda.synchronize()
         mix_ms = reduce_max(m0.elapsed_time(m1), world)
+        mms, mcg = [], []
+        for _ in range(K):
+            st = mix.advance_auto(1)
+            mms.append(st["ms_total"])
+            mcg.append(st["cg_iterations"])
         mval = world * interior * K / (mix_ms * 1e-3)
         out["mixed"] = {"value": mval, "unit": UNIT, "ms_per_step": mix_ms / K, "p50_step_ms": statistics.median(mms),
                         "p99_step_ms": float(np.percentile(mms, 99)), "phi_err_dx_band3dx_after_1_step_vs_fp64": phi_err_band, "phi_err_dx_all_cells_after_1_step_vs_fp64": phi_err,
@@ -312,6 +411,11 @@ def run_garm(args) -> None:
             out["mixed"]["roofline"] = reinit_roofline(mix, torch, stream, int(scene.phi.size), 4, 30, peaks)
             out["mixed"]["roofline"]["traffic"] = profiled_traffic("reinit_stage_f32_dam_break_128.txt", n)
         mix.close()
+
+    # many uneven scenes at once (mixed): the batched form of the same pipeline
+    if not args.no_batch:
+        out["batch"] = run_batch(args, torch, world, W, K)
+        out["batch"]["speedup_vs_fp64"] = out["batch"]["value"] / value if args.precision == "fp64" else None
 
     # CPU baseline: the oracle (a CPU port of the reference's FP64 path) on this host,
     # one step of the same 128^3 workload started from the GPU's state
@@ -369,7 +473,7 @@ def run_reference(args) -> None:
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": 1e3 * total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": f"3D dam break {n}^3 MAC grid, plain FP64 form (BASELINE config C2)", "n": n},
+        "config": {"workload": f"3D dam break {n}^3 MAC grid, plain FP64 form", "n": n},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
                          "sample": f"{K} full oracle steps of the {n}^3 dam break; warm-up capped at 1 step"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

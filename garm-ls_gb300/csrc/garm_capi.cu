@@ -51,6 +51,7 @@ __global__ void kPressureToCells(int64_t N, const int *grid2mat, const double *p
 garm_status dalloc(State &s, void **p, size_t bytes) {
 	*p = nullptr;
 	if (bytes == 0) return GARM_OK;
+	if (s.dryRun) { s.deviceBytes += bytes; return GARM_OK; }
 	if (s.nAllocs >= int(sizeof(s.allocs) / sizeof(s.allocs[0]))) return GARM_OOM;
 	if (cudaMalloc(p, bytes) != cudaSuccess) { cudaGetLastError(); *p = nullptr; return GARM_OOM; }
 	if (cudaMemsetAsync(*p, 0, bytes, s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
@@ -148,6 +149,7 @@ garm_status allocState(State &s) {
 	GARM_TRY(dalloc(s, &s.restartFlag, 64));
 	GARM_TRY(dalloc(s, &s.stepCounter, 64));
 	GARM_TRY(dalloc(s, &s.statsDev, size_t(kStatsCap) * kStatsSlots * 8));
+	if (s.dryRun) return GARM_OK;
 	if (cudaMallocHost(&s.statsHost, size_t(kStatsCap) * kStatsSlots * 8) != cudaSuccess) { cudaGetLastError(); s.statsHost = nullptr; return GARM_OOM; }
 	// staging: the largest .sav field (Π: D*D doubles per cell)
 	size_t big = N * 8 * size_t(D * D);
@@ -470,8 +472,9 @@ garm_status buildStepGraphs(State &s) {
 	return GARM_OK;
 }
 
-// `steps` steps with dt from the device (Simulator::advanceTimeBySteps policy).
-garm_status advanceAuto(State &s, int steps, garm_step_stats *st) {
+// Enqueue `steps` steps with dt from the device (Simulator::advanceTimeBySteps
+// policy); returns without synchronising.  ev[0]/ev[8] bracket the enqueued work.
+garm_status enqueueAuto(State &s, int steps) {
 	if (!s.graphTried) GARM_TRY(buildStepGraphs(s));
 	GARM_TRY(record(s, 0));
 	for (int k = 0; k < steps; k++) {
@@ -490,14 +493,27 @@ garm_status advanceAuto(State &s, int steps, garm_step_stats *st) {
 		}
 	}
 	GARM_TRY(record(s, 8));
+	s.pendingSteps = steps;
+	return GARM_OK;
+}
+
+// Wait for the enqueued steps and read their records.
+garm_status collect(State &s, garm_step_stats *st) {
 	garm_step_stats local{};
 	garm_step_stats &S = st ? *st : local;
 	std::memset(&S, 0, sizeof(S));
-	const garm_status pr = readRecords(s, steps < kStatsCap ? steps : kStatsCap, &S);
+	const int k = s.pendingSteps < 1 ? 1 : (s.pendingSteps < kStatsCap ? s.pendingSteps : kStatsCap);
+	const garm_status pr = readRecords(s, k, &S);
 	float ms = 0;
 	cudaEventElapsedTime(&ms, s.ev[0], s.ev[8]);
 	S.ms_total = ms;
+	s.pendingSteps = 0;
 	return pr;
+}
+
+garm_status advanceAuto(State &s, int steps, garm_step_stats *st) {
+	GARM_TRY(enqueueAuto(s, steps));
+	return collect(s, st);
 }
 
 }  // namespace
@@ -538,6 +554,35 @@ garm_status garm_config_default(garm_config *c) {
 	c->mixed_inner_tolerance = 1e-4;
 	c->mixed_max_refinements = 12;
 	return GARM_OK;
+}
+
+garm_status garm_sim_estimate_bytes(const garm_grid_desc *gd, const garm_config *cfg, size_t *bytes) {
+	if (!gd || !bytes) return GARM_INVALID;
+	if (gd->dim != 2 && gd->dim != 3) return GARM_INVALID;
+	garm_config c;
+	if (cfg) c = *cfg; else garm_config_default(&c);
+	State s;
+	s.dryRun = true;
+	s.cfg = c;
+	s.dim = gd->dim;
+	s.mixed = c.precision == GARM_PRECISION_MIXED;
+	s.esz = s.mixed ? 4 : 8;
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&s.numSMs, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) { cudaGetLastError(); s.numSMs = 160; }
+	const int D = s.dim;
+	int n[3];
+	for (int a = 0; a < 3; a++) n[a] = a < D ? gd->resolution[a] : 1;
+	s.N = int64_t(n[0]) * n[1] * n[2];
+	s.NN = int64_t(n[0] + 1) * (n[1] + 1) * (D == 3 ? n[2] + 1 : 1);
+	s.Ftot = 0;
+	for (int a = 0; a < 3; a++) {
+		s.F[a] = 0;
+		if (a < D) { int64_t f = 1; for (int b = 0; b < D; b++) f *= n[b] + (b == a ? 1 : 0); s.F[a] = f; }
+		s.Ftot += s.F[a];
+	}
+	const garm_status r = allocState(s);
+	*bytes = s.deviceBytes;
+	return r;
 }
 
 garm_status garm_sim_create(const garm_grid_desc *gd, const garm_config *cfg, void *stream, garm_sim **out) {
@@ -669,6 +714,56 @@ garm_status garm_sim_set_clock(garm_sim *sim, unsigned frame_rate, double cfl) {
 garm_status garm_sim_advance_auto(garm_sim *sim, int steps, garm_step_stats *stats) {
 	if (!sim || steps < 1) return GARM_INVALID;
 	return advanceAuto(sim->s, steps, stats);
+}
+
+garm_status garm_sim_enqueue_auto(garm_sim *sim, int steps) {
+	if (!sim || steps < 1) return GARM_INVALID;
+	return enqueueAuto(sim->s, steps);
+}
+
+garm_status garm_sim_poll(garm_sim *sim, int *done) {
+	if (!sim || !done) return GARM_INVALID;
+	const cudaError_t e = cudaEventQuery(sim->s.ev[8]);
+	if (e == cudaSuccess) { *done = 1; return GARM_OK; }
+	if (e == cudaErrorNotReady) { cudaGetLastError(); *done = 0; return GARM_OK; }
+	return GARM_CUDA_ERROR;
+}
+
+garm_status garm_sim_collect(garm_sim *sim, garm_step_stats *stats) {
+	if (!sim) return GARM_INVALID;
+	return collect(sim->s, stats);
+}
+
+garm_status garm_batch_advance_auto(garm_sim *const *sims, int count, int steps, garm_step_stats *stats) {
+	if (!sims || count < 1 || steps < 1) return GARM_INVALID;
+	for (int i = 0; i < count; i++) if (!sims[i]) return GARM_INVALID;
+	// one step of every scene per round, each on its own stream, so scenes overlap on the device
+	for (int i = 0; i < count; i++) { State &s = sims[i]->s; if (!s.graphTried) GARM_TRY(buildStepGraphs(s)); GARM_TRY(record(s, 0)); }
+	for (int k = 0; k < steps; k++) {
+		for (int i = 0; i < count; i++) {
+			State &s = sims[i]->s;
+			if (s.graphOk) {
+				const int parity = (s.u[0] == s.evenU0) ? 0 : 1;
+				if (cudaGraphLaunch(s.stepGraph[parity], s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
+				s.hostSteps++; s.stepIndex++; s.launches += s.graphLaunches;
+				swapRoles(s);
+			} else {
+				GARM_TRY(beginStep(s));
+				GARM_TRY(enqueueAutoDt(s));
+				GARM_TRY(enqueueStep(s, false));
+			}
+		}
+	}
+	garm_status worst = GARM_OK;
+	for (int i = 0; i < count; i++) {
+		State &s = sims[i]->s;
+		GARM_TRY(record(s, 8));
+		s.pendingSteps = steps;
+		const garm_status r = collect(s, stats ? &stats[i] : nullptr);
+		if (r != GARM_OK && r != GARM_NOT_CONVERGED) return r;
+		if (r == GARM_NOT_CONVERGED) worst = r;
+	}
+	return worst;
 }
 
 garm_status garm_sim_graph_active(const garm_sim *sim, int *active) {

@@ -78,6 +78,7 @@ struct State {
 	void *stage = nullptr; size_t stageBytes = 0;
 	// every device allocation, freed by garm_sim_destroy
 	void *allocs[160] = {}; int nAllocs = 0; size_t deviceBytes = 0;
+	bool dryRun = false;       // count allocation sizes only (garm_sim_estimate_bytes)
 	// timing events
 	cudaEvent_t ev[10] = {};
 	// device-resident stepping: dt of the current step, the Simulator frame clock
@@ -97,6 +98,7 @@ struct State {
 	bool graphTried = false, graphOk = false;
 	void *evenU0 = nullptr;            // u[0] buffer of the even-step graph
 	long long graphLaunches = 0;       // kernels in one captured step
+	int pendingSteps = 0;              // steps enqueued and not yet collected
 };
 
 // Per-step records live in a device ring indexed by a device step counter, so a

@@ -75,6 +75,7 @@ _SIGS = {
     "garm_config_default": (C.c_int, [C.POINTER(Config)]),
     "garm_sim_create": (C.c_int, [C.POINTER(GridDesc), C.POINTER(Config), C.c_void_p, C.POINTER(C.c_void_p)]),
     "garm_sim_destroy": (C.c_int, [C.c_void_p]),
+    "garm_sim_estimate_bytes": (C.c_int, [C.POINTER(GridDesc), C.POINTER(Config), C.POINTER(C.c_size_t)]),
     "garm_sim_device_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
     "garm_sim_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
     "garm_sim_field_bytes": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_size_t)]),
@@ -86,6 +87,10 @@ _SIGS = {
     "garm_sim_set_clock": (C.c_int, [C.c_void_p, C.c_uint, C.c_double]),
     "garm_sim_advance_auto": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(StepStats)]),
     "garm_sim_graph_active": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "garm_sim_enqueue_auto": (C.c_int, [C.c_void_p, C.c_int]),
+    "garm_sim_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "garm_sim_collect": (C.c_int, [C.c_void_p, C.POINTER(StepStats)]),
+    "garm_batch_advance_auto": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.POINTER(StepStats)]),
     "garm_sim_max_speed": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "garm_sim_time_step": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_double)]),
     "garm_stage_advect": (C.c_int, [C.c_void_p, C.c_double]),
@@ -253,6 +258,23 @@ class Simulation:
         d["status"] = st
         return d
 
+    def enqueue_auto(self, steps: int) -> None:
+        check(self.lib.garm_sim_enqueue_auto(self.handle, int(steps)), "garm_sim_enqueue_auto")
+
+    def poll(self) -> bool:
+        v = C.c_int()
+        check(self.lib.garm_sim_poll(self.handle, C.byref(v)), "garm_sim_poll")
+        return bool(v.value)
+
+    def collect(self, allow_not_converged: bool = True) -> dict:
+        stats = StepStats()
+        st = self.lib.garm_sim_collect(self.handle, C.byref(stats))
+        if st != OK and not (allow_not_converged and st == NOT_CONVERGED):
+            check(st, "garm_sim_collect")
+        d = stats.as_dict()
+        d["status"] = st
+        return d
+
     def graph_active(self) -> bool:
         v = C.c_int()
         check(self.lib.garm_sim_graph_active(self.handle, C.byref(v)), "garm_sim_graph_active")
@@ -306,6 +328,12 @@ class Simulation:
         return None
 
 
+def estimate_bytes(grid: GridDesc, cfg: Config) -> int:
+    n = C.c_size_t()
+    check(load().garm_sim_estimate_bytes(C.byref(grid), C.byref(cfg), C.byref(n)), "garm_sim_estimate_bytes")
+    return n.value
+
+
 def reinit_host(phi: np.ndarray, spacing: float, iters: int, cfl: float, precision: int = PRECISION_FP64) -> np.ndarray:
     """WENO5 reinitialisation of a numpy cell field on the GPU (TestReinit usage)."""
     lib = load()
@@ -315,3 +343,14 @@ def reinit_host(phi: np.ndarray, spacing: float, iters: int, cfl: float, precisi
     check(lib.garm_reinit_host(dim, size, float(spacing), a.ctypes.data_as(C.POINTER(C.c_double)), int(iters), float(cfl),
                                int(precision)), "garm_reinit_host")
     return a
+
+
+def batch_advance_auto(sims: list, steps: int) -> list:
+    """garm_batch_advance_auto over `sims` (each created with its own stream)."""
+    lib = load()
+    arr = (C.c_void_p * len(sims))(*[s.handle.value for s in sims])
+    stats = (StepStats * len(sims))()
+    st = lib.garm_batch_advance_auto(arr, len(sims), int(steps), stats)
+    if st not in (OK, NOT_CONVERGED):
+        check(st, "garm_batch_advance_auto")
+    return [s.as_dict() for s in stats]

@@ -120,6 +120,9 @@ garm_status garm_config_default(garm_config *cfg);
  * (Source/Core/Boundary.cpp:8-35) for the domain box walls. */
 garm_status garm_sim_create(const garm_grid_desc *grid, const garm_config *cfg, void *stream, garm_sim **out);
 garm_status garm_sim_destroy(garm_sim *sim);
+/* Device bytes garm_sim_create would allocate for this grid and configuration,
+ * without allocating (admission control; no reference counterpart). */
+garm_status garm_sim_estimate_bytes(const garm_grid_desc *grid, const garm_config *cfg, size_t *bytes);
 garm_status garm_sim_device_bytes(const garm_sim *sim, size_t *bytes);
 /* Kernels launched by this simulation since creation (no reference counterpart: instrumentation). */
 garm_status garm_sim_launch_count(const garm_sim *sim, long long *count);
@@ -152,6 +155,17 @@ garm_status garm_sim_advance(garm_sim *sim, double dt, garm_step_stats *stats);
  * ms_total the whole call.  Replaces the Simulator loop around advance(). */
 garm_status garm_sim_set_clock(garm_sim *sim, unsigned frame_rate, double cfl);
 garm_status garm_sim_advance_auto(garm_sim *sim, int steps, garm_step_stats *stats);
+/* Asynchronous form for serving loops: enqueue `steps` auto steps on the
+ * simulation's stream and return at once; poll for completion; collect the
+ * statistics (waits if needed).  Scenes on different streams overlap on the GPU. */
+garm_status garm_sim_enqueue_auto(garm_sim *sim, int steps);
+garm_status garm_sim_poll(garm_sim *sim, int *done);
+garm_status garm_sim_collect(garm_sim *sim, garm_step_stats *stats);
+/* Batched scenes: `steps` auto steps of every simulation, issued round-robin one
+ * step per scene on each scene's own stream (create the simulations with a NULL
+ * stream so each owns one).  stats (may be NULL) receives one record per scene.
+ * A scene's results do not depend on the batch it runs in. */
+garm_status garm_batch_advance_auto(garm_sim *const *sims, int count, int steps, garm_step_stats *stats);
 /* 1 when garm_sim_advance_auto replays captured step graphs (no reference counterpart). */
 garm_status garm_sim_graph_active(const garm_sim *sim, int *active);
 
