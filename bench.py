@@ -49,6 +49,8 @@ def parse():
                    help="dam: the 128^3 dam break (default line, with mixed and batch sub-objects); "
                         "batch: 48 uneven pool scenes only; serve: the Poisson request stream only")
     p.add_argument("--batch-scenes", type=int, default=48)
+    p.add_argument("--reinit-plan", default=None, metavar="FORM,THREADS,CELLS",
+                   help="pin the reinitialisation launch plan of the dam-break grid instead of autotuning it")
     p.add_argument("--requests", type=int, default=48, help="serve: number of requests")
     return p.parse_args()
 
@@ -178,7 +180,9 @@ def reinit_roofline(sim, torch, stream, n_cells: int, esz: int, iters: int, peak
     src = "measured"
     if not peak:
         peak, src = 6800.0, "fallback"
-    return {"kernel": "kReinitStage (WENO5 TVD-RK3 sub-stage)", "bound": "hbm", "achieved": round(achieved, 1),
+    plan = sim.reinit_plan()
+    name = {"cells": "kReinitCells", "columns": "kReinitColumns", "sweeps": "kWenoSweep x3"}[plan["form"]]
+    return {"kernel": f"{name} (WENO5 TVD-RK3 sub-stage)", "plan": plan, "bound": "hbm", "achieved": round(achieved, 1),
             "peak": peak, "peak_source": src, "unit": "GB/s", "frac": round(achieved / peak, 4),
             "traffic": None, "ms_per_launch": round(ms_per_launch, 4), "algorithmic_bytes_per_launch": int(bytes_per_launch)}
 
@@ -294,6 +298,10 @@ def run_garm(args) -> None:
     scene = scenes.dam_break(3, n)
     dx = scene.grid.spacing
     interior = n ** 3
+    if args.reinit_plan:
+        form, threads, cells = args.reinit_plan.split(",")
+        for prec in (capi.PRECISION_FP64, capi.PRECISION_MIXED):
+            capi.reinit_plan_set([scene.grid.resolution[a] for a in range(3)], prec, form, int(threads), int(cells))
 
     def make(precision):
         cfg = capi.default_config(precision=precision)

@@ -117,6 +117,10 @@ template <int D, typename T> garm_status finishBoundary(State &s);
 template <int D, typename T> garm_status advectFields(State &s);
 template <int D, typename T> garm_status generateCurrentFields(State &s);
 template <int D, typename T> garm_status reinitialize(State &s);
+// Launch plan (form GARM_REINIT_*, threads per block, cells per thread) the
+// reinitialisation autotuner chose for this grid, and its sub-stage time in ms.
+template <int D, typename T> garm_status reinitPlanInfo(State &s, int *form, int *block, int *chunk, float *ms);
+garm_status pinReinitPlan(int dim, int esz, const int *size, int form, int block, int chunk);
 template <int D, typename T> garm_status extrapolateToCollider(State &s);
 template <int D, typename T> garm_status checkReferenceMap(State &s, int *keep, int *tot, int *bad);
 template <int D, typename T> garm_status checkReferenceMapAsync(State &s, bool record);

@@ -6,6 +6,10 @@
 //   enforceBoundaryLevelSet (LevelSetLiquid.cpp:966-975)
 #include "garm_internal.h"
 
+#include <map>
+#include <mutex>
+#include <vector>
+
 namespace garm {
 
 // ---------------------------------------------------------------------------
@@ -92,6 +96,19 @@ garm_status generateCurrentFields(State &s) {
 // ---------------------------------------------------------------------------
 // WENO5 reinitialisation (Reinitialization.h:20-80)
 // ---------------------------------------------------------------------------
+// The scheme (Derivatives.h:134-159) builds both one-sided derivatives of a
+// cell from seven values along each axis.  Everything here is arranged around
+// one fact: the five differences that give φ⁻ of cell i+1 are the five that
+// give φ⁺ of cell i, in reverse order, so the two share their ε, their three
+// smoothness indicators and their scaled weights; they differ only in the
+// candidate stencils and in which weight goes with which stencil.  A "face
+// set" is those five differences around the face between i and i+1.
+//
+// The arithmetic differs from the reference's order of operations (each
+// one-sided derivative is a ratio num/den with the 1/(6 dx) factor applied
+// once to the squared sum), so results agree with the FP64 oracle to rounding
+// (~1e-13·dx after a full reinitialisation), not bitwise.
+
 // 2^-e for the binary exponent e of x > 0 (x normal): an exact power-of-two
 // scale built from the exponent bits, used to keep the WENO weights in range.
 __device__ __forceinline__ double pow2NegExp(double x) {
@@ -104,94 +121,466 @@ __device__ __forceinline__ float pow2NegExp(float x) {
 	return __int_as_float((127 - e) << 23);
 }
 
-// One one-sided WENO5 derivative from five differences (Derivatives.h:137-157),
-// returned without the 1/(6 dx) factor.  The three weights α_k = d_k/(s_k+ε)^2 are
-// normalised with a single division: with q_k = (s_k+ε)·2^-e (2^e ~ ε, an exact
-// scale) every q_k lies in [1/2, ~7e7], so d_k·q_i^2·q_j^2 neither overflows nor
-// underflows in FP32 or FP64, and Σα_k P_k / Σα_k = Σ w_k P_k / Σ w_k with
-// w_1 = .1 q_2^2 q_3^2, w_2 = .6 q_1^2 q_3^2, w_3 = .3 q_1^2 q_2^2.
+// max of two non-negative, non-NaN values.  For such values the IEEE bit
+// patterns order like the numbers, so an integer max gives exactly fmax and
+// keeps the FP64 pipe free.
+__device__ __forceinline__ double maxNonNeg(double a, double b) {
+	const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+	return __longlong_as_double(x > y ? x : y);
+}
+__device__ __forceinline__ float maxNonNeg(float a, float b) {
+	return __int_as_float(max(__float_as_int(a), __float_as_int(b)));
+}
+__device__ __forceinline__ bool signBit(double a) { return __double2hiint(a) < 0; }
+__device__ __forceinline__ bool signBit(float a) { return __float_as_int(a) < 0; }
+
+// 1/x for x in [2^-125, 2^125], by Newton–Raphson iteration for the reciprocal
+// (y ← y(1 + e + e²), e = 1 − x·y, the second-order form of y ← y(2 − x·y);
+// Muller et al., Handbook of Floating-Point Arithmetic, ch. 4) from the single-
+// precision hardware approximation rcp.approx.ftz.f32 (at most 1 ulp of float).
+// The FP64 seed is built with integer operations: x's exponent re-biased and the
+// top 23 bits of its mantissa make a float within 2^-23 of x, and the float
+// result widens back exactly the same way.  The seed is then within 2^-21 of
+// 1/x, one refinement leaves e³ < 2^-63, and the result is within 2 ulp of
+// the correctly rounded reciprocal.  The WENO weight sums below always lie in
+// [1, 2^106]: each scaled q lies in [1, 2^27].
+__device__ __forceinline__ double recipPos(double x) {
+	const int hi = __double2hiint(x), lo = __double2loint(x);
+	const int ex = ((hi >> 20) & 0x7ff) - 1023;
+	const unsigned man = (unsigned(hi & 0xfffff) << 3) | (unsigned(lo) >> 29);
+	const float xf = __int_as_float(((ex + 127) << 23) | int(man));
+	float yf;
+	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(xf));
+	const int yb = __float_as_int(yf);
+	const int ey = ((yb >> 23) & 0xff) - 127;
+	const double y = __hiloint2double(((ey + 1023) << 20) | ((yb & 0x7fffff) >> 3), (yb & 7) << 29);
+	const double e = fma(-x, y, 1.0);
+	return fma(y, fma(e, e, e), y);
+}
+__device__ __forceinline__ float recipPos(float x) {
+	float y;
+	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+	return fmaf(y, fmaf(-x, y, 1.0f), y);
+}
+
+template <typename T> struct WenoConst {
+	// ε floor: 1e-99 in FP64 (Derivatives.h:144); FP32 takes the smallest comparable normal number
+	static constexpr T floorEps = sizeof(T) == 8 ? T(1e-99) : T(1e-30);
+};
+
+// One one-sided derivative in ratio form.  num/den · 1/(6 dx) is the derivative.
+template <typename T> struct Ratio { T num, den; };
+
+// Scaled squared weights of a face set: with q_k = (s_k+ε)·2^-e (2^e ≤ ε < 2^(e+1),
+// an exact scale) every q_k lies in [1, ~7e7], so products of two q_k^2 neither overflow nor
+// underflow in FP32 or FP64; α_k = d_k/(s_k+ε)^2 then normalises to the same
+// weights as w_1 = .1 q_2^2 q_3^2, w_2 = .6 q_1^2 q_3^2, w_3 = .3 q_1^2 q_2^2.
+template <typename T> struct FaceWeights { T a, b, c; };  // a = t2 t3, b = .6 t1 t3, c = t1 t2
 template <typename T>
-__device__ __forceinline__ T wenoSide(T d0, T d1, T d2, T d3, T d4, T sq0, T sq1, T sq2, T sq3, T sq4, T floorEps) {
-	const T m = fmax(fmax(fmax(sq0, sq1), fmax(sq2, sq3)), sq4);
-	const T eps = fma(m, T(1e-6), floorEps);
-	const T P1 = T(2) * d0 - T(7) * d1 + T(11) * d2;   // 6·phix1
-	const T P2 = -d1 + T(5) * d2 + T(2) * d3;           // 6·phix2
-	const T P3 = T(2) * d2 + T(5) * d3 - d4;            // 6·phix3
-	const T e1 = d0 - T(2) * d1 + d2, f1 = d0 - T(4) * d1 + T(3) * d2;
-	const T e2 = d1 - T(2) * d2 + d3, f2 = d1 - d3;
-	const T e3 = d2 - T(2) * d3 + d4, f3 = T(3) * d2 - T(4) * d3 + d4;
-	const T c13 = T(13.0 / 12.0);
-	const T s1 = fma(c13 * e1, e1, T(0.25) * f1 * f1);
-	const T s2 = fma(c13 * e2, e2, T(0.25) * f2 * f2);
-	const T s3 = fma(c13 * e3, e3, T(0.25) * f3 * f3);
+__device__ __forceinline__ FaceWeights<T> faceWeights(T s1, T s2, T s3, T eps) {
 	const T sc = pow2NegExp(eps);
 	const T q1 = (s1 + eps) * sc, q2 = (s2 + eps) * sc, q3 = (s3 + eps) * sc;
 	const T t1 = q1 * q1, t2 = q2 * q2, t3 = q3 * q3;
-	const T w1 = T(0.1) * t2 * t3, w2 = T(0.6) * t1 * t3, w3 = T(0.3) * t1 * t2;
-	return (w1 * P1 + w2 * P2 + w3 * P3) / (w1 + w2 + w3);
+	return {t2 * t3, T(0.6) * (t1 * t3), t1 * t2};
 }
-
-// weno5 (Derivatives.h:134-159): one-sided derivatives (φ⁻, φ⁺) from seven values.
+// φ⁻ of the cell right of the face: stencils on (E1..E5) with weights (.1a, b, .3c).
 template <typename T>
-__device__ __forceinline__ void weno5(const T v[7], T invDx, T &dm, T &dp) {
-	// 1e-99 in FP64 (Derivatives.h:144); FP32 takes the smallest comparable normal number
-	const T floorEps = sizeof(T) == 8 ? T(1e-99) : T(1e-30);
+__device__ __forceinline__ Ratio<T> rightRole(const FaceWeights<T> &w, T P1, T P2, T P3) {
+	const T w1 = T(0.1) * w.a, w3 = T(0.3) * w.c;
+	return {fma(w1, P1, fma(w.b, P2, w3 * P3)), w1 + w.b + w3};
+}
+// φ⁺ of the cell left of the face: stencils on (E5..E1) with weights (.1c, b, .3a).
+template <typename T>
+__device__ __forceinline__ Ratio<T> leftRole(const FaceWeights<T> &w, T R1, T R2, T R3) {
+	const T w1 = T(0.1) * w.c, w3 = T(0.3) * w.a;
+	return {fma(w1, R1, fma(w.b, R2, w3 * R3)), w1 + w.b + w3};
+}
+// Smoothness indicators of (v1, v2, v3) in the three positions of a face set
+// (Derivatives.h:147-149): g = 13/12 (v1-2v2+v3)^2 is common to all three.
+template <typename T> __device__ __forceinline__ T smoothG(T a, T b, T c) { const T e = a - T(2) * b + c; return T(13.0 / 12.0) * e * e; }
+template <typename T> __device__ __forceinline__ T smoothL(T g, T a, T b, T c) { const T f = a - T(4) * b + T(3) * c; return fma(T(0.25) * f, f, g); }
+template <typename T> __device__ __forceinline__ T smoothM(T g, T a, T c) { const T f = a - c; return fma(T(0.25) * f, f, g); }
+template <typename T> __device__ __forceinline__ T smoothR(T g, T a, T b, T c) { const T f = T(3) * a - T(4) * b + c; return fma(T(0.25) * f, f, g); }
+// Candidate stencils (6× the third-order one-sided values)
+template <typename T> __device__ __forceinline__ T stencil1(T a, T b, T c) { return T(2) * a - T(7) * b + T(11) * c; }
+template <typename T> __device__ __forceinline__ T stencil2(T a, T b, T c) { return -a + T(5) * b + T(2) * c; }
+template <typename T> __device__ __forceinline__ T stencil3(T a, T b, T c) { return T(2) * a + T(5) * b - c; }
+
+// Both one-sided derivatives of one cell from its seven values along an axis
+// (weno5 of Derivatives.h:134-159): φ⁻ from the face set D1..D5, φ⁺ from D2..D6.
+// The two face sets share two g terms and two candidate stencils.
+template <typename T>
+__device__ __forceinline__ void wenoCell(const T v[7], Ratio<T> &m, Ratio<T> &p) {
 	const T D1 = v[1] - v[0], D2 = v[2] - v[1], D3 = v[3] - v[2], D4 = v[4] - v[3], D5 = v[5] - v[4], D6 = v[6] - v[5];
-	const T Q1 = D1 * D1, Q2 = D2 * D2, Q3 = D3 * D3, Q4 = D4 * D4, Q5 = D5 * D5, Q6 = D6 * D6;
-	const T k = invDx * T(1.0 / 6.0);
-	dm = wenoSide<T>(D1, D2, D3, D4, D5, Q1, Q2, Q3, Q4, Q5, floorEps) * k;
-	dp = wenoSide<T>(D6, D5, D4, D3, D2, Q6, Q5, Q4, Q3, Q2, floorEps) * k;
+	const T M = maxNonNeg(maxNonNeg(D2 * D2, D3 * D3), maxNonNeg(D4 * D4, D5 * D5));
+	const T epsM = fma(maxNonNeg(M, D1 * D1), T(1e-6), WenoConst<T>::floorEps);
+	const T epsP = fma(maxNonNeg(M, D6 * D6), T(1e-6), WenoConst<T>::floorEps);
+	const T g1 = smoothG(D1, D2, D3), g2 = smoothG(D2, D3, D4), g3 = smoothG(D3, D4, D5), g4 = smoothG(D4, D5, D6);
+	const FaceWeights<T> wm = faceWeights(smoothL(g1, D1, D2, D3), smoothM(g2, D2, D4), smoothR(g3, D3, D4, D5), epsM);
+	const FaceWeights<T> wp = faceWeights(smoothL(g2, D2, D3, D4), smoothM(g3, D3, D5), smoothR(g4, D4, D5, D6), epsP);
+	const T P2 = stencil2(D2, D3, D4), P3 = stencil3(D3, D4, D5);
+	m = rightRole(wm, stencil1(D1, D2, D3), P2, P3);
+	p = leftRole(wp, stencil1(D6, D5, D4), P3, P2);  // stencil2(D5,D4,D3) = P3, stencil3(D4,D3,D2) = P2
 }
 
-// One TVD-RK3 sub-stage: out = lin(base, in + dt*L(in)).
-// mode 0: out = adv;  mode 1: out = (3*base + adv)/4;  mode 2: out = (base + 2*adv)/3.
+// Godunov term of one axis (Reinitialization.h:60-70): for φ < 0 keep φ⁻ < 0 and
+// φ⁺ > 0, for φ ≥ 0 keep φ⁻ > 0 and φ⁺ < 0; the kept ones enter squared.  The
+// sign of a ratio is the sign of its numerator (den > 0), so the choice is made
+// on sign bits before any division.
+template <typename T>
+__device__ __forceinline__ T godunovSq(bool neg, const Ratio<T> &m, const Ratio<T> &p) {
+	const T x = signBit(m.num) == neg ? m.num * recipPos(m.den) : T(0);
+	const T y = signBit(p.num) != neg ? p.num * recipPos(p.den) : T(0);
+	return fma(x, x, y * y);
+}
+
+// The pseudo-time update of one sub-stage from the Godunov sum (raw, without the
+// (1/(6dx))^2 factor): adv = φ + Δτ·S(φ)·(1 − |∇φ|) with the smoothed sign
+// S = φ/sqrt(φ² + (dx|∇φ|)²) (Reinitialization.h:26, 72-75), then the TVD-RK3
+// combination of the sub-stage: mode 0 adv, mode 1 (3 base + adv)/4,
+// mode 2 (base + 2 adv)/3.
+template <typename T, int Mode>
+__device__ __forceinline__ T rkUpdate(T f, T rawSum, T k, T dx, T dt, const T *base, int64_t id) {
+	const T grad = sqrt(rawSum) * k;
+	const T sp = dx * grad;
+	const T sgn = f * rsqrt(fma(f, f, sp * sp));
+	const T adv = fma(dt * sgn, T(1) - grad, f);
+	if (Mode == 0) return adv;
+	if (Mode == 1) return fma(base[id], T(3), adv) * T(0.25);
+	return fma(adv, T(2), base[id]) * T(1.0 / 3.0);
+}
+
+// Cell form: one thread per cell, seven clamped loads per axis (clamp-to-edge,
+// GridBasedData.h:47).  Used where columns give too little parallelism.
 template <int D, typename T, int Mode>
-__global__ void __launch_bounds__(kBlock) kReinitStage(G<D, T> g, const T *__restrict__ in, const T *base, T *out, T dt) {
+__global__ void __launch_bounds__(kBlock) kReinitCells(G<D, T> g, const T *__restrict__ in, const T *base, T *out, T dt) {
 	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
 	if (id >= g.count()) return;
 	int i, j, k;
 	g.coord(id, i, j, k);
 	const T f = ldg(in + id);
-	// Stencil addressing: the base of the line through the cell along each axis,
-	// plus one clamped coordinate per load (clamp-to-edge, GridBasedData.h:47).
 	const int sx = g.s[0], sy = g.s[1], sz = D == 3 ? g.s[2] : 1;
 	const int sxy = sx * sy;
 	const T *line[3] = {in + (id - i), in + (id - j * sx), in + (id - k * sxy)};
 	const int lim[3] = {sx - 1, sy - 1, sz - 1};
 	const int pos[3] = {i, j, k};
 	const int str[3] = {1, sx, sxy};
+	const bool neg = f < T(0);
 	T sum = T(0);
 #pragma unroll
 	for (int a = 0; a < D; a++) {
 		T v[7];
 #pragma unroll
 		for (int t = 0; t < 7; t++) v[t] = ldg(line[a] + min(max(pos[a] + t - 3, 0), lim[a]) * str[a]);
-		T dm, dp;
-		weno5<T>(v, g.inv, dm, dp);
-		if (f < T(0)) { const T x = fmin(dm, T(0)), y = fmax(dp, T(0)); sum += x * x; sum += y * y; }
-		else { const T x = fmax(dm, T(0)), y = fmin(dp, T(0)); sum += x * x; sum += y * y; }
+		Ratio<T> m, p;
+		wenoCell<T>(v, m, p);
+		sum += godunovSq(neg, m, p);
 	}
-	sum = sqrt(sum);
-	const T sp = g.dx * sum;
-	const T sgn = f * rsqrt(f * f + sp * sp);  // smoothed sign (Reinitialization.h:26)
-	const T adv = f + dt * sgn * (T(1) - sum);
-	T r;
-	if (Mode == 0) r = adv;
-	else if (Mode == 1) r = (base[id] * T(3) + adv) / T(4);
-	else r = (base[id] + adv * T(2)) / T(3);
-	out[id] = r;
+	out[id] = rkUpdate<T, Mode>(f, sum, g.inv * T(1.0 / 6.0), g.dx, dt, base, id);
 }
 
+// Column form: each thread owns one point of the plane normal to the last axis
+// (z in 3D, y in 2D) and walks `chunk` cells along that axis with the seven
+// values in registers.  Along the walk each face set is built once and serves
+// φ⁺ of the cell below and φ⁻ of the cell above; the in-plane axes use the cell
+// form's clamped loads.  Consecutive threads hold consecutive plane points, so
+// every load and store is coalesced.
+template <int D, typename T, int Mode>
+__global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__restrict__ in, const T *base, T *out, T dt, int chunk) {
+	constexpr int W = D - 1;
+	const int sx = g.s[0], sy = D == 3 ? g.s[1] : 1;
+	const int plane = sx * sy;
+	const int pidx = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pidx >= plane) return;
+	const int sw = g.s[W];
+	const int w0 = blockIdx.y * chunk;
+	if (w0 >= sw) return;
+	const int w1 = min(w0 + chunk, sw);
+	const int j = D == 3 ? pidx / sx : 0;
+	const int i = pidx - j * sx;
+	const T *col = in + pidx;
+	const T k6 = g.inv * T(1.0 / 6.0);
+	// window v[t] = φ at w - 3 + t (clamped)
+	T v[7];
+#pragma unroll
+	for (int t = 0; t < 7; t++) v[t] = ldg(col + int64_t(min(max(w0 - 3 + t, 0), sw - 1)) * plane);
+	// φ⁻ of cell w0 from the face set below it (values w0-3 .. w0+2)
+	Ratio<T> mW;
+	{
+		const T E1 = v[1] - v[0], E2 = v[2] - v[1], E3 = v[3] - v[2], E4 = v[4] - v[3], E5 = v[5] - v[4];
+		const T Q = maxNonNeg(maxNonNeg(maxNonNeg(E1 * E1, E2 * E2), maxNonNeg(E3 * E3, E4 * E4)), E5 * E5);
+		const T eps = fma(Q, T(1e-6), WenoConst<T>::floorEps);
+		const FaceWeights<T> fw = faceWeights(smoothL(smoothG(E1, E2, E3), E1, E2, E3), smoothM(smoothG(E2, E3, E4), E2, E4),
+		                                      smoothR(smoothG(E3, E4, E5), E3, E4, E5), eps);
+		mW = rightRole(fw, stencil1(E1, E2, E3), stencil2(E2, E3, E4), stencil3(E3, E4, E5));
+	}
+	// differences, their squares and the g terms carried along the walk:
+	// E[t] = v[t+1] - v[t] for the face set above the current cell (t = 1..5)
+	T E1 = v[2] - v[1], E2 = v[3] - v[2], E3 = v[4] - v[3], E4 = v[5] - v[4], E5 = v[6] - v[5];
+	T S1 = E1 * E1, S2 = E2 * E2, S3 = E3 * E3, S4 = E4 * E4, S5 = E5 * E5;
+	T gA = smoothG(E1, E2, E3), gB = smoothG(E2, E3, E4);
+	const int64_t pstride = plane;
+	for (int w = w0; w < w1; w++) {
+		const int64_t id = int64_t(w) * pstride + pidx;
+		const T f = v[3];
+		const bool neg = f < T(0);
+		// face set above cell w: E1..E5 (values w-2 .. w+3)
+		const T gC = smoothG(E3, E4, E5);
+		const T Q = maxNonNeg(maxNonNeg(maxNonNeg(S1, S2), maxNonNeg(S3, S4)), S5);
+		const FaceWeights<T> fw = faceWeights(smoothL(gA, E1, E2, E3), smoothM(gB, E2, E4), smoothR(gC, E3, E4, E5),
+		                                      fma(Q, T(1e-6), WenoConst<T>::floorEps));
+		const Ratio<T> pW = leftRole(fw, stencil1(E5, E4, E3), stencil2(E4, E3, E2), stencil3(E3, E2, E1));
+		const Ratio<T> mNext = rightRole(fw, stencil1(E1, E2, E3), stencil2(E2, E3, E4), stencil3(E3, E4, E5));
+		T sum = godunovSq(neg, mW, pW);
+		// in-plane axes
+#pragma unroll
+		for (int a = 0; a < D - 1; a++) {
+			const int c = a == 0 ? i : j, lim = (a == 0 ? sx : sy) - 1, str = a == 0 ? 1 : sx;
+			const T *line = in + (id - int64_t(c) * str);
+			T u[7];
+#pragma unroll
+			for (int t = 0; t < 7; t++) u[t] = ldg(line + min(max(c + t - 3, 0), lim) * str);
+			Ratio<T> m, p;
+			wenoCell<T>(u, m, p);
+			sum += godunovSq(neg, m, p);
+		}
+		out[id] = rkUpdate<T, Mode>(f, sum, k6, g.dx, dt, base, id);
+		// slide the window one cell up
+		if (w + 1 < w1) {
+#pragma unroll
+			for (int t = 0; t < 6; t++) v[t] = v[t + 1];
+			v[6] = ldg(col + int64_t(min(w + 4, sw - 1)) * plane);
+			E1 = E2; E2 = E3; E3 = E4; E4 = E5; E5 = v[6] - v[5];
+			S1 = S2; S2 = S3; S3 = S4; S4 = S5; S5 = E5 * E5;
+			gA = gB; gB = gC;
+			mW = mNext;
+		}
+	}
+}
+
+// Sweep form: three passes per sub-stage, one per axis (x, then y, then z).
+// Each thread owns a line along the pass's axis and walks `chunk` cells of it;
+// every face set of the line is built once and serves φ⁺ of the cell below it
+// and φ⁻ of the cell above it.  The faces use the arrangement of Jiang & Peng
+// (2000, "Weighted ENO schemes for Hamilton-Jacobi equations"), an exact
+// rewrite of the same weights: a central part 12C(i) = 7(D_i + D_{i+1}) -
+// (D_{i-1} + D_{i+2}) shared by both one-sided derivatives of cell i, and a
+// correction in the face's third differences T1 = a-2b+c, T2 = b-2c+d of its
+// second differences a..d, whose smoothness indicators are
+// 13(x-y)^2 + 3(..)^2 (12 times the reference's, with ε scaled by 12 alike):
+//   12 φ⁻(i+1) = 12C(i+1) + T2 - (.4 t2t3 T1 + .6 t1t2 T2) / (.1 t2t3 + .6 t1t3 + .3 t1t2)
+//   12 φ⁺(i)   = 12C(i)   - T1 + (.4 t1t2 T2 + .6 t2t3 T1) / (.1 t1t2 + .6 t1t3 + .3 t2t3)
+// Differences, squares, g terms, third differences and central parts slide
+// with the walk, so a face costs about 57 operations against ~116 per axis of
+// the cell form.  The Godunov sum of the first passes goes to `out` (x pass:
+// stored, y pass: added); the last pass adds its own and applies the update.
+template <typename T> __device__ __forceinline__ T g13(T x, T y) { const T d = x - y; return (T(13) * d) * d; }
+
+template <int D, typename T, int A, int Mode>
+__global__ void __launch_bounds__(256) kWenoSweep(G<D, T> g, const T *__restrict__ in, const T *base, T *out, T dt, int chunk) {
+	constexpr int Stage = A == 0 ? 0 : (A == D - 1 ? 2 : 1);
+	const int sx = g.s[0], sy = g.s[1], sz = D == 3 ? g.s[2] : 1;
+	const int len = g.s[A];
+	const int nLines = A == 0 ? sy * sz : (A == 1 ? sx * sz : sx * sy);
+	const int L = blockIdx.x * blockDim.x + threadIdx.x;
+	if (L >= nLines) return;
+	const int w0 = blockIdx.y * chunk;
+	if (w0 >= len) return;
+	const int w1 = min(w0 + chunk, len);
+	int64_t lb, st;
+	if (A == 0) { lb = int64_t(L) * sx; st = 1; }
+	else if (A == 1) { const int z = L / sx; lb = int64_t(z) * sx * sy + (L - z * sx); st = sx; }
+	else { lb = L; st = int64_t(sx) * sy; }
+	const T *line = in + lb;
+	const int last = len - 1;
+	auto ld = [&](int w) { return ldg(line + int64_t(min(max(w, 0), last)) * st); };
+	const T epsFloor = sizeof(T) == 8 ? T(1.2e-98) : T(1.2e-29);  // 12 x the reference's ε floor
+	// state before the face f0 = w0 - 1 (between cells w0-1 and w0): φ_{f0-2 .. f0+2}
+	const int f0 = w0 - 1;
+	const T p0 = ld(f0 - 2), p1 = ld(f0 - 1);
+	T phiF = ld(f0), phiF1 = ld(f0 + 1), phiF2 = ld(f0 + 2);
+	T E1 = p1 - p0, E2 = phiF - p1, E3 = phiF1 - phiF, E4 = phiF2 - phiF1;   // D_{f-1} .. D_{f+2}
+	T Q1 = E1 * E1, Q2 = E2 * E2, Q3 = E3 * E3, Q4 = E4 * E4;
+	T a = E2 - E1, b = E3 - E2, c = E4 - E3;                                // Δ_f .. Δ_{f+2}
+	T gab = g13(a, b), gbc = g13(b, c);
+	T T1 = fma(T(-2), b, a + c);
+	T T1x4 = T(0.4) * T1, T1x6 = T(0.6) * T1;
+	T C12 = T(0), dmCarry = T(0);
+	const T k = g.inv * T(1.0 / 12.0);
+	for (int f = f0; f < w1; f++) {
+		const T pn = ld(f + 3);
+		const T E5 = pn - phiF2, Q5 = E5 * E5;
+		const T d = E5 - E4;
+		const T T2 = fma(T(-2), c, b + d);
+		const T T2x4 = T(0.4) * T2, T2x6 = T(0.6) * T2;
+		const T gcd = g13(c, d);
+		const T l0 = fma(T(-3), b, a), l1 = b + c, l2 = fma(T(3), c, -d);
+		const T is0 = fma(T(3) * l0, l0, gab), is1 = fma(T(3) * l1, l1, gbc), is2 = fma(T(3) * l2, l2, gcd);
+		const T Qm = maxNonNeg(maxNonNeg(maxNonNeg(Q1, Q2), maxNonNeg(Q3, Q4)), Q5);
+		const T eps = fma(Qm, T(1.2e-5), epsFloor);
+		const T sc = pow2NegExp(eps), es = eps * sc;
+		const T q1 = fma(is0, sc, es), q2 = fma(is1, sc, es), q3 = fma(is2, sc, es);
+		const T t1 = q1 * q1, t2 = q2 * q2, t3 = q3 * q3;
+		const T Aw = t2 * t3, Bw = T(0.6) * (t1 * t3), Cw = t1 * t2;
+		const T Cn = fma(T(7), E3 + E4, -(E2 + E5));                            // 12 C(f+1)
+		const T denR = fma(T(0.3), Cw, fma(T(0.1), Aw, Bw));
+		const T numR = fma(Aw, T1x4, Cw * T2x6);
+		const T dmNext = fma(-numR, recipPos(denR), Cn + T2);                   // 12 φ⁻(f+1)
+		if (f >= w0) {
+			const T denL = fma(T(0.3), Aw, fma(T(0.1), Cw, Bw));
+			const T numL = fma(Cw, T2x4, Aw * T1x6);
+			const T dpF = fma(numL, recipPos(denL), C12 - T1);                  // 12 φ⁺(f)
+			const bool neg = phiF < T(0);
+			const T x = signBit(dmCarry) == neg ? dmCarry : T(0);
+			const T y = signBit(dpF) != neg ? dpF : T(0);
+			const T sum = fma(x, x, y * y);
+			const int64_t id = lb + int64_t(f) * st;
+			if (Stage == 0) out[id] = sum;
+			else if (Stage == 1) out[id] = out[id] + sum;
+			else out[id] = rkUpdate<T, Mode>(phiF, out[id] + sum, k, g.dx, dt, base, id);
+		}
+		dmCarry = dmNext; C12 = Cn;
+		E1 = E2; E2 = E3; E3 = E4; E4 = E5;
+		Q1 = Q2; Q2 = Q3; Q3 = Q4; Q4 = Q5;
+		a = b; b = c; c = d;
+		gab = gbc; gbc = gcd;
+		T1 = T2; T1x4 = T2x4; T1x6 = T2x6;
+		phiF = phiF1; phiF1 = phiF2; phiF2 = pn;
+	}
+}
+
+// Launch plan of the reinitialisation sub-stages for one grid shape: the cell
+// form, the column form or the sweep form, with `block` threads and `chunk`
+// cells per thread.  Chosen by timing (reinitPlanFor) and cached per device
+// and shape.
+enum ReinitForm { kFormCells = GARM_REINIT_CELLS, kFormColumns = GARM_REINIT_COLUMNS, kFormSweeps = GARM_REINIT_SWEEPS };
+struct ReinitPlan { int form = kFormColumns, block = 128, chunk = 8; float ms = 0; };
+
+template <int D, typename T, int A, int Mode>
+static void launchSweep(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g, const T *in, const T *base, T *out, T dt) {
+	const int sx = g.s[0], sy = g.s[1], sz = D == 3 ? g.s[2] : 1;
+	const int nLines = A == 0 ? sy * sz : (A == 1 ? sx * sz : sx * sy);
+	const dim3 grid((nLines + pl.block - 1) / pl.block, (g.s[A] + pl.chunk - 1) / pl.chunk);
+	kWenoSweep<D, T, A, Mode><<<grid, pl.block, 0, st>>>(g, in, base, out, dt, pl.chunk);
+}
+
+// One sub-stage; returns the number of kernels launched.
+template <int D, typename T, int Mode>
+static int launchReinit(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g, const T *in, const T *base, T *out, T dt) {
+	if (pl.form == kFormCells) {
+		kReinitCells<D, T, Mode><<<gridFor(g.count()), kBlock, 0, st>>>(g, in, base, out, dt);
+		return 1;
+	}
+	if (pl.form == kFormSweeps) {
+		launchSweep<D, T, 0, Mode>(pl, st, g, in, base, out, dt);
+		launchSweep<D, T, 1, Mode>(pl, st, g, in, base, out, dt);
+		if (D == 3) launchSweep<D, T, D == 3 ? 2 : 1, Mode>(pl, st, g, in, base, out, dt);
+		return D;
+	}
+	const int plane = g.s[0] * (D == 3 ? g.s[1] : 1);
+	const int sw = g.s[D - 1];
+	const dim3 grid((plane + pl.block - 1) / pl.block, (sw + pl.chunk - 1) / pl.chunk);
+	kReinitColumns<D, T, Mode><<<grid, pl.block, 0, st>>>(g, in, base, out, dt, pl.chunk);
+	return 1;
+}
+
+namespace {
+struct PlanKey {
+	int dev, dim, esz, s0, s1, s2;
+	bool operator<(const PlanKey &o) const {
+		const int a[6] = {dev, dim, esz, s0, s1, s2}, b[6] = {o.dev, o.dim, o.esz, o.s0, o.s1, o.s2};
+		for (int q = 0; q < 6; q++) if (a[q] != b[q]) return a[q] < b[q];
+		return false;
+	}
+};
+std::mutex g_planMutex;
+std::map<PlanKey, ReinitPlan> g_plans;
+}  // namespace
+
+// The launch plan for this shape.  The first time a shape is seen on a device
+// (outside stream capture) every candidate runs sub-stage 0 (in → out only, so
+// the field is untouched) twice on the caller's stream and the fastest is kept;
+// the tuning synchronises that stream once.  Under capture, or when a timing
+// call fails, the plan is the default column form and nothing is cached.
+template <int D, typename T>
+static ReinitPlan reinitPlanFor(cudaStream_t st, const G<D, T> &g, const T *phi, T *scratch, T dt) {
+	int dev = 0;
+	cudaGetDevice(&dev);
+	const PlanKey key{dev, D, int(sizeof(T)), g.s[0], g.s[1], D == 3 ? g.s[2] : 1};
+	{
+		std::lock_guard<std::mutex> lock(g_planMutex);
+		auto it = g_plans.find(key);
+		if (it != g_plans.end()) return it->second;
+	}
+	ReinitPlan best;
+	cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+	if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) { cudaGetLastError(); return best; }
+	std::vector<ReinitPlan> cand;
+	cand.push_back({kFormCells, kBlock, 0});
+	for (int b : {64, 128, 256})
+		for (int c : {4, 8, 16, 32}) cand.push_back({kFormColumns, b, c});
+	for (int b : {64, 128, 256})
+		for (int c : {8, 16, 32, 64}) cand.push_back({kFormSweeps, b, c});
+	cudaEvent_t e0, e1;
+	if (cudaEventCreate(&e0) != cudaSuccess) { cudaGetLastError(); return best; }
+	if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); cudaGetLastError(); return best; }
+	bool ok = true;
+	float bestMs = 1e30f;
+	for (ReinitPlan &c : cand) {
+		launchReinit<D, T, 0>(c, st, g, phi, nullptr, scratch, dt);  // warm
+		cudaEventRecord(e0, st);
+		launchReinit<D, T, 0>(c, st, g, phi, nullptr, scratch, dt);
+		cudaEventRecord(e1, st);
+		if (cudaEventSynchronize(e1) != cudaSuccess) { ok = false; break; }
+		float ms = 0;
+		cudaEventElapsedTime(&ms, e0, e1);
+		c.ms = ms;
+		if (ms < bestMs) { bestMs = ms; best = c; }
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	if (!ok || cudaGetLastError() != cudaSuccess) return ReinitPlan{};
+	std::lock_guard<std::mutex> lock(g_planMutex);
+	g_plans[key] = best;
+	return best;
+}
+
+// Pin (or, with block 0, forget) the plan of one shape on the current device.
+garm_status pinReinitPlan(int dim, int esz, const int *size, int form, int block, int chunk) {
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return GARM_CUDA_ERROR; }
+	const PlanKey key{dev, dim, esz, size[0], size[1], dim == 3 ? size[2] : 1};
+	std::lock_guard<std::mutex> lock(g_planMutex);
+	if (block == 0) { g_plans.erase(key); return GARM_OK; }
+	ReinitPlan pl;
+	pl.form = form;
+	pl.block = form == kFormCells ? kBlock : block;
+	pl.chunk = form == kFormCells ? 0 : chunk;
+	g_plans[key] = pl;
+	return GARM_OK;
+}
+
+// Reinitialisation::solve<5> with TVD-RK3 (Reinitialization.h:50-80).  The three
+// planes rotate roles every iteration (u0 → X → Y → X holds u0's successor), so
+// no sub-stage writes a plane it reads; after a multiple of three iterations the
+// result is back in phi, otherwise one copy puts it there.
 template <int D, typename T>
 static garm_status reinitLoop(cudaStream_t st, const G<D, T> &g, T *phi, T *A, T *B, int iters, double cfl, long long *launches) {
 	const T dt = T(double(g.dx) * cfl);
-	const unsigned nb = gridFor(g.count());
+	if (iters <= 0) return GARM_OK;
+	const ReinitPlan pl = reinitPlanFor<D, T>(st, g, phi, A, dt);
+	T *buf[3] = {phi, A, B};
+	int cur = 0, n = 0;
 	for (int it = 0; it < iters; it++) {
-		kReinitStage<D, T, 0><<<nb, kBlock, 0, st>>>(g, phi, nullptr, A, dt);
-		kReinitStage<D, T, 1><<<nb, kBlock, 0, st>>>(g, A, phi, B, dt);
-		kReinitStage<D, T, 2><<<nb, kBlock, 0, st>>>(g, B, phi, phi, dt);
-		if (launches) *launches += 3;
+		T *u0 = buf[cur], *X = buf[(cur + 1) % 3], *Y = buf[(cur + 2) % 3];
+		n += launchReinit<D, T, 0>(pl, st, g, u0, nullptr, X, dt);
+		n += launchReinit<D, T, 1>(pl, st, g, X, u0, Y, dt);
+		n += launchReinit<D, T, 2>(pl, st, g, Y, u0, X, dt);
+		cur = (cur + 1) % 3;
 	}
+	if (cur != 0 && cudaMemcpyAsync(phi, buf[cur], size_t(g.count()) * sizeof(T), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+		return GARM_CUDA_ERROR;
+	if (launches) *launches += n;
 	GARM_CHECK_LAUNCH();
 	return GARM_OK;
 }
@@ -200,6 +589,15 @@ template <int D, typename T>
 garm_status reinitialize(State &s) {
 	const G<D, T> g = cellGrid<D, T>(s.geom);
 	return reinitLoop<D, T>(s.stream, g, (T *)s.phi, (T *)s.rA, (T *)s.rB, s.cfg.reinit_iters, s.cfg.reinit_cfl, &s.launches);
+}
+
+// The cached (or freshly tuned) plan of this simulation's grid, for reporting.
+template <int D, typename T>
+garm_status reinitPlanInfo(State &s, int *form, int *block, int *chunk, float *ms) {
+	const G<D, T> g = cellGrid<D, T>(s.geom);
+	const ReinitPlan pl = reinitPlanFor<D, T>(s.stream, g, (const T *)s.phi, (T *)s.rA, T(double(g.dx) * s.cfg.reinit_cfl));
+	*form = pl.form; *block = pl.block; *chunk = pl.chunk; *ms = pl.ms;
+	return GARM_OK;
 }
 
 template <int D, typename T>
@@ -416,6 +814,7 @@ garm_status enforceBoundaryLevelSet(State &s, void *field, double tol) {
 #define GARM_INST(D, T) \
 	template garm_status generateCurrentFields<D, T>(State &); \
 	template garm_status reinitialize<D, T>(State &); \
+	template garm_status reinitPlanInfo<D, T>(State &, int *, int *, int *, float *); \
 	template garm_status reinitRaw<D, T>(cudaStream_t, const int *, double, T *, T *, T *, int, double); \
 	template garm_status checkReferenceMap<D, T>(State &, int *, int *, int *); \
 	template garm_status checkReferenceMapAsync<D, T>(State &, bool); \

@@ -20,6 +20,7 @@ STATUS_NAMES = {OK: "ok", INVALID: "invalid", OOM: "oom", NOT_CONVERGED: "not_co
                 CUDA_ERROR: "cuda_error", TIMEOUT: "timeout", UNSUPPORTED: "unsupported"}
 
 PRECISION_FP64, PRECISION_MIXED = 0, 1
+REINIT_FORMS = ["cells", "columns", "sweeps"]  # GARM_REINIT_CELLS, _COLUMNS, _SWEEPS
 
 # garm_field
 (FIELD_VELOCITY, FIELD_LEVEL_SET, FIELD_REF_MAP, FIELD_REF_MAP_GRAD, FIELD_REF_LEVEL_SET, FIELD_REF_LEVEL_SET_GRAD,
@@ -87,6 +88,9 @@ _SIGS = {
     "garm_sim_set_clock": (C.c_int, [C.c_void_p, C.c_uint, C.c_double]),
     "garm_sim_advance_auto": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(StepStats)]),
     "garm_sim_graph_active": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "garm_reinit_plan_set": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int, C.c_int, C.c_int]),
+    "garm_sim_reinit_plan": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                       C.POINTER(C.c_float)]),
     "garm_sim_enqueue_auto": (C.c_int, [C.c_void_p, C.c_int]),
     "garm_sim_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "garm_sim_collect": (C.c_int, [C.c_void_p, C.POINTER(StepStats)]),
@@ -280,6 +284,12 @@ class Simulation:
         check(self.lib.garm_sim_graph_active(self.handle, C.byref(v)), "garm_sim_graph_active")
         return bool(v.value)
 
+    def reinit_plan(self) -> dict:
+        f, b, c, ms = C.c_int(), C.c_int(), C.c_int(), C.c_float()
+        check(self.lib.garm_sim_reinit_plan(self.handle, C.byref(f), C.byref(b), C.byref(c), C.byref(ms)),
+              "garm_sim_reinit_plan")
+        return {"form": REINIT_FORMS[f.value], "threads": b.value, "cells_per_thread": c.value, "ms": ms.value}
+
     def max_speed(self) -> float:
         v = C.c_double()
         check(self.lib.garm_sim_max_speed(self.handle, C.byref(v)), "garm_sim_max_speed")
@@ -343,6 +353,14 @@ def reinit_host(phi: np.ndarray, spacing: float, iters: int, cfl: float, precisi
     check(lib.garm_reinit_host(dim, size, float(spacing), a.ctypes.data_as(C.POINTER(C.c_double)), int(iters), float(cfl),
                                int(precision)), "garm_reinit_host")
     return a
+
+
+def reinit_plan_set(shape_xyz, precision: int, form: str, threads: int, cells_per_thread: int) -> None:
+    """Pin the reinitialisation launch plan of one grid shape (cells per axis, x first):
+    form "cells" | "columns" | "sweeps"; threads=0 returns the shape to the autotuner."""
+    size = (C.c_int * 3)(*([int(x) for x in shape_xyz] + [1] * (3 - len(shape_xyz))))
+    check(load().garm_reinit_plan_set(len(shape_xyz), int(precision), size, REINIT_FORMS.index(form), int(threads),
+                                      int(cells_per_thread)), "garm_reinit_plan_set")
 
 
 def batch_advance_auto(sims: list, steps: int) -> list:

@@ -168,6 +168,23 @@ garm_status garm_sim_collect(garm_sim *sim, garm_step_stats *stats);
 garm_status garm_batch_advance_auto(garm_sim *const *sims, int count, int steps, garm_step_stats *stats);
 /* 1 when garm_sim_advance_auto replays captured step graphs (no reference counterpart). */
 garm_status garm_sim_graph_active(const garm_sim *sim, int *active);
+/* Launch forms of the WENO5 reinitialisation sub-stages (no reference counterpart):
+ * one thread per cell; threads walking columns along the last axis; or one pass
+ * per axis, threads walking lines of that axis. */
+#define GARM_REINIT_CELLS 0
+#define GARM_REINIT_COLUMNS 1
+#define GARM_REINIT_SWEEPS 2
+/* The launch plan the reinitialisation autotuner chose for this simulation's grid:
+ * form, threads per block, cells each thread walks and the timed sub-stage in ms.
+ * Plans are tuned once per grid shape, precision and device in the process, on
+ * first use outside stream capture. */
+garm_status garm_sim_reinit_plan(garm_sim *sim, int *form, int *threads, int *cells_per_thread, float *ms);
+/* Pin the reinitialisation plan of one grid shape (cell counts per axis, storage
+ * layout) and precision on the current device, replacing the autotuner's choice.
+ * For the column and sweep forms threads is 32..256 (a multiple of 32) and
+ * cells_per_thread >= 1; the cell form ignores both.  threads 0 forgets the
+ * pinned or tuned plan, so the next use tunes again. */
+garm_status garm_reinit_plan_set(int dim, int precision, const int *size, int form, int threads, int cells_per_thread);
 
 /* max over faces of |u| (GridBasedData::normMax, Source/Core/GridBasedData.h:55-68). */
 garm_status garm_sim_max_speed(garm_sim *sim, double *out);

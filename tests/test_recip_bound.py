@@ -1,0 +1,56 @@
+"""Error bound of the WENO weight normalisation's reciprocal, checked on the CPU.
+
+The device computes 1/x for x in [1, 2^106] from a single-precision seed (x's
+mantissa truncated to 23 bits, the hardware rcp.approx.f32 result, at most 1 ulp
+of float off) refined once by the Newton–Raphson step y(1 + e + e^2) with
+e = fma(-x, y, 1).  Here the seed is emulated with its worst cases (truncation
+plus a ±1-ulp float reciprocal) and the FP64 fused operations are evaluated
+exactly and rounded once, as a fused multiply-add does.
+"""
+from __future__ import annotations
+
+import random
+from fractions import Fraction
+
+import numpy as np
+
+
+def fma(a: float, b: float, c: float) -> float:
+    return float(Fraction(a) * Fraction(b) + Fraction(c))
+
+
+def seed(x: float, ulps: int) -> float:
+    xf = np.float32(x)
+    # truncate (not round) the mantissa to float precision
+    bits = np.float64(x).view(np.uint64)
+    trunc = (bits >> np.uint64(29)) << np.uint64(29)
+    xt = float(np.uint64(trunc).view(np.float64))
+    assert abs(xt - float(xf)) <= abs(float(xf)) * 2.0 ** -23
+    y = np.float32(1.0) / np.float32(xt)
+    for _ in range(abs(ulps)):
+        y = np.nextafter(y, np.float32(np.inf) if ulps > 0 else np.float32(0))
+    return float(y)
+
+
+def refine(x: float, y: float) -> float:
+    e = fma(-x, y, 1.0)
+    return fma(y, fma(e, e, e), y)
+
+
+def test_reciprocal_within_two_ulp():
+    rng = random.Random(5)
+    worst = 0.0
+    for n in range(3000):
+        x = 2.0 ** rng.uniform(0.0, 106.0)
+        for ulps in (-1, 0, 1):
+            r = refine(x, seed(x, ulps))
+            exact = 1 / Fraction(x)
+            rel = abs(Fraction(r) - exact) / exact
+            worst = max(worst, float(rel))
+    assert worst <= 2.0 ** -52, worst  # two ulp of the correctly rounded value
+
+
+def test_reciprocal_edges():
+    for x in (1.0, 2.0 ** 106, 1.5, 3.0, 7.0, 2.0 ** 53 - 1):
+        r = refine(x, seed(x, 1))
+        assert abs(Fraction(r) * Fraction(x) - 1) <= Fraction(2) ** -52

@@ -1,0 +1,86 @@
+"""The two arrangements of the WENO5 one-sided derivatives used by the kernels,
+restated in numpy and checked against the reference's form (Derivatives.h:134-159,
+as the oracle computes it) on random lines.
+
+Face form: the face between cells i and i+1 has five first differences
+E1..E5 (φ_{i-2..i+3}); its second differences a, b, c, d give the smoothness
+indicators (scaled by 12, with ε scaled alike) and its third differences
+T1 = a-2b+c, T2 = b-2c+d.  With the central part 12C(i) = 7(D_i + D_{i+1}) -
+(D_{i-1} + D_{i+2}) (Jiang & Peng 2000, "Weighted ENO schemes for Hamilton-Jacobi
+equations"), one face gives both
+    12 φ⁻(i+1) = 12C(i+1) + T2 - (.4 t2t3 T1 + .6 t1t2 T2) / (.1 t2t3 + .6 t1t3 + .3 t1t2)
+    12 φ⁺(i)   = 12C(i)   - T1 + (.4 t1t2 T2 + .6 t2t3 T1) / (.1 t1t2 + .6 t1t3 + .3 t2t3)
+with t_k = ((IS_k + ε')·2^-e)^2, 2^e ≤ ε' < 2^(e+1) (an exact scale that keeps the
+products of two t_k in range).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def reference_weno(v):
+    """weno5 of the oracle: (dm, dp) in difference units (no 1/dx) from 7 values."""
+    out = []
+    for side in (0, 1):
+        if side:
+            dev = [v[6] - v[5], v[5] - v[4], v[4] - v[3], v[3] - v[2], v[2] - v[1]]
+        else:
+            dev = [v[1] - v[0], v[2] - v[1], v[3] - v[2], v[4] - v[3], v[5] - v[4]]
+        eps = max(d * d for d in dev) * 1e-6 + 1e-99
+        p1 = dev[0] / 3 - dev[1] * 7 / 6 + dev[2] * 11 / 6
+        p2 = -dev[1] / 6 + dev[2] * 5 / 6 + dev[3] / 3
+        p3 = dev[2] / 3 + dev[3] * 5 / 6 - dev[4] / 6
+        s1 = (dev[0] - 2 * dev[1] + dev[2]) ** 2 * 13 / 12 + (dev[0] - 4 * dev[1] + 3 * dev[2]) ** 2 / 4
+        s2 = (dev[1] - 2 * dev[2] + dev[3]) ** 2 * 13 / 12 + (dev[1] - dev[3]) ** 2 / 4
+        s3 = (dev[2] - 2 * dev[3] + dev[4]) ** 2 * 13 / 12 + (3 * dev[2] - 4 * dev[3] + dev[4]) ** 2 / 4
+        a1, a2, a3 = .1 / (s1 + eps) ** 2, .6 / (s2 + eps) ** 2, .3 / (s3 + eps) ** 2
+        out.append((a1 * p1 + a2 * p2 + a3 * p3) / (a1 + a2 + a3))
+    return out
+
+
+def face_form(phi):
+    """(12 φ⁻, 12 φ⁺) of every cell of a clamped line, built face by face."""
+    n = len(phi)
+    at = lambda k: phi[min(max(k, 0), n - 1)]
+    dm, dp = np.zeros(n), np.zeros(n)
+    for f in range(-1, n):                      # face between f and f+1
+        E = [at(f - 1 + q) - at(f - 2 + q) for q in range(5)]   # D_{f-1} .. D_{f+3}
+        a, b, c, d = E[1] - E[0], E[2] - E[1], E[3] - E[2], E[4] - E[3]
+        T1, T2 = a - 2 * b + c, b - 2 * c + d
+        is0 = 13 * (a - b) ** 2 + 3 * (a - 3 * b) ** 2
+        is1 = 13 * (b - c) ** 2 + 3 * (b + c) ** 2
+        is2 = 13 * (c - d) ** 2 + 3 * (3 * c - d) ** 2
+        eps = 12 * (max(e * e for e in E) * 1e-6 + 1e-99)
+        sc = 2.0 ** -np.floor(np.log2(eps))          # exact power-of-two scale, as on the device
+        t1, t2, t3 = ((is0 + eps) * sc) ** 2, ((is1 + eps) * sc) ** 2, ((is2 + eps) * sc) ** 2
+        A, B, Cc = t2 * t3, .6 * t1 * t3, t1 * t2
+        C_left = 7 * (E[1] + E[2]) - (E[0] + E[3])     # cell f
+        C_right = 7 * (E[2] + E[3]) - (E[1] + E[4])    # cell f+1
+        if f + 1 < n:
+            dm[f + 1] = C_right + T2 - (.4 * A * T1 + .6 * Cc * T2) / (.1 * A + B + .3 * Cc)
+        if f >= 0:
+            dp[f] = C_left - T1 + (.4 * Cc * T2 + .6 * A * T1) / (.1 * Cc + B + .3 * A)
+    return dm, dp
+
+
+def test_face_form_matches_reference():
+    rng = np.random.default_rng(0)
+    for trial in range(40):
+        n = int(rng.integers(1, 24))
+        kind = trial % 4
+        x = np.arange(n) * 0.1
+        if kind == 0:
+            phi = rng.normal(size=n)
+        elif kind == 1:
+            phi = np.abs(x - rng.uniform(0, n * 0.1)) - 0.3          # kink
+        elif kind == 2:
+            phi = np.full(n, rng.normal())                             # flat: ε floor only
+        else:
+            phi = np.cumsum(rng.normal(size=n)) * 1e-3
+        dm, dp = face_form(phi)
+        for i in range(n):
+            v = [phi[min(max(i + t - 3, 0), n - 1)] for t in range(7)]
+            rm, rp = reference_weno(v)
+            scale = max(1e-300, max(abs(q) for q in np.diff(v)) if n > 1 else 1.0)
+            assert abs(dm[i] / 12 - rm) <= 1e-12 * scale, (trial, i)
+            assert abs(dp[i] / 12 - rp) <= 1e-12 * scale, (trial, i)
