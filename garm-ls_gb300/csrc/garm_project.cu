@@ -164,8 +164,8 @@ struct CgArgs {
 	int *err;
 	double tol;
 	int maxIter;
-	double innerTol;
-	int maxRefine;
+	double drop;        // mixed: residual reduction that triggers an FP64 residual replacement
+	int replaceEvery;   // mixed: replace at least every this many iterations (0: only on the drop)
 	double *scal;  // [0] relative residual, [1] tolerance used
 	int *ints;     // [0] matvecs, [1] refinements
 };
@@ -475,55 +475,251 @@ __global__ void __launch_bounds__(kCgBlock) kPcgFp64(CgArgs a) {
 	}
 }
 
-// Mixed form: FP64 iterative refinement around FP32 inner PCG sweeps.
-//   x64 = 0; repeat: r64 = b - A64 x64 (FP64); stop when |r64| <= tol |b|;
-//   solve A32 e = r64 (FP32 vectors, FP64 reductions) to innerTol; x64 += e.
+// Mixed form: one FP32 PCG (the Chronopoulos–Gear iteration of pcgCore, FP32
+// vectors and element arithmetic, FP64 reductions and scalars) with FP64
+// residual replacement (van der Vorst & Ye, "Residual replacement strategies
+// for Krylov subspace iterative methods", SIAM J. Sci. Comput. 22, 2000, as
+// used by reliable-update mixed-precision CG).  The FP32 iterates x32 are a
+// correction to the FP64 solution x64.  Whenever the recursive residual has
+// dropped by the factor `drop` since the last replacement, or looks converged:
+//   x64 += x32, x32 = 0;  r = b - A64 x64 in FP64 (the convergence test uses
+//   this true residual only);  r32 = r;  u = M^-1 r32, w = A32 u recomputed;
+// and the iteration continues with the same search direction p and s = A p,
+// β and α formed from the new γ = r·u, δ = w·u by the usual recurrences.  No
+// Krylov information is discarded, so the iteration count stays close to the
+// FP64 solver's, while the residual the solve reports is FP64-exact.
+// Returns in outs: matvecs, replacements, relative true residual, tolerance.
+template <int NB, bool Reg>
+__device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &epoch, int &itOut, int &replOut, double &relOut, double &tolOut) {
+	using V = float;
+	using E = NbW32;
+	const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x, nthr = int64_t(gridDim.x) * blockDim.x;
+	const int64_t S = a.stride;
+	const E *__restrict__ ent = a.ent32;
+	const V *__restrict__ dg = a.diag32;
+	const V *__restrict__ invd = a.invd32;
+	Pack<V> *stb[2] = {(Pack<V> *)a.pack32[0], (Pack<V> *)a.pack32[1]};
+	V *__restrict__ x32 = a.e32;
+	V *__restrict__ p32 = a.p32;
+	itOut = 0; replOut = 0; relOut = 0; tolOut = a.tol;
+	// set-up: x64 = x32 = p = s = 0, r = b, u = M^-1 r, w = A u
+	double acc[3] = {0, 0, 0};
+	for (int64_t i = tid; i < n; i += nthr) {
+		const double b64 = a.b[i];
+		const V bi = V(b64), di = invd[i];
+		const V ui = mulRn(bi, di);
+		V wi = dg[i] * ui;
+#pragma unroll
+		for (int k = 0; k < NB; k++) {
+			const E e = ent[k * S + i];
+			if (e.nb >= 0) wi = fma(-e.w, mulRn(V(a.b[e.nb]), invd[e.nb]), wi);
+		}
+		a.x[i] = 0; x32[i] = V(0); p32[i] = V(0);
+		stb[0][i] = Pack<V>{bi, wi, V(0), di};
+		acc[0] += double(bi) * double(ui);
+		acc[1] += double(wi) * double(ui);
+		acc[2] += b64 * b64;
+	}
+	blockPartials<3>(acc, a.partials, a.maxBlocks, sh);
+	if (!gridSync(a.bar, a.err, epoch)) return;
+	double tot[5];
+	gridTotals<3, 5>(a.partials, a.maxBlocks, tot, sh, [](double *t) { t[3] = 0; t[4] = t[0] / t[1]; });
+	const double b2 = tot[2];
+	if (b2 == 0) return;
+	const double tol = fmax(a.tol, DBL_EPSILON / sqrt(b2));
+	const double threshold = fmax(tol * tol * b2, DBL_MIN);
+	tolOut = tol;
+	relOut = 1;
+	if (b2 < threshold) { relOut = 0; return; }
+	const double drop2 = a.drop * a.drop;
+	double gamma = tot[0], lastTrue = b2;
+	int cur = 0, it = 0, lastReplace = 0;
+	constexpr bool reg = Reg;
+	// register-resident copies (used when every thread owns at most kRegUnknowns unknowns)
+	E en[kRegUnknowns][NB];
+	V dgi[kRegUnknowns], pp[kRegUnknowns], xx[kRegUnknowns];
+	Pack<V> me[kRegUnknowns];
+	bool own[kRegUnknowns];
+	if constexpr (reg) {
+#pragma unroll
+		for (int c = 0; c < kRegUnknowns; c++) {
+			const int64_t i = tid + c * nthr;
+			own[c] = i < n;
+			pp[c] = V(0); xx[c] = V(0);
+			if (own[c]) {
+				dgi[c] = dg[i];
+				me[c] = stb[0][i];
+#pragma unroll
+				for (int k = 0; k < NB; k++) en[c][k] = ent[k * S + i];
+			} else {
+				dgi[c] = V(0);
+				me[c] = Pack<V>{V(0), V(0), V(0), V(0)};
+#pragma unroll
+				for (int k = 0; k < NB; k++) { en[c][k] = E{}; en[c][k].nb = -1; }
+			}
+		}
+	}
+	while (it < a.maxIter) {
+		// ---- one C-G iteration (as pcgCore) ----
+		const double alpha = tot[4];
+		const V bV = V(tot[3]), aV = V(alpha);
+		{
+			const Pack<V> *__restrict__ sc = stb[cur];
+			Pack<V> *__restrict__ sn = stb[cur ^ 1];
+			// dot partials: FP32 over at most kRegUnknowns unknowns, then FP64
+			double g = 0, d = 0, rr = 0;
+			V g32 = V(0), d32 = V(0), r32 = V(0);
+			int cnt = 0;
+			auto update = [&](const Pack<V> &m, V dgI, V pOld, V xOld, auto entry, Pack<V> &mOut, V &pOut, V &xOut) {
+				const V ui = mulRn(m.r, m.d);
+				const V pi = fma(bV, pOld, ui);
+				const V si = fma(bV, m.s, m.w);
+				const V rni = fma(-aV, si, m.r);
+				const V uni = mulRn(rni, m.d);
+				V wni = dgI * uni;
+#pragma unroll
+				for (int k = 0; k < NB; k++) {
+					const E e = entry(k);
+					if (e.nb >= 0) {
+						const Pack<V> q = sc[e.nb];
+						const V snb = fma(bV, q.s, q.w);
+						const V rnb = fma(-aV, snb, q.r);
+						wni = fma(-e.w, mulRn(rnb, q.d), wni);
+					}
+				}
+				pOut = pi;
+				xOut = fma(aV, pi, xOld);
+				mOut = Pack<V>{rni, wni, si, m.d};
+				g32 = fma(rni, uni, g32);
+				d32 = fma(wni, uni, d32);
+				r32 = fma(rni, rni, r32);
+				if (++cnt == kRegUnknowns) { g += double(g32); d += double(d32); rr += double(r32); g32 = d32 = r32 = V(0); cnt = 0; }
+			};
+			if constexpr (reg) {
+#pragma unroll
+				for (int c = 0; c < kRegUnknowns; c++) {
+					if (!own[c]) continue;
+					update(me[c], dgi[c], pp[c], xx[c], [&](int k) { return en[c][k]; }, me[c], pp[c], xx[c]);
+					sn[tid + c * nthr] = me[c];
+				}
+			} else {
+				for (int64_t i = tid; i < n; i += nthr) {
+					Pack<V> m = sc[i];
+					V pv = p32[i], xv = x32[i];
+					update(m, dg[i], pv, xv, [&](int k) { return ent[k * S + i]; }, m, pv, xv);
+					sn[i] = m; p32[i] = pv; x32[i] = xv;
+				}
+			}
+			cur ^= 1;
+			double part[3] = {g + double(g32), d + double(d32), rr + double(r32)};
+			blockPartials<3>(part, a.partials, a.maxBlocks, sh);
+		}
+		if (!gridSync(a.bar, a.err, epoch)) break;
+		const double gOld = gamma;
+		gridTotals<3, 5>(a.partials, a.maxBlocks, tot, sh, [gOld, alpha](double *t) {
+			t[3] = t[0] / gOld;
+			t[4] = t[0] / (t[1] - t[3] * t[0] / alpha);
+		});
+		it++;
+		gamma = tot[0];
+		const bool due = a.replaceEvery > 0 && it - lastReplace >= a.replaceEvery;
+		if (!(tot[2] < drop2 * lastTrue || tot[2] < threshold || it >= a.maxIter || due)) continue;
+		lastReplace = it;
+
+		// ---- residual replacement ----
+		// (1) fold the FP32 correction into the FP64 solution
+		if constexpr (reg) {
+#pragma unroll
+			for (int c = 0; c < kRegUnknowns; c++)
+				if (own[c]) { const int64_t i = tid + c * nthr; a.x[i] += double(xx[c]); xx[c] = V(0); }
+		} else {
+			for (int64_t i = tid; i < n; i += nthr) { a.x[i] += double(x32[i]); x32[i] = V(0); }
+		}
+		if (!gridSync(a.bar, a.err, epoch)) break;
+		// (2) r = b - A64 x64 in FP64, stored as the FP32 residual of the other buffer
+		{
+			const Pack<V> *__restrict__ sc = stb[cur];
+			Pack<V> *__restrict__ sn = stb[cur ^ 1];
+			double acc2[1] = {0};
+			auto residual = [&](int64_t i, const Pack<V> &m) {
+				double ax = a.diag[i] * a.x[i];
+#pragma unroll
+				for (int k = 0; k < NB; k++) {
+					const NbW64 e = a.ent[k * S + i];
+					if (e.nb >= 0) ax -= e.w * a.x[e.nb];
+				}
+				const double ri = a.b[i] - ax;
+				acc2[0] += ri * ri;
+				return Pack<V>{V(ri), m.w, m.s, m.d};
+			};
+			if constexpr (reg) {
+#pragma unroll
+				for (int c = 0; c < kRegUnknowns; c++)
+					if (own[c]) { const int64_t i = tid + c * nthr; me[c] = residual(i, me[c]); sn[i] = me[c]; }
+			} else {
+				for (int64_t i = tid; i < n; i += nthr) sn[i] = residual(i, sc[i]);
+			}
+			blockPartials<1>(acc2, a.partials, a.maxBlocks, sh);
+		}
+		if (!gridSync(a.bar, a.err, epoch)) break;
+		double tr[1];
+		gridTotals<1, 1>(a.partials, a.maxBlocks, tr, sh, NoFin{});
+		replOut++;
+		relOut = sqrt(tr[0] / b2);
+		if (tr[0] < threshold || it >= a.maxIter) break;
+		lastTrue = tr[0];
+		// (3) u = M^-1 r, w = A32 u from the replaced residuals; new γ, δ and the scalars
+		{
+			const Pack<V> *__restrict__ sc = stb[cur ^ 1];
+			Pack<V> *__restrict__ sn = stb[cur];
+			double g = 0, d = 0;
+			auto rebuild = [&](const Pack<V> &m, V dgI, auto entry) {
+				const V ui = mulRn(m.r, m.d);
+				V wi = dgI * ui;
+#pragma unroll
+				for (int k = 0; k < NB; k++) {
+					const E e = entry(k);
+					if (e.nb >= 0) { const Pack<V> q = sc[e.nb]; wi = fma(-e.w, mulRn(q.r, q.d), wi); }
+				}
+				g += double(m.r) * double(ui);
+				d += double(wi) * double(ui);
+				return Pack<V>{m.r, wi, m.s, m.d};
+			};
+			if constexpr (reg) {
+#pragma unroll
+				for (int c = 0; c < kRegUnknowns; c++)
+					if (own[c]) { me[c] = rebuild(me[c], dgi[c], [&](int k) { return en[c][k]; }); sn[tid + c * nthr] = me[c]; }
+			} else {
+				for (int64_t i = tid; i < n; i += nthr) sn[i] = rebuild(sc[i], dg[i], [&](int k) { return ent[k * S + i]; });
+			}
+			double part[2] = {g, d};
+			blockPartials<2>(part, a.partials, a.maxBlocks, sh);
+		}
+		if (!gridSync(a.bar, a.err, epoch)) break;
+		gridTotals<2, 5>(a.partials, a.maxBlocks, tot, sh, [gOld, alpha](double *t) {
+			t[2] = 0;
+			t[3] = t[0] / gOld;
+			t[4] = t[0] / (t[1] - t[3] * t[0] / alpha);
+		});
+		gamma = tot[0];
+	}
+	itOut = it;
+}
+
 template <int NB>
 __global__ void __launch_bounds__(kCgBlock) kPcgMixed(CgArgs a) {
 	__shared__ double sh[3 * 32];
 	const int n = *a.nDev;
-	const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x, nthr = int64_t(gridDim.x) * blockDim.x;
 	unsigned epoch = 0;
-	for (int64_t i = tid; i < n; i += nthr) a.x[i] = 0;
-	int mvTotal = 0, sweeps = 0;
-	double relres = 0, tolUsed = a.tol;
-	const bool alive = gridSync(a.bar, a.err, epoch);  // x = 0 everywhere before the first residual
-	while (alive) {
-		// r64 = b - A64 x64 and |b|^2, |r64|^2 in FP64
-		double acc[2] = {0, 0};
-		for (int64_t i = tid; i < n; i += nthr) {
-			double ax = a.diag[i] * a.x[i];
-#pragma unroll
-			for (int k = 0; k < NB; k++) {
-				const NbW64 e = a.ent[k * a.stride + i];
-				if (e.nb >= 0) ax -= e.w * a.x[e.nb];
-			}
-			const double bi = a.b[i];
-			const double ri = bi - ax;
-			a.r64[i] = ri;
-			acc[0] += bi * bi;
-			acc[1] += ri * ri;
-		}
-		blockPartials<2>(acc, a.partials, a.maxBlocks, sh);
-		if (!gridSync(a.bar, a.err, epoch)) break;
-		double t[2];
-		gridTotals<2, 2>(a.partials, a.maxBlocks, t, sh, NoFin{});
-		if (t[0] == 0) { relres = 0; break; }
-		tolUsed = fmax(a.tol, DBL_EPSILON / sqrt(t[0]));
-		relres = sqrt(t[1] / t[0]);
-		if (relres <= tolUsed || sweeps >= a.maxRefine) break;
-		double rr = 0, b2 = 0;
-		bool ok = true;
-		mvTotal += pcgCore<NB, float>(a, n, a.ent32, a.diag32, a.invd32, a.r64, a.e32, a.p32, (Pack<float> *)a.pack32[0], (Pack<float> *)a.pack32[1], a.innerTol, a.maxIter, sh, epoch, &rr, &b2, &ok);
-		if (!ok) break;
-		for (int64_t i = tid; i < n; i += nthr) a.x[i] += double(a.e32[i]);
-		sweeps++;
-		if (!gridSync(a.bar, a.err, epoch)) break;
-	}
+	int it = 0, repl = 0;
+	double rel = 0, tolUsed = a.tol;
+	const int64_t nthr = int64_t(gridDim.x) * blockDim.x;
+	if (n <= kRegUnknowns * nthr) pcgMixedReplace<NB, true>(a, n, sh, epoch, it, repl, rel, tolUsed);
+	else pcgMixedReplace<NB, false>(a, n, sh, epoch, it, repl, rel, tolUsed);
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
-		a.ints[0] = mvTotal;
-		a.ints[1] = sweeps;
-		a.scal[0] = relres;
+		a.ints[0] = it;
+		a.ints[1] = repl;
+		a.scal[0] = rel;
 		a.scal[1] = tolUsed;
 	}
 }
@@ -602,7 +798,7 @@ garm_status projectAsync(State &s, bool record) {
 	a.partials = s.partials; a.maxBlocks = s.maxBlocks;
 	a.bar = s.barrier; a.err = s.cgInts + 4;
 	a.tol = s.cfg.cg_tolerance; a.maxIter = s.cfg.cg_max_iters;
-	a.innerTol = s.cfg.mixed_inner_tolerance; a.maxRefine = s.cfg.mixed_max_refinements;
+	a.drop = s.cfg.mixed_residual_drop; a.replaceEvery = s.cfg.mixed_replace_interval;
 	a.scal = s.cgScalars; a.ints = s.cgInts;
 
 	cudaError_t e = cudaMemsetAsync(s.barrier, 0, 2 * sizeof(unsigned), s.stream);

@@ -51,8 +51,8 @@ class Config(C.Structure):
                 ("reinit_interval", C.c_int), ("cg_tolerance", C.c_double), ("cg_max_iters", C.c_int),
                 ("boundary_extrap_radius", C.c_double), ("air_extrap_radius", C.c_double),
                 ("rm_threshold", C.c_double), ("rm_band", C.c_double), ("rm_ratio", C.c_double),
-                ("enable_gravity", C.c_int), ("mixed_inner_tolerance", C.c_double),
-                ("mixed_max_refinements", C.c_int)]
+                ("enable_gravity", C.c_int), ("mixed_residual_drop", C.c_double),
+                ("mixed_replace_interval", C.c_int)]
 
 
 class StepStats(C.Structure):

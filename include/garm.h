@@ -89,15 +89,17 @@ typedef struct garm_config {
     double rm_band;                   /* 4   */
     double rm_ratio;                  /* 1e-5 */
     int enable_gravity;               /* 1   (LevelSetLiquid.h:72) */
-    double mixed_inner_tolerance;     /* inner FP32 PCG tolerance of one refinement sweep (mixed only) */
-    int mixed_max_refinements;        /* outer FP64 iterative-refinement sweeps (mixed only) */
+    double mixed_residual_drop;       /* mixed only: the FP32 PCG's residual is replaced by the FP64 true
+                                         residual b - A x each time it has dropped by this factor */
+    int mixed_replace_interval;       /* mixed only: replace at least every this many iterations (0: never
+                                         by count) */
 } garm_config;
 
 /* Per-step statistics returned by garm_sim_advance. */
 typedef struct garm_step_stats {
     int restarted;            /* 1 when checkReferenceMap failed and restart() ran */
     int cg_iterations;        /* total PCG iterations (inner iterations summed in mixed mode) */
-    int cg_refinements;       /* outer refinement sweeps (mixed); 1 in FP64 */
+    int cg_refinements;       /* FP64 residual replacements (mixed); 1 in FP64 */
     int unknowns;             /* pressure unknowns of this step */
     double cg_residual;       /* final relative residual |b-Ax|/|b| */
     int rm_total;             /* band cells inspected by checkReferenceMap */

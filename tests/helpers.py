@@ -25,8 +25,8 @@ def host_default_config(**kw) -> capi.Config:
     c.rm_band = 4.0
     c.rm_ratio = 1e-5
     c.enable_gravity = 1
-    c.mixed_inner_tolerance = 1e-4
-    c.mixed_max_refinements = 12
+    c.mixed_residual_drop = 0.1
+    c.mixed_replace_interval = 0
     for k, v in kw.items():
         setattr(c, k, v)
     return c

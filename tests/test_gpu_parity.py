@@ -258,7 +258,7 @@ def test_mixed_precision_within_1e3_dx(oracle_mod, garm_lib, capsys, name):
     with capsys.disabled():
         print(f"\n[mixed vs FP64 oracle, {name}] phi band(3dx) {ephi:.3e} dx, all cells {ephi_all:.3e} dx, "
               f"u rel (fluid faces) {eu:.3e}, wall ties {ties}, xi {exi:.3e} dx, "
-              f"cg {sg['cg_iterations']} it / {sg['cg_refinements']} sweeps, residual {sg['cg_residual']:.2e}")
+              f"cg {sg['cg_iterations']} it / {sg['cg_refinements']} replacements, residual {sg['cg_residual']:.2e}")
     assert sg["status"] == capi.OK
     assert sg["cg_residual"] <= 1e-8
     assert ephi <= 1e-3
