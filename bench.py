@@ -148,11 +148,19 @@ def state_fields():
             capi.FIELD_REF_LEVEL_SET_GRAD, capi.FIELD_ADV_REGION]
 
 
-def profiled_traffic(name: str, n: int):
-    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of one ncu
-    capture summarised under profiles/, when it was taken on this workload size."""
-    p = REPO / "profiles" / name
-    if n != 128 or not p.exists():
+PROFILED_PLANS = {  # (form, precision) -> ncu summary of that WENO5 sub-stage at 128^3
+    ("sweeps", "fp64"): "weno_sweeps_fp64_dam_break_128.txt",
+    ("columns", "mixed"): "weno_columns_f32_dam_break_128.txt",
+}
+
+
+def profiled_traffic(plan: dict, precision: str, n: int):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the ncu
+    capture summarised under profiles/, when it was taken on this workload size and for
+    the launch form the autotuner picked here (None otherwise)."""
+    name = PROFILED_PLANS.get((plan["form"], precision))
+    p = REPO / "profiles" / name if name else None
+    if n != 128 or p is None or not p.exists():
         return None
     for ln in p.read_text().splitlines():
         if ln.startswith("traffic_bytes_per_launch:"):
@@ -353,8 +361,7 @@ def run_garm(args) -> None:
     }
     if rank == 0:
         out["roofline"] = reinit_roofline(sim, torch, stream, int(scene.phi.size), 8 if args.precision == "fp64" else 4, 30, peaks)
-        out["roofline"]["traffic"] = profiled_traffic(
-            "reinit_stage_fp64_dam_break_128.txt" if args.precision == "fp64" else "reinit_stage_f32_dam_break_128.txt", n)
+        out["roofline"]["traffic"] = profiled_traffic(out["roofline"]["plan"], args.precision, n)
 
     # end to end through the C ABI with host buffers: upload the step's input state
     # from pinned memory, advance, download the state and the level set
@@ -417,7 +424,7 @@ def run_garm(args) -> None:
                         "dtype": "f32 storage+math, f64 dots/residual/refinement/RM test"}
         if rank == 0:
             out["mixed"]["roofline"] = reinit_roofline(mix, torch, stream, int(scene.phi.size), 4, 30, peaks)
-            out["mixed"]["roofline"]["traffic"] = profiled_traffic("reinit_stage_f32_dam_break_128.txt", n)
+            out["mixed"]["roofline"]["traffic"] = profiled_traffic(out["mixed"]["roofline"]["plan"], "mixed", n)
         mix.close()
 
     # many uneven scenes at once (mixed): the batched form of the same pipeline
