@@ -475,20 +475,116 @@ __global__ void __launch_bounds__(kCgBlock) kPcgFp64(CgArgs a) {
 	}
 }
 
+// ---------------------------------------------------------------------------
+// Double-float sums on the FP32 pipe.  GB300 issues one FP64 warp instruction
+// per 16 cycles per SM, so FP64-accurate dot products of FP32 vectors are
+// formed instead as unevaluated pairs hi + lo of floats: each product is exact
+// (a·b = p + e with e = fma(a, b, -p)) and each addition error-free (Knuth's
+// TwoSum), which carries about 44 significant bits (Dekker 1971; Ogita, Rump &
+// Oishi, "Accurate sum and dot product", 2005).  Only the per-block totals are
+// widened to FP64.  Explicit _rn intrinsics keep the compiler from fusing the
+// steps that the error terms rely on.
+// ---------------------------------------------------------------------------
+struct DF { float hi, lo; };
+__device__ __forceinline__ DF dfTwoSum(float a, float b) {
+	const float s = __fadd_rn(a, b);
+	const float bb = __fsub_rn(s, a);
+	return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ void dfAddProd(DF &acc, float a, float b) {
+	const float p = __fmul_rn(a, b);
+	const float e = fmaf(a, b, -p);
+	const DF t = dfTwoSum(acc.hi, p);
+	acc.hi = t.hi;
+	acc.lo = __fadd_rn(acc.lo, __fadd_rn(t.lo, e));
+}
+__device__ __forceinline__ DF dfMerge(DF a, DF b) {
+	const DF s = dfTwoSum(a.hi, b.hi);
+	const float lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+	const float hi = __fadd_rn(s.hi, lo);
+	return {hi, __fsub_rn(lo, __fsub_rn(hi, s.hi))};
+}
+__device__ __forceinline__ DF dfWarpSum(DF v) {
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v = dfMerge(v, DF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)});
+	return v;
+}
+// Block sums of NV double-float values → partials (as float pairs) [v*maxBlocks + blockIdx].
+template <int NV>
+__device__ __forceinline__ void blockPartialsDF(DF (&acc)[NV], double *partials, int maxBlocks, double *sh) {
+	float2 *s2 = reinterpret_cast<float2 *>(sh);
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+	for (int v = 0; v < NV; v++) {
+		const DF x = dfWarpSum(acc[v]);
+		if (lane == 0) s2[v * 16 + w] = make_float2(x.hi, x.lo);
+	}
+	__syncthreads();
+	if (w == 0) {
+		float2 *p2 = reinterpret_cast<float2 *>(partials);
+#pragma unroll
+		for (int v = 0; v < NV; v++) {
+			DF x{0.f, 0.f};
+			if (lane < nw) { const float2 q = s2[v * 16 + lane]; x = DF{q.x, q.y}; }
+			x = dfWarpSum(x);
+			if (lane == 0) p2[v * maxBlocks + blockIdx.x] = make_float2(x.hi, x.lo);
+		}
+	}
+	__syncthreads();
+}
+// Grid totals of NV double-float partials, widened to FP64 by lane 0, which then
+// runs `fin` on them; the NOUT results are broadcast to the block.
+template <int NV, int NOUT, typename Fin>
+__device__ __forceinline__ void gridTotalsDF(const double *partials, int maxBlocks, double (&out)[NOUT], double *sh, Fin fin) {
+	const int lane = threadIdx.x & 31;
+	if (threadIdx.x < 32) {
+		const float2 *p2 = reinterpret_cast<const float2 *>(partials);
+		double t[NOUT];
+#pragma unroll
+		for (int v = 0; v < NV; v++) {
+			DF x{0.f, 0.f};
+			for (int b = lane; b < (int)gridDim.x; b += 32) {
+				const float2 q = p2[v * maxBlocks + b];  // ordered by gridSync, as ldcg
+				x = dfMerge(x, DF{q.x, q.y});
+			}
+			x = dfWarpSum(x);
+			t[v] = double(x.hi) + double(x.lo);
+		}
+		if (lane == 0) {
+			fin(t);
+#pragma unroll
+			for (int v = 0; v < NOUT; v++) sh[v] = t[v];
+		}
+	}
+	__syncthreads();
+#pragma unroll
+	for (int v = 0; v < NOUT; v++) out[v] = sh[v];
+	__syncthreads();
+}
+
+// Power of two s with s·rms(r) in [1, 2): the FP32 system is solved for s·r so
+// its values, products and sums stay far from the FP32 range limits whatever
+// the scale of the pressure equation.
+__device__ __forceinline__ double unitScale(double sumSq, int n) {
+	const double rms = sqrt(sumSq / double(n > 0 ? n : 1));
+	return rms > 0 ? ldexp(1.0, -ilogb(rms)) : 1.0;
+}
+
 // Mixed form: one FP32 PCG (the Chronopoulos–Gear iteration of pcgCore, FP32
-// vectors and element arithmetic, FP64 reductions and scalars) with FP64
-// residual replacement (van der Vorst & Ye, "Residual replacement strategies
-// for Krylov subspace iterative methods", SIAM J. Sci. Comput. 22, 2000, as
-// used by reliable-update mixed-precision CG).  The FP32 iterates x32 are a
-// correction to the FP64 solution x64.  Whenever the recursive residual has
-// dropped by the factor `drop` since the last replacement, or looks converged:
-//   x64 += x32, x32 = 0;  r = b - A64 x64 in FP64 (the convergence test uses
-//   this true residual only);  r32 = r;  u = M^-1 r32, w = A32 u recomputed;
-// and the iteration continues with the same search direction p and s = A p,
-// β and α formed from the new γ = r·u, δ = w·u by the usual recurrences.  No
-// Krylov information is discarded, so the iteration count stays close to the
-// FP64 solver's, while the residual the solve reports is FP64-exact.
-// Returns in outs: matvecs, replacements, relative true residual, tolerance.
+// vectors and element arithmetic, double-float dot products widened to FP64 per
+// block, FP64 scalars) with FP64 residual replacement (van der Vorst & Ye,
+// "Residual replacement strategies for Krylov subspace iterative methods",
+// SIAM J. Sci. Comput. 22, 2000, as used by reliable-update mixed-precision CG).
+// The FP32 iterates x32 are a scaled correction to the FP64 solution x64.
+// Whenever the recursive residual has dropped by the factor `drop` since the
+// last replacement, or looks converged:
+//   x64 += x32/s, x32 = 0;  r = b - A64 x64 in FP64 (the convergence test uses
+//   this true residual only);  new scale s';  r32 = s' r;  u = M^-1 r32 and
+//   w = A32 u recomputed;  p, s·A p and γ_old rescaled by s'/s (exact);
+// and the iteration continues with the same search direction, β and α formed
+// from the new γ = r·u, δ = w·u by the usual recurrences.  No Krylov
+// information is discarded, so the iteration count stays close to the FP64
+// solver's, while the residual the solve reports is FP64-exact.
 template <int NB, bool Reg>
 __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &epoch, int &itOut, int &replOut, double &relOut, double &tolOut) {
 	using V = float;
@@ -502,45 +598,54 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 	V *__restrict__ x32 = a.e32;
 	V *__restrict__ p32 = a.p32;
 	itOut = 0; replOut = 0; relOut = 0; tolOut = a.tol;
-	// set-up: x64 = x32 = p = s = 0, r = b, u = M^-1 r, w = A u
-	double acc[3] = {0, 0, 0};
-	for (int64_t i = tid; i < n; i += nthr) {
-		const double b64 = a.b[i];
-		const V bi = V(b64), di = invd[i];
-		const V ui = mulRn(bi, di);
-		V wi = dg[i] * ui;
-#pragma unroll
-		for (int k = 0; k < NB; k++) {
-			const E e = ent[k * S + i];
-			if (e.nb >= 0) wi = fma(-e.w, mulRn(V(a.b[e.nb]), invd[e.nb]), wi);
-		}
-		a.x[i] = 0; x32[i] = V(0); p32[i] = V(0);
-		stb[0][i] = Pack<V>{bi, wi, V(0), di};
-		acc[0] += double(bi) * double(ui);
-		acc[1] += double(wi) * double(ui);
-		acc[2] += b64 * b64;
+	// |b|^2 in FP64 (sets the tolerance and the first scale)
+	{
+		double acc[1] = {0};
+		for (int64_t i = tid; i < n; i += nthr) { const double b = a.b[i]; acc[0] += b * b; }
+		blockPartials<1>(acc, a.partials, a.maxBlocks, sh);
 	}
-	blockPartials<3>(acc, a.partials, a.maxBlocks, sh);
 	if (!gridSync(a.bar, a.err, epoch)) return;
-	double tot[5];
-	gridTotals<3, 5>(a.partials, a.maxBlocks, tot, sh, [](double *t) { t[3] = 0; t[4] = t[0] / t[1]; });
-	const double b2 = tot[2];
+	double b2v[1];
+	gridTotals<1, 1>(a.partials, a.maxBlocks, b2v, sh, NoFin{});
+	const double b2 = b2v[0];
 	if (b2 == 0) return;
 	const double tol = fmax(a.tol, DBL_EPSILON / sqrt(b2));
 	const double threshold = fmax(tol * tol * b2, DBL_MIN);
 	tolOut = tol;
 	relOut = 1;
 	if (b2 < threshold) { relOut = 0; return; }
+	double scale = unitScale(b2, n);
+	// set-up: x64 = x32 = p = s = 0, r = scale·b, u = M^-1 r, w = A u
+	{
+		DF acc[2] = {{0.f, 0.f}, {0.f, 0.f}};
+		for (int64_t i = tid; i < n; i += nthr) {
+			const V bi = V(a.b[i] * scale), di = invd[i];
+			const V ui = mulRn(bi, di);
+			V wi = dg[i] * ui;
+#pragma unroll
+			for (int k = 0; k < NB; k++) {
+				const E e = ent[k * S + i];
+				if (e.nb >= 0) wi = fma(-e.w, mulRn(V(a.b[e.nb] * scale), invd[e.nb]), wi);
+			}
+			a.x[i] = 0; x32[i] = V(0); p32[i] = V(0);
+			stb[0][i] = Pack<V>{bi, wi, V(0), di};
+			dfAddProd(acc[0], bi, ui);
+			dfAddProd(acc[1], wi, ui);
+		}
+		blockPartialsDF<2>(acc, a.partials, a.maxBlocks, sh);
+	}
+	if (!gridSync(a.bar, a.err, epoch)) return;
+	double tot[5];
+	gridTotalsDF<2, 5>(a.partials, a.maxBlocks, tot, sh, [](double *t) { t[2] = 0; t[3] = 0; t[4] = t[0] / t[1]; });
 	const double drop2 = a.drop * a.drop;
 	double gamma = tot[0], lastTrue = b2;
 	int cur = 0, it = 0, lastReplace = 0;
-	constexpr bool reg = Reg;
 	// register-resident copies (used when every thread owns at most kRegUnknowns unknowns)
 	E en[kRegUnknowns][NB];
 	V dgi[kRegUnknowns], pp[kRegUnknowns], xx[kRegUnknowns];
 	Pack<V> me[kRegUnknowns];
 	bool own[kRegUnknowns];
-	if constexpr (reg) {
+	if constexpr (Reg) {
 #pragma unroll
 		for (int c = 0; c < kRegUnknowns; c++) {
 			const int64_t i = tid + c * nthr;
@@ -566,10 +671,7 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 		{
 			const Pack<V> *__restrict__ sc = stb[cur];
 			Pack<V> *__restrict__ sn = stb[cur ^ 1];
-			// dot partials: FP32 over at most kRegUnknowns unknowns, then FP64
-			double g = 0, d = 0, rr = 0;
-			V g32 = V(0), d32 = V(0), r32 = V(0);
-			int cnt = 0;
+			DF acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
 			auto update = [&](const Pack<V> &m, V dgI, V pOld, V xOld, auto entry, Pack<V> &mOut, V &pOut, V &xOut) {
 				const V ui = mulRn(m.r, m.d);
 				const V pi = fma(bV, pOld, ui);
@@ -590,12 +692,11 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 				pOut = pi;
 				xOut = fma(aV, pi, xOld);
 				mOut = Pack<V>{rni, wni, si, m.d};
-				g32 = fma(rni, uni, g32);
-				d32 = fma(wni, uni, d32);
-				r32 = fma(rni, rni, r32);
-				if (++cnt == kRegUnknowns) { g += double(g32); d += double(d32); rr += double(r32); g32 = d32 = r32 = V(0); cnt = 0; }
+				dfAddProd(acc[0], rni, uni);
+				dfAddProd(acc[1], wni, uni);
+				dfAddProd(acc[2], rni, rni);
 			};
-			if constexpr (reg) {
+			if constexpr (Reg) {
 #pragma unroll
 				for (int c = 0; c < kRegUnknowns; c++) {
 					if (!own[c]) continue;
@@ -611,37 +712,36 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 				}
 			}
 			cur ^= 1;
-			double part[3] = {g + double(g32), d + double(d32), rr + double(r32)};
-			blockPartials<3>(part, a.partials, a.maxBlocks, sh);
+			blockPartialsDF<3>(acc, a.partials, a.maxBlocks, sh);
 		}
 		if (!gridSync(a.bar, a.err, epoch)) break;
 		const double gOld = gamma;
-		gridTotals<3, 5>(a.partials, a.maxBlocks, tot, sh, [gOld, alpha](double *t) {
+		gridTotalsDF<3, 5>(a.partials, a.maxBlocks, tot, sh, [gOld, alpha](double *t) {
 			t[3] = t[0] / gOld;
 			t[4] = t[0] / (t[1] - t[3] * t[0] / alpha);
 		});
 		it++;
 		gamma = tot[0];
+		const double s2 = scale * scale;
 		const bool due = a.replaceEvery > 0 && it - lastReplace >= a.replaceEvery;
-		if (!(tot[2] < drop2 * lastTrue || tot[2] < threshold || it >= a.maxIter || due)) continue;
+		if (!(tot[2] < drop2 * lastTrue * s2 || tot[2] < threshold * s2 || it >= a.maxIter || due)) continue;
 		lastReplace = it;
 
 		// ---- residual replacement ----
-		// (1) fold the FP32 correction into the FP64 solution
-		if constexpr (reg) {
+		// (1) fold the scaled FP32 correction into the FP64 solution
+		const double inv = 1.0 / scale;  // a power of two: exact
+		if constexpr (Reg) {
 #pragma unroll
 			for (int c = 0; c < kRegUnknowns; c++)
-				if (own[c]) { const int64_t i = tid + c * nthr; a.x[i] += double(xx[c]); xx[c] = V(0); }
+				if (own[c]) { const int64_t i = tid + c * nthr; a.x[i] += double(xx[c]) * inv; xx[c] = V(0); }
 		} else {
-			for (int64_t i = tid; i < n; i += nthr) { a.x[i] += double(x32[i]); x32[i] = V(0); }
+			for (int64_t i = tid; i < n; i += nthr) { a.x[i] += double(x32[i]) * inv; x32[i] = V(0); }
 		}
 		if (!gridSync(a.bar, a.err, epoch)) break;
-		// (2) r = b - A64 x64 in FP64, stored as the FP32 residual of the other buffer
+		// (2) r = b - A64 x64 in FP64
 		{
-			const Pack<V> *__restrict__ sc = stb[cur];
-			Pack<V> *__restrict__ sn = stb[cur ^ 1];
 			double acc2[1] = {0};
-			auto residual = [&](int64_t i, const Pack<V> &m) {
+			for (int64_t i = tid; i < n; i += nthr) {
 				double ax = a.diag[i] * a.x[i];
 #pragma unroll
 				for (int k = 0; k < NB; k++) {
@@ -649,15 +749,8 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 					if (e.nb >= 0) ax -= e.w * a.x[e.nb];
 				}
 				const double ri = a.b[i] - ax;
+				a.r64[i] = ri;
 				acc2[0] += ri * ri;
-				return Pack<V>{V(ri), m.w, m.s, m.d};
-			};
-			if constexpr (reg) {
-#pragma unroll
-				for (int c = 0; c < kRegUnknowns; c++)
-					if (own[c]) { const int64_t i = tid + c * nthr; me[c] = residual(i, me[c]); sn[i] = me[c]; }
-			} else {
-				for (int64_t i = tid; i < n; i += nthr) sn[i] = residual(i, sc[i]);
 			}
 			blockPartials<1>(acc2, a.partials, a.maxBlocks, sh);
 		}
@@ -668,44 +761,57 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 		relOut = sqrt(tr[0] / b2);
 		if (tr[0] < threshold || it >= a.maxIter) break;
 		lastTrue = tr[0];
-		// (3) u = M^-1 r, w = A32 u from the replaced residuals; new γ, δ and the scalars
+		// (3) rescale; r32 = s' r; u = M^-1 r32, w = A32 u; p and s·A p follow the scale
+		const double newScale = unitScale(tr[0], n);
+		const V ratio = V(newScale / scale);  // a power of two
+		const double ratio2 = (newScale / scale) * (newScale / scale);
+		scale = newScale;
 		{
-			const Pack<V> *__restrict__ sc = stb[cur ^ 1];
-			Pack<V> *__restrict__ sn = stb[cur];
-			double g = 0, d = 0;
-			auto rebuild = [&](const Pack<V> &m, V dgI, auto entry) {
-				const V ui = mulRn(m.r, m.d);
+			const Pack<V> *__restrict__ sc = stb[cur];
+			Pack<V> *__restrict__ sn = stb[cur ^ 1];
+			DF acc[2] = {{0.f, 0.f}, {0.f, 0.f}};
+			auto rebuild = [&](int64_t i, const Pack<V> &m, V dgI, auto entry) {
+				const V ri = V(a.r64[i] * scale);
+				const V ui = mulRn(ri, m.d);
 				V wi = dgI * ui;
 #pragma unroll
 				for (int k = 0; k < NB; k++) {
 					const E e = entry(k);
-					if (e.nb >= 0) { const Pack<V> q = sc[e.nb]; wi = fma(-e.w, mulRn(q.r, q.d), wi); }
+					if (e.nb >= 0) wi = fma(-e.w, mulRn(V(a.r64[e.nb] * scale), sc[e.nb].d), wi);
 				}
-				g += double(m.r) * double(ui);
-				d += double(wi) * double(ui);
-				return Pack<V>{m.r, wi, m.s, m.d};
+				dfAddProd(acc[0], ri, ui);
+				dfAddProd(acc[1], wi, ui);
+				return Pack<V>{ri, wi, m.s * ratio, m.d};
 			};
-			if constexpr (reg) {
+			if constexpr (Reg) {
 #pragma unroll
 				for (int c = 0; c < kRegUnknowns; c++)
-					if (own[c]) { me[c] = rebuild(me[c], dgi[c], [&](int k) { return en[c][k]; }); sn[tid + c * nthr] = me[c]; }
+					if (own[c]) {
+						const int64_t i = tid + c * nthr;
+						me[c] = rebuild(i, me[c], dgi[c], [&](int k) { return en[c][k]; });
+						pp[c] *= ratio;
+						sn[i] = me[c];
+					}
 			} else {
-				for (int64_t i = tid; i < n; i += nthr) sn[i] = rebuild(sc[i], dg[i], [&](int k) { return ent[k * S + i]; });
+				for (int64_t i = tid; i < n; i += nthr) {
+					sn[i] = rebuild(i, sc[i], dg[i], [&](int k) { return ent[k * S + i]; });
+					p32[i] *= ratio;
+				}
 			}
-			double part[2] = {g, d};
-			blockPartials<2>(part, a.partials, a.maxBlocks, sh);
+			cur ^= 1;
+			blockPartialsDF<2>(acc, a.partials, a.maxBlocks, sh);
 		}
 		if (!gridSync(a.bar, a.err, epoch)) break;
-		gridTotals<2, 5>(a.partials, a.maxBlocks, tot, sh, [gOld, alpha](double *t) {
+		const double gOldScaled = gOld * ratio2;
+		gridTotalsDF<2, 5>(a.partials, a.maxBlocks, tot, sh, [gOldScaled, alpha](double *t) {
 			t[2] = 0;
-			t[3] = t[0] / gOld;
+			t[3] = t[0] / gOldScaled;
 			t[4] = t[0] / (t[1] - t[3] * t[0] / alpha);
 		});
 		gamma = tot[0];
 	}
 	itOut = it;
 }
-
 template <int NB>
 __global__ void __launch_bounds__(kCgBlock) kPcgMixed(CgArgs a) {
 	__shared__ double sh[3 * 32];
