@@ -195,6 +195,9 @@ def reinit_roofline(sim, torch, stream, n_cells: int, esz: int, iters: int, peak
             "traffic": None, "ms_per_launch": round(ms_per_launch, 4), "algorithmic_bytes_per_launch": int(bytes_per_launch)}
 
 
+BATCH_CG_CELLS_PER_BLOCK = 262144  # measured best for the 48-scene batch (4096: 177M, 262144: 194-198M cell-steps/s)
+
+
 def batch_scenes(count: int, seed: int = 0):
     """`count` independent pool scenes: n drawn uniformly from {64, 96, 128, 160},
     1-3 seed-placed spheres of radius 0.05-0.15 over a pool of depth 0.1-0.4."""
@@ -212,6 +215,9 @@ def run_batch(args, torch, world: int, W: int, K: int) -> dict:
     from garm import capi
     scs = batch_scenes(args.batch_scenes)
     cfg = capi.default_config(precision=capi.PRECISION_MIXED)
+    # each scene's pressure solve takes one SM per 262144 interior cells (1-16 SMs here), so the
+    # solves of different scenes run side by side instead of each taking the whole GPU
+    cfg.cg_cells_per_block = BATCH_CG_CELLS_PER_BLOCK
     streams = [torch.cuda.Stream() for _ in scs]
     sims = []
     for sc, st in zip(scs, streams):
@@ -250,6 +256,7 @@ def run_batch(args, torch, world: int, W: int, K: int) -> dict:
     return {"value": world * cells * K / (ms * 1e-3), "unit": UNIT, "ms_per_batch_step": ms / K, "scenes": len(scs),
             "interior_cells": cells, "sizes": sorted({int(round(sc.interior_cells ** (1 / 3))) for sc in scs}),
             "resident_bytes": resident, "graph_replay": graphs, "gpu_launches": launches,
+            "cg_cells_per_block": BATCH_CG_CELLS_PER_BLOCK,
             "p50_scene_step_ms": float(np.percentile(per_step, 50)), "p99_scene_step_ms": float(np.percentile(per_step, 99)),
             "dtype": "f32 storage+math, f64 dots/residual/refinement/RM test",
             "workload": f"{len(scs)} pool scenes, n uniform in {{64,96,128,160}}, 1-3 spheres, mixed, "

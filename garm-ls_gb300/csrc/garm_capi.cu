@@ -553,6 +553,7 @@ garm_status garm_config_default(garm_config *c) {
 	c->enable_gravity = 1;
 	c->mixed_residual_drop = 0.1;
 	c->mixed_replace_interval = 0;
+	c->cg_cells_per_block = 0;
 	return GARM_OK;
 }
 
@@ -595,7 +596,7 @@ garm_status garm_sim_create(const garm_grid_desc *gd, const garm_config *cfg, vo
 	garm_config c;
 	if (cfg) c = *cfg; else garm_config_default(&c);
 	if (c.precision != GARM_PRECISION_FP64 && c.precision != GARM_PRECISION_MIXED) return GARM_INVALID;
-	if (c.reinit_iters < 0 || c.cg_max_iters < 0 || !(c.cg_tolerance > 0)) return GARM_INVALID;
+	if (c.reinit_iters < 0 || c.cg_max_iters < 0 || !(c.cg_tolerance > 0) || c.cg_cells_per_block < 0) return GARM_INVALID;
 
 	garm_sim *sim = new (std::nothrow) garm_sim();
 	if (!sim) return GARM_OOM;

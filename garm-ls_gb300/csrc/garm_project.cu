@@ -9,6 +9,8 @@
 //   applyPressureGradient (Projector.cpp:91-123)
 #include "garm_internal.h"
 
+#include <algorithm>
+
 #include <cfloat>
 
 namespace garm {
@@ -918,14 +920,13 @@ garm_status projectAsync(State &s, bool record) {
 	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kfn, kCgBlock, 0);
 	if (e != cudaSuccess || perSM <= 0) return GARM_CUDA_ERROR;
 	// one resident 512-thread block per SM for large scenes; small scenes take one
-	// block per 4096 interior cells so that several scenes' solves can share the GPU.
-	// The cooperative launch verifies co-residency.
+	// block per cg_cells_per_block (default 4096) interior cells so that several
+	// scenes' solves can share the GPU.  The cooperative launch verifies co-residency.
 	int64_t interior = 1;
 	for (int q = 0; q < D; q++) interior *= (s.geom.n[q] - 2 * s.geom.bw);
-	int blocks = int((interior + 4095) / 4096);
+	const int64_t perBlock = s.cfg.cg_cells_per_block > 0 ? s.cfg.cg_cells_per_block : 4096;
+	int blocks = int(std::min<int64_t>((interior + perBlock - 1) / perBlock, s.numSMs));
 	if (blocks < 1) blocks = 1;
-	if (blocks > s.numSMs) blocks = s.numSMs;
-	if (blocks > s.maxBlocks) blocks = s.maxBlocks;
 	if (blocks > s.maxBlocks) blocks = s.maxBlocks;
 	void *args[] = {&a};
 	e = cudaLaunchCooperativeKernel(kfn, dim3(blocks), dim3(kCgBlock), args, 0, s.stream);

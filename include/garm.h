@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define GARM_ABI_VERSION 1
+#define GARM_ABI_VERSION 2
 
 typedef enum garm_status {
     GARM_OK = 0,
@@ -93,6 +93,9 @@ typedef struct garm_config {
                                          residual b - A x each time it has dropped by this factor */
     int mixed_replace_interval;       /* mixed only: replace at least every this many iterations (0: never
                                          by count) */
+    int cg_cells_per_block;           /* pressure solve: one 512-thread block (one SM) per this many interior
+                                         cells, at most one per SM; 0 selects 4096.  Larger values leave
+                                         SMs free for other scenes' work when scenes run concurrently */
 } garm_config;
 
 /* Per-step statistics returned by garm_sim_advance. */

@@ -13,8 +13,8 @@ from helpers import host_default_config, load_scene
 pytestmark = pytest.mark.gpu
 
 
-def _sim(scene, precision):
-    s = capi.Simulation(scene.grid, host_default_config(precision=precision))
+def _sim(scene, precision, cfg=None):
+    s = capi.Simulation(scene.grid, cfg if cfg is not None else host_default_config(precision=precision))
     load_scene(s, scene)
     s.initialize()
     s.stage("restart")
@@ -51,7 +51,7 @@ def test_serving_results_equal_alone_and_budget_respected(garm_lib, capsys):
     for res in out["results"]:
         req = next(r for r in reqs if r.rid == res.rid)
         sc = serving.build_scene(req)
-        s = _sim(sc, capi.PRECISION_MIXED)
+        s = _sim(sc, capi.PRECISION_MIXED, server.cfg)  # the same solver partition as in the mix
         s.advance_auto(req.steps)
         assert np.array_equal(s.download(capi.FIELD_LEVEL_SET), res.phi), f"request {req.rid}"
         s.close()
