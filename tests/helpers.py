@@ -87,3 +87,62 @@ def band_error(a, b, ref_phi, dx: float, band: float = 3.0) -> float:
     if not np.any(m):
         return 0.0
     return float(np.max(np.abs(np.asarray(a) - np.asarray(b))[m]))
+
+
+# --- Rotation case of the reference's GA advection test (TestAdvect2D.cpp:32-59, 256-290) ---
+ROT_LENGTH, ROT_DT, ROT_FRAMES_PER_TURN = 10.0, 0.02, 314
+
+
+def zalesak_phi(x, y):
+    """Slotted disk: circle (0, 2.5) r 1.5 minus the box [-0.25, 0.25] x [0, 3.5]
+    (TestAdvect2D.cpp:33-41, 57-58, lengths x 10)."""
+    circle = np.sqrt(x * x + (y - 2.5) ** 2) - 1.5
+    box = scenes.box_sdf([x, y], [-0.25, 0.0], [0.5, 3.5])
+    return np.maximum(circle, -box)
+
+
+def rotation_case(s: int):
+    """Grid (s^2 cells on [-5, 5]^2, no solid ring), cell φ, face velocity (.sav layout) and the
+    angular speed of one turn per ROT_FRAMES_PER_TURN steps of ROT_DT."""
+    dx = ROT_LENGTH / s
+    grid = capi.grid_desc(2, [s, s], dx, [0.0, 0.0], boundary_width=0)
+    c = -ROT_LENGTH / 2 + (np.arange(s) + 0.5) * dx
+    f = -ROT_LENGTH / 2 + np.arange(s + 1) * dx
+    omega = 2 * np.pi / (ROT_FRAMES_PER_TURN * ROT_DT)
+    Y, X = np.meshgrid(c, c, indexing="ij")
+    phi = np.ascontiguousarray(zalesak_phi(X, Y))
+    yx, xx = np.meshgrid(c, f, indexing="ij")     # x-faces: shape (s, s+1)
+    yy, xy = np.meshgrid(f, c, indexing="ij")     # y-faces: shape (s+1, s)
+    u = np.concatenate([(-yx * omega).ravel(), (xy * omega).ravel()])
+    return grid, phi, u, omega
+
+
+def rotation_truth(s: int, steps: int):
+    """The initial shape rotated by steps·ROT_DT·ω, at the cell centres."""
+    dx = ROT_LENGTH / s
+    c = -ROT_LENGTH / 2 + (np.arange(s) + 0.5) * dx
+    Y, X = np.meshgrid(c, c, indexing="ij")
+    a = 2 * np.pi * steps / ROT_FRAMES_PER_TURN
+    return zalesak_phi(np.cos(a) * X + np.sin(a) * Y, -np.sin(a) * X + np.cos(a) * Y)
+
+
+def run_rotation(sim, s: int, steps: int) -> np.ndarray:
+    """GA advection of ξ and Π in the steady rotation (velocity re-uploaded each step),
+    then φ = φ0(ξ) by the compose stage; returns φ."""
+    grid, phi, u, _ = rotation_case(s)
+    sim.upload(capi.FIELD_LEVEL_SET, phi.ravel())
+    sim.upload(capi.FIELD_VELOCITY, u)
+    sim.initialize()
+    sim.stage("restart")
+    sim.upload(capi.FIELD_ADV_REGION, np.ones(s * s, dtype=np.uint8))  # no air clamp
+    for _ in range(steps):
+        sim.upload(capi.FIELD_VELOCITY, u)
+        sim.stage("advect", ROT_DT)
+    sim.stage("compose")
+    return sim.download(capi.FIELD_LEVEL_SET).reshape(s, s)
+
+
+def band_l1(phi, truth, dx, band: float = 3.0) -> float:
+    """Mean |φ - truth| over cells with |truth| <= band·dx (TestAdvect2D.cpp:236-251)."""
+    m = np.abs(truth) <= band * dx
+    return float(np.mean(np.abs(phi - truth)[m]))

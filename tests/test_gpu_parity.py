@@ -276,3 +276,19 @@ def test_not_converged_is_reported_not_fatal(oracle_mod, garm_lib):
     assert sg["status"] == capi.NOT_CONVERGED and so["status"] == capi.NOT_CONVERGED
     assert sg["cg_iterations"] == 1 and so["cg_iterations"] == 1
     assert np.all(np.isfinite(g.download(capi.FIELD_VELOCITY)))
+
+
+def test_ga_advection_rotation_matches_oracle(oracle_mod, garm_lib):
+    """The GA advection known-answer case (slotted disk in a steady rotation, no solid
+    ring) through the C ABI: 40 advect stages then compose, against the oracle."""
+    from helpers import ROT_LENGTH, run_rotation, rotation_case
+    s = 64
+    grid, *_ = rotation_case(s)
+    g = capi.Simulation(grid, host_default_config())
+    o = oracle_mod.OracleSim(grid, host_default_config())
+    pg = run_rotation(g, s, 40)
+    po = run_rotation(o, s, 40)
+    dx = ROT_LENGTH / s
+    assert linf(pg, po) <= 1e-9 * dx
+    for f in (capi.FIELD_REF_MAP, capi.FIELD_REF_MAP_GRAD):
+        assert rel(g.download(f), o.download(f)) <= 1e-11, f

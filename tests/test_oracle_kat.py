@@ -172,3 +172,23 @@ def test_oracle_reports_not_converged(oracle_mod):
     o = oracle_mod.OracleSim(sc.grid, host_default_config(cg_max_iters=1))
     load_scene(o, sc)
     assert o.initialize() == capi.NOT_CONVERGED
+
+
+def test_ga_advection_rotation_converges(oracle_mod):
+    """Known-answer test after the reference's GA advection program (TestAdvect2D.cpp,
+    Rotation case, Hermite + reference map): the slotted disk turned half a revolution
+    by the hot path's own stages (velocity re-uploaded each step so it stays the steady
+    rotation; ξ, Π advected; φ = φ0(ξ) composed).  The band L1 error against the
+    rotated shape is small and falls about 4x from 50 to 100 cells per axis; beyond
+    that the RK2 backtrace's time error (|x|(ω dt)^3/6 per step) sets a floor."""
+    from helpers import ROT_LENGTH, band_l1, rotation_case, rotation_truth, run_rotation, host_default_config
+    errs = {}
+    for s in (50, 100):
+        grid, *_ = rotation_case(s)
+        o = oracle_mod.OracleSim(grid, host_default_config())
+        phi = run_rotation(o, s, 157)
+        errs[s] = band_l1(phi, rotation_truth(s, 157), ROT_LENGTH / s)
+        o.close()
+    assert errs[50] < 0.1 * (ROT_LENGTH / 50)
+    assert errs[100] < 0.04 * (ROT_LENGTH / 100)
+    assert errs[100] < errs[50] / 4
