@@ -154,6 +154,22 @@ PROFILED_PLANS = {  # (form, precision) -> ncu summary of that WENO5 sub-stage a
 }
 
 
+def profiled_pipe(plan: dict, precision: str, n: int):
+    """The compute pipe that bounds the profiled WENO5 sub-stage and its busy fraction
+    (mean over the captured launches of the ncu pipe metric), from the summary under profiles/."""
+    name = PROFILED_PLANS.get((plan["form"], precision))
+    p = REPO / "profiles" / name if name else None
+    if n != 128 or p is None or not p.exists():
+        return None
+    metric = "sm__inst_executed_pipe_fp64.avg.pct_of_peak_sustained_active" if precision == "fp64" \
+        else "smsp__issue_active.avg.pct_of_peak_sustained_active"
+    vals = [float(ln.split()[1]) for ln in p.read_text().splitlines() if ln.startswith(metric)]
+    if not vals:
+        return None
+    return {"pipe": "fp64" if precision == "fp64" else "issue", "metric": metric,
+            "frac": round(sum(vals) / len(vals) / 100, 3), "source": f"profiles/{name}"}
+
+
 def profiled_traffic(plan: dict, precision: str, n: int):
     """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the ncu
     capture summarised under profiles/, when it was taken on this workload size and for
@@ -369,6 +385,7 @@ def run_garm(args) -> None:
     if rank == 0:
         out["roofline"] = reinit_roofline(sim, torch, stream, int(scene.phi.size), 8 if args.precision == "fp64" else 4, 30, peaks)
         out["roofline"]["traffic"] = profiled_traffic(out["roofline"]["plan"], args.precision, n)
+        out["roofline"]["compute"] = profiled_pipe(out["roofline"]["plan"], args.precision, n)
 
     # end to end through the C ABI with host buffers: upload the step's input state
     # from pinned memory, advance, download the state and the level set
@@ -432,6 +449,7 @@ def run_garm(args) -> None:
         if rank == 0:
             out["mixed"]["roofline"] = reinit_roofline(mix, torch, stream, int(scene.phi.size), 4, 30, peaks)
             out["mixed"]["roofline"]["traffic"] = profiled_traffic(out["mixed"]["roofline"]["plan"], "mixed", n)
+            out["mixed"]["roofline"]["compute"] = profiled_pipe(out["mixed"]["roofline"]["plan"], "mixed", n)
         mix.close()
 
     # many uneven scenes at once (mixed): the batched form of the same pipeline
