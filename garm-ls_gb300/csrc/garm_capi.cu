@@ -140,6 +140,7 @@ garm_status allocState(State &s) {
 	s.maxBlocks = s.numSMs * 2;
 	GARM_TRY(dalloc(s, &s.partials, size_t(s.maxBlocks) * 4 * 8));
 	GARM_TRY(dalloc(s, &s.barrier, 64));
+	GARM_TRY(dalloc(s, &s.volumeOut, 64));
 	GARM_TRY(dalloc(s, &s.cgScalars, 64));
 	GARM_TRY(dalloc(s, &s.cgInts, 64));
 	GARM_TRY(dalloc(s, &s.redU64, 64));
@@ -787,6 +788,11 @@ garm_status garm_reinit_plan_set(int dim, int precision, const int *size, int fo
 		if (threads < 32 || threads > 256 || threads % 32 != 0) return GARM_INVALID;
 	}
 	return pinReinitPlan(dim, precision == GARM_PRECISION_FP64 ? 8 : 4, size, form, threads, cells_per_thread);
+}
+
+garm_status garm_sim_volume(garm_sim *sim, int evaluator_order, double *out) {
+	if (!sim || !out || (evaluator_order != 0 && evaluator_order != 1)) return GARM_INVALID;
+	return GARM_DISPATCH(sim->s, levelSetVolume, sim->s, evaluator_order, out);
 }
 
 garm_status garm_sim_max_speed(garm_sim *sim, double *out) {

@@ -68,6 +68,7 @@ struct State {
 	double *cgP64 = nullptr;
 	float *cgP32 = nullptr, *cgE32 = nullptr;
 	double *partials = nullptr; int maxBlocks = 0;
+	double *volumeOut = nullptr;   // result slot of the volume diagnostic
 	unsigned *barrier = nullptr;   // [count, generation]
 	double *cgScalars = nullptr;   // device-side scalars written by the persistent solver
 	int *cgInts = nullptr;
@@ -117,6 +118,8 @@ template <int D, typename T> garm_status finishBoundary(State &s);
 template <int D, typename T> garm_status advectFields(State &s);
 template <int D, typename T> garm_status generateCurrentFields(State &s);
 template <int D, typename T> garm_status reinitialize(State &s);
+// calculateVolume of tmp (synchronises the stream); evaluatorOrder: 3D corner order (see garm.h).
+template <int D, typename T> garm_status levelSetVolume(State &s, int evaluatorOrder, double *out);
 // Launch plan (form GARM_REINIT_*, threads per block, cells per thread) the
 // reinitialisation autotuner chose for this grid, and its sub-stage time in ms.
 template <int D, typename T> garm_status reinitPlanInfo(State &s, int *form, int *block, int *chunk, float *ms);

@@ -89,6 +89,7 @@ _SIGS = {
     "garm_sim_advance_auto": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(StepStats)]),
     "garm_sim_graph_active": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "garm_reinit_plan_set": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int, C.c_int, C.c_int]),
+    "garm_sim_volume": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "garm_sim_reinit_plan": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                        C.POINTER(C.c_float)]),
     "garm_sim_enqueue_auto": (C.c_int, [C.c_void_p, C.c_int]),
@@ -289,6 +290,12 @@ class Simulation:
         check(self.lib.garm_sim_reinit_plan(self.handle, C.byref(f), C.byref(b), C.byref(c), C.byref(ms)),
               "garm_sim_reinit_plan")
         return {"form": REINIT_FORMS[f.value], "threads": b.value, "cells_per_thread": c.value, "ms": ms.value}
+
+    def volume(self, evaluator_order: bool = False) -> float:
+        """calculateVolume of the current tmp level set (garm_sim_volume)."""
+        v = C.c_double()
+        check(self.lib.garm_sim_volume(self.handle, int(evaluator_order), C.byref(v)), "garm_sim_volume")
+        return v.value
 
     def max_speed(self) -> float:
         v = C.c_double()

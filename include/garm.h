@@ -191,6 +191,15 @@ garm_status garm_sim_reinit_plan(garm_sim *sim, int *form, int *threads, int *ce
  * pinned or tuned plan, so the next use tunes again. */
 garm_status garm_reinit_plan_set(int dim, int precision, const int *size, int form, int threads, int cells_per_thread);
 
+/* calculateVolume (Source/Core/LevelSetLiquid.cpp:1162-1190): volume (2D: area) of the
+ * liquid from the tmp level set, kept outside the timed step as a diagnostic.  2D sums the
+ * filled marching-squares contour; 3D sums the marching-cubes-style volume of every cube
+ * between samples (MC-style-vol-eval/fraction.hpp).  evaluator_order 0 passes each cube's
+ * corners as the reference does (x-fastest stencil order, which swaps two corner pairs
+ * relative to the evaluator's convention; first-order accurate); 1 passes them in the
+ * evaluator's own order (second-order accurate; no reference counterpart). */
+garm_status garm_sim_volume(garm_sim *sim, int evaluator_order, double *out);
+
 /* max over faces of |u| (GridBasedData::normMax, Source/Core/GridBasedData.h:55-68). */
 garm_status garm_sim_max_speed(garm_sim *sim, double *out);
 /* LevelSetLiquid::getTimeStep (Source/Core/LevelSetLiquid.h:129): cfl*dx/max|u| (may be +inf). */

@@ -47,6 +47,15 @@ def load() -> C.CDLL:
     lib.orc_stage.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(StepStats), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.orc_max_speed.restype = C.c_double
     lib.orc_max_speed.argtypes = [C.c_void_p]
+    lib.orc_volume.restype = C.c_double
+    lib.orc_volume.argtypes = [C.c_void_p]
+    lib.orc_mc_cube_volume.restype = C.c_double
+    lib.orc_mc_cube_volume.argtypes = [C.POINTER(C.c_double)]
+    lib.orc_ms_square_area.restype = C.c_double
+    lib.orc_ms_square_area.argtypes = [C.POINTER(C.c_double)]
+    lib.orc_mc_tables_ok.restype = C.c_int
+    lib.orc_field_volume.restype = C.c_double
+    lib.orc_field_volume.argtypes = [C.c_int, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int]
     lib.orc_set_threads.argtypes = [C.c_int]
     lib.orc_max_threads.restype = C.c_int
     lib.orc_reinit.argtypes = [C.c_int, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int, C.c_double]
@@ -112,6 +121,10 @@ class OracleSim:
     def max_speed(self) -> float:
         return self.lib.orc_max_speed(self.h)
 
+    def volume(self) -> float:
+        """calculateVolume (LevelSetLiquid.cpp:1162-1190) of the current tmp level set."""
+        return self.lib.orc_volume(self.h)
+
     def stage(self, name: str, arg: float = 0.0):
         st = StepStats()
         keep, tot, bad = C.c_int(), C.c_int(), C.c_int()
@@ -166,3 +179,28 @@ def cubic_eval(val: np.ndarray, spacing: float, origin, pts: np.ndarray) -> np.n
     out = np.empty(len(p))
     load().orc_cubic_eval(dim, size, float(spacing), _dp(o), _dp(v), len(p), _dp(p), _dp(out))
     return out
+
+
+def mc_cube_volume(v8) -> float:
+    """MC-style volume of one unit cube, corners in the evaluator's order."""
+    a = np.ascontiguousarray(v8, dtype=np.float64)
+    return load().orc_mc_cube_volume(_dp(a))
+
+
+def ms_square_area(v4) -> float:
+    """Filled marching-squares area of one unit square, corners (0,0), (1,0), (0,1), (1,1)."""
+    a = np.ascontiguousarray(v4, dtype=np.float64)
+    return load().orc_ms_square_area(_dp(a))
+
+
+def field_volume(phi: np.ndarray, spacing: float, evaluator_order: bool = False) -> float:
+    """calculateVolume of a bare cell field (numpy shape reversed(size)); evaluator_order
+    passes each cube's corners in the MC-style evaluator's own order (3D) instead of the
+    reference's x-fastest stencil order."""
+    a = np.ascontiguousarray(phi, dtype=np.float64)
+    size = (C.c_int * 3)(*([int(x) for x in reversed(a.shape)] + [1] * (3 - a.ndim)))
+    return load().orc_field_volume(a.ndim, size, float(spacing), _dp(a), int(evaluator_order))
+
+
+def mc_tables_ok() -> bool:
+    return bool(load().orc_mc_tables_ok())

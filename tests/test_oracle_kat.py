@@ -192,3 +192,61 @@ def test_ga_advection_rotation_converges(oracle_mod):
     assert errs[50] < 0.1 * (ROT_LENGTH / 50)
     assert errs[100] < 0.04 * (ROT_LENGTH / 100)
     assert errs[100] < errs[50] / 4
+
+
+def half_space_cube_volume(n, d0) -> float:
+    """Exact volume of {x in [0,1]^3 : n.(x - 1/2) + d0 < 0} (inclusion-exclusion over the
+    cube's corners of the simplex volumes max(b - a.v, 0)^3 / (6 a1 a2 a3), a > 0)."""
+    import itertools
+    a = np.array(n, dtype=float)
+    b = -d0 + 0.5 * a.sum()          # a.x < b
+    for k in range(3):                # reflect axes so every a_k > 0
+        if a[k] < 0:
+            b -= a[k]
+            a[k] = -a[k]
+    tot = 0.0
+    for v in itertools.product((0, 1), repeat=3):
+        tot += (-1) ** sum(v) * max(b - float(np.dot(a, v)), 0.0) ** 3
+    return tot / (6 * a[0] * a[1] * a[2])
+
+
+def test_volume_diagnostic_known_answers(oracle_mod):
+    """calculateVolume (LevelSetLiquid.cpp:1162-1190).  Cell pieces: empty and full
+    cells, a planar cut (exact for any plane: the surface is then the plane itself),
+    the marching-squares saddle rule; whole fields: a ball and a disk converge to
+    4/3 pi r^3 and pi r^2."""
+    import itertools
+    O = oracle_mod
+    assert O.mc_tables_ok()
+    assert O.mc_cube_volume([1.0] * 8) == 0.0 and O.mc_cube_volume([-1.0] * 8) == 1.0
+    corners = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    rng = np.random.default_rng(4)
+    for _ in range(500):
+        n = rng.normal(size=3)
+        d0 = rng.uniform(-0.6, 0.6)
+        vals = [float(np.dot(n, np.array(c) - 0.5) + d0) for c in corners]
+        assert abs(O.mc_cube_volume(vals) - half_space_cube_volume(n, d0)) < 1e-12
+    # marching squares: a planar cut is a polygon; a saddle joins through the centre iff the mean <= 0
+    assert abs(O.ms_square_area([-1.0, 1.0, -1.0, 1.0]) - 0.5) < 1e-15
+    assert abs(O.ms_square_area([-1.0, 1.0, 1.0, -0.5]) - (0.5 * 0.5 * 0.5 + 0.5 * (0.5 / 1.5) * (0.5 / 1.5))) < 1e-15
+    joined = O.ms_square_area([-1.0, 0.5, 0.5, -1.0])
+    assert joined > 0.5
+    # balls and disks.  The reference passes each cube to the evaluator in x-fastest
+    # order, which swaps two pairs of corners: its volumes converge at first order.
+    # In the evaluator's own order they converge at second order.
+    ref_err, own_err, disk_err = [], [], []
+    for s in (32, 64, 128):
+        dx = 1.0 / s
+        g = (np.arange(s) + 0.5) * dx
+        X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+        phi = np.ascontiguousarray((np.sqrt((X - .5) ** 2 + (Y - .5) ** 2 + (Z - .5) ** 2) - 0.3).transpose(2, 1, 0))
+        exact = 4 / 3 * np.pi * 0.3 ** 3
+        ref_err.append(abs(O.field_volume(phi, dx) / exact - 1))
+        own_err.append(abs(O.field_volume(phi, dx, evaluator_order=True) / exact - 1))
+        Y2, X2 = np.meshgrid(g, g, indexing="ij")
+        phi2 = np.sqrt((X2 - .5) ** 2 + (Y2 - .5) ** 2) - 0.3
+        disk_err.append(abs(O.field_volume(np.ascontiguousarray(phi2), dx) / (np.pi * 0.3 ** 2) - 1))
+    assert ref_err[0] < 2.5e-2 and ref_err[2] < 5e-3
+    assert ref_err[0] / ref_err[1] > 1.8 and ref_err[1] / ref_err[2] > 1.8      # first order
+    assert own_err[0] / own_err[1] > 3.2 and own_err[1] / own_err[2] > 3.2      # second order
+    assert disk_err[0] < 1e-2 and disk_err[1] / disk_err[2] > 3.0
