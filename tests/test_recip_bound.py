@@ -54,3 +54,36 @@ def test_reciprocal_edges():
     for x in (1.0, 2.0 ** 106, 1.5, 3.0, 7.0, 2.0 ** 53 - 1):
         r = refine(x, seed(x, 1))
         assert abs(Fraction(r) * Fraction(x) - 1) <= Fraction(2) ** -52
+
+
+def rsqrt_seed(x: float, ulps: int) -> float:
+    bits = np.float64(x).view(np.uint64)
+    xt = float(np.uint64((bits >> np.uint64(29)) << np.uint64(29)).view(np.float64))
+    y = np.float32(1.0) / np.sqrt(np.float32(xt))
+    for _ in range(abs(ulps) + 1):   # the hardware value may be a further ulp off
+        y = np.nextafter(y, np.float32(np.inf) if ulps >= 0 else np.float32(0))
+    return float(y)
+
+
+def rsqrt_refine(x: float, y: float) -> float:
+    """y(1 + e/2 + 3e^2/8), e = 1 - x y^2, with the device's fused operations."""
+    e = fma(-float(Fraction(x) * Fraction(y)), y, 1.0)   # x*y rounded, then fused
+    t = e * fma(e, 0.375, 0.5)
+    return fma(y, t, y)
+
+
+def test_inverse_sqrt_within_two_ulp():
+    """The WENO5 update's 1/sqrt (FP64 form) from an FP32 seed and one second-order
+    Newton step, checked against exact arithmetic over its range [2^-120, 2^120]."""
+    import math
+    rng = random.Random(7)
+    worst = 0.0
+    for _ in range(3000):
+        x = 2.0 ** rng.uniform(-120.0, 120.0)
+        for ulps in (-2, 0, 2):
+            r = rsqrt_refine(x, rsqrt_seed(x, ulps))
+            exact = 1 / math.sqrt(float(Fraction(x)))  # reference value in FP64
+            # compare in exact arithmetic: |r^2 x - 1| ~ 2 * relative error
+            rel = abs(Fraction(r) ** 2 * Fraction(x) - 1) / 2
+            worst = max(worst, float(rel))
+    assert worst <= 2.0 ** -52, worst
