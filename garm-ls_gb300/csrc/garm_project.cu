@@ -273,54 +273,59 @@ template <typename V> struct Pack;
 template <> struct __align__(16) Pack<float> { float r, w, s, d; };
 template <> struct __align__(32) Pack<double> { double r, w, s, d; };
 
-// Preconditioned CG in the Chronopoulos–Gear arrangement (one global reduction
-// per iteration), solving A e = rhs from e = 0 with the Jacobi preconditioner.
-// Mathematically it is the PCG of LinearSystem.h:23-39 (Eigen's algorithm, the
-// same stopping rule |r|^2 < max(tol^2 |b|^2, DBL_MIN), tol = max(tol, eps/|b|)):
+// Both forms run preconditioned CG in the Chronopoulos–Gear arrangement (one
+// global reduction per iteration), solving A e = rhs from e = 0 with the Jacobi
+// preconditioner.  Mathematically it is the PCG of LinearSystem.h:23-39 (Eigen's
+// algorithm, the same stopping rule |r|^2 < max(tol^2 |b|^2, DBL_MIN),
+// tol = max(tol, eps/|b|)):
 //     u = M^-1 r, w = A u,  γ = r·u,  δ = w·u,
 //     β = γ/γ_old, α = γ / (δ - β γ / α_old),
 //     p = u + β p,  s = w + β s,  x += α p,  r -= α s.
-// One iteration is one fused phase plus one grid barrier: a thread updates its
-// own unknowns and recomputes, from last iteration's {r, w, s} of its
-// neighbours, their new u (the same fma/mul sequence as the owner, so
-// bit-identical), which gives w_new = A u_new without a second barrier.  The
-// packed state is double-buffered.  Element arithmetic is in V; per-thread
-// partial dots are promoted to FP64 and reduced in a fixed order; α and β are
-// formed in FP64 (uniformly in every block).  Returns the number of matvecs.
-template <typename V> struct EntOf;
-template <> struct EntOf<double> { using T = NbW64; };
-template <> struct EntOf<float> { using T = NbW32; };
+// Per-thread partial dots are reduced in a fixed order; α and β are formed in FP64
+// by one lane of every block, identically in every block.
 
-template <int NB, typename V>
-__device__ int pcgCore(const CgArgs &a, int n, const typename EntOf<V>::T *__restrict__ ent, const V *__restrict__ dg, const V *__restrict__ invd, const double *rhsD,
-                       V *__restrict__ x, V *__restrict__ p, Pack<V> *st0, Pack<V> *st1, double tolRel, int maxIter, double *sh, unsigned &epoch,
-                       double *outRR, double *outB2, bool *ok) {
+// FP64 form: the iteration in two phases.  Phase 1 updates the own unknowns (p, s,
+// x, r) and publishes u = M^-1 r; after a grid barrier, phase 2 forms w = A u from
+// the neighbours' published u and the three dot products, then the reduction and
+// its barrier.  (The mixed form instead recomputes the neighbours' new u from their
+// packed {r, w, s} to save the first barrier; in FP64 that recompute, two fma and a
+// product per neighbour entry, costs more FP64-pipe time than the barrier.)
+template <int NB, bool Reg>
+__device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, unsigned &epoch, double *outRR, double *outB2, bool *ok) {
+	using V = double;
+	using E = NbW64;
 	const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x, nthr = int64_t(gridDim.x) * blockDim.x;
 	const int64_t S = a.stride;
-	Pack<V> *stb[2] = {st0, st1};
+	const E *__restrict__ ent = a.ent;
+	const V *__restrict__ dg = a.diag;
+	const V *__restrict__ invd = a.invd;
+	const double *__restrict__ rhs = a.b;
+	V *__restrict__ x = a.x;
+	V *__restrict__ p = a.p64;
+	V *__restrict__ uG = a.r64;                      // u = M^-1 r of every unknown
+	Pack<V> *__restrict__ st = (Pack<V> *)a.pack64[0];  // own {r, w, s, 1/diag}; only the owner reads it
 	// set-up: x = 0, r = b, s = 0, p = 0, w = A M^-1 b; partial r·u, w·u, r·r
 	V acc0 = V(0), acc1 = V(0), acc2 = V(0);
 	for (int64_t i = tid; i < n; i += nthr) {
-		const V bi = V(rhsD[i]), di = invd[i];
+		const V bi = rhs[i], di = invd[i];
 		const V ui = mulRn(bi, di);
 		V wi = dg[i] * ui;
 #pragma unroll
 		for (int k = 0; k < NB; k++) {
-			const auto e = ent[k * S + i];
-			if (e.nb >= 0) wi = fma(-V(e.w), mulRn(V(rhsD[e.nb]), invd[e.nb]), wi);
+			const E e = ent[k * S + i];
+			if (e.nb >= 0) wi = fma(-e.w, mulRn(rhs[e.nb], invd[e.nb]), wi);
 		}
 		x[i] = V(0); p[i] = V(0);
-		st0[i] = Pack<V>{bi, wi, V(0), di};
+		st[i] = Pack<V>{bi, wi, V(0), di};
 		acc0 = fma(bi, ui, acc0);
 		acc1 = fma(wi, ui, acc1);
 		acc2 = fma(bi, bi, acc2);
 	}
 	{
-		double acc[3] = {double(acc0), double(acc1), double(acc2)};
+		double acc[3] = {acc0, acc1, acc2};
 		blockPartials<3>(acc, a.partials, a.maxBlocks, sh);
 	}
 	if (!gridSync(a.bar, a.err, epoch)) { *ok = false; return 0; }
-	// totals γ, δ, |r|^2, then (lane 0 only) β = 0 and α = γ/δ for the first iteration
 	double tot[5];
 	gridTotals<3, 5>(a.partials, a.maxBlocks, tot, sh, [](double *t) { t[3] = 0; t[4] = t[0] / t[1]; });
 	double gamma = tot[0];
@@ -328,29 +333,23 @@ __device__ int pcgCore(const CgArgs &a, int n, const typename EntOf<V>::T *__res
 	*outB2 = rhsNorm2;
 	*outRR = rhsNorm2;
 	if (rhsNorm2 == 0) return 0;
-	const double tol = fmax(tolRel, DBL_EPSILON / sqrt(rhsNorm2));
+	const double tol = fmax(a.tol, DBL_EPSILON / sqrt(rhsNorm2));
 	const double threshold = fmax(tol * tol * rhsNorm2, DBL_MIN);
 	if (rhsNorm2 < threshold) return 0;
 
-	int cur = 0, it = 0;
-	if (n <= kRegUnknowns * nthr) {
-		// Register-resident path: each thread owns at most kRegUnknowns unknowns and
-		// keeps their neighbour entries, diagonal, p, x and packed state in registers
-		// for the whole solve; an iteration is the neighbour gathers, one packed store
-		// per unknown, the reduction and one barrier.
-		using E = typename EntOf<V>::T;
-		E en[kRegUnknowns][NB];
-		V dgi[kRegUnknowns], pp[kRegUnknowns], xx[kRegUnknowns];
-		Pack<V> me[kRegUnknowns];
-		bool own[kRegUnknowns];
+	E en[kRegUnknowns][NB];
+	V dgi[kRegUnknowns], pp[kRegUnknowns], xx[kRegUnknowns], un[kRegUnknowns];
+	Pack<V> me[kRegUnknowns];
+	bool own[kRegUnknowns];
+	if constexpr (Reg) {
 #pragma unroll
 		for (int c = 0; c < kRegUnknowns; c++) {
 			const int64_t i = tid + c * nthr;
 			own[c] = i < n;
-			pp[c] = V(0); xx[c] = V(0);
+			pp[c] = V(0); xx[c] = V(0); un[c] = V(0);
 			if (own[c]) {
 				dgi[c] = dg[i];
-				me[c] = st0[i];
+				me[c] = st[i];
 #pragma unroll
 				for (int k = 0; k < NB; k++) en[c][k] = ent[k * S + i];
 			} else {
@@ -360,12 +359,13 @@ __device__ int pcgCore(const CgArgs &a, int n, const typename EntOf<V>::T *__res
 				for (int k = 0; k < NB; k++) { en[c][k] = E{}; en[c][k].nb = -1; }
 			}
 		}
-		while (it < maxIter) {
-			const double alpha = tot[4];
-			const V bV = V(tot[3]), aV = V(alpha);
-			const Pack<V> *__restrict__ sc = stb[cur];
-			Pack<V> *__restrict__ sn = stb[cur ^ 1];
-			V g = V(0), d = V(0), rr = V(0);
+	}
+	int it = 0;
+	while (it < a.maxIter) {
+		const double alpha = tot[4];
+		const V bV = V(tot[3]), aV = V(alpha);
+		// phase 1: p, s, x, r and u of the own unknowns; u published
+		if constexpr (Reg) {
 #pragma unroll
 			for (int c = 0; c < kRegUnknowns; c++) {
 				if (!own[c]) continue;
@@ -373,80 +373,61 @@ __device__ int pcgCore(const CgArgs &a, int n, const typename EntOf<V>::T *__res
 				const V pi = fma(bV, pp[c], ui);
 				const V si = fma(bV, me[c].s, me[c].w);
 				const V rni = fma(-aV, si, me[c].r);
-				const V uni = mulRn(rni, me[c].d);
-				V wni = dgi[c] * uni;
-#pragma unroll
-				for (int k = 0; k < NB; k++) {
-					if (en[c][k].nb >= 0) {
-						const Pack<V> q = sc[en[c][k].nb];
-						const V snb = fma(bV, q.s, q.w);
-						const V rnb = fma(-aV, snb, q.r);
-						wni = fma(-V(en[c][k].w), mulRn(rnb, q.d), wni);
-					}
-				}
+				un[c] = mulRn(rni, me[c].d);
 				pp[c] = pi;
 				xx[c] = fma(aV, pi, xx[c]);
-				me[c] = Pack<V>{rni, wni, si, me[c].d};
-				sn[tid + c * nthr] = me[c];
+				me[c].r = rni; me[c].s = si;
+				uG[tid + c * nthr] = un[c];
+			}
+		} else {
+			for (int64_t i = tid; i < n; i += nthr) {
+				Pack<V> m = st[i];
+				const V ui = mulRn(m.r, m.d);
+				const V pi = fma(bV, p[i], ui);
+				const V si = fma(bV, m.s, m.w);
+				const V rni = fma(-aV, si, m.r);
+				uG[i] = mulRn(rni, m.d);
+				p[i] = pi;
+				x[i] = fma(aV, pi, x[i]);
+				m.r = rni; m.s = si;
+				st[i] = m;
+			}
+		}
+		if (!gridSync(a.bar, a.err, epoch)) { *ok = false; it++; break; }
+		// phase 2: w = A u from the neighbours' published u; γ = r·u, δ = w·u, |r|^2
+		V g = V(0), d = V(0), rr = V(0);
+		if constexpr (Reg) {
+#pragma unroll
+			for (int c = 0; c < kRegUnknowns; c++) {
+				if (!own[c]) continue;
+				V wni = dgi[c] * un[c];
+#pragma unroll
+				for (int k = 0; k < NB; k++)
+					if (en[c][k].nb >= 0) wni = fma(-en[c][k].w, uG[en[c][k].nb], wni);
+				me[c].w = wni;
+				g = fma(me[c].r, un[c], g);
+				d = fma(wni, un[c], d);
+				rr = fma(me[c].r, me[c].r, rr);
+			}
+		} else {
+			for (int64_t i = tid; i < n; i += nthr) {
+				const V uni = uG[i];
+				V wni = dg[i] * uni;
+#pragma unroll
+				for (int k = 0; k < NB; k++) {
+					const E e = ent[k * S + i];
+					if (e.nb >= 0) wni = fma(-e.w, uG[e.nb], wni);
+				}
+				const V rni = st[i].r;
+				st[i].w = wni;
 				g = fma(rni, uni, g);
 				d = fma(wni, uni, d);
 				rr = fma(rni, rni, rr);
 			}
-			cur ^= 1;
-			double acc[3] = {double(g), double(d), double(rr)};
-			blockPartials<3>(acc, a.partials, a.maxBlocks, sh);
-			if (!gridSync(a.bar, a.err, epoch)) { *ok = false; it++; break; }
-			const double gOld = gamma;
-			gridTotals<3, 5>(a.partials, a.maxBlocks, tot, sh, [gOld, alpha](double *t) {
-				t[3] = t[0] / gOld;
-				t[4] = t[0] / (t[1] - t[3] * t[0] / alpha);
-			});
-			it++;
-			*outRR = tot[2];
-			if (tot[2] < threshold) break;
-			gamma = tot[0];
 		}
-#pragma unroll
-		for (int c = 0; c < kRegUnknowns; c++)
-			if (own[c]) x[tid + c * nthr] = xx[c];
-		return it;
-	}
-	while (it < maxIter) {
-		const double alpha = tot[4];
-		const V bV = V(tot[3]), aV = V(alpha);
-		const Pack<V> *__restrict__ sc = stb[cur];
-		Pack<V> *__restrict__ sn = stb[cur ^ 1];
-		V g = V(0), d = V(0), rr = V(0);
-		for (int64_t i = tid; i < n; i += nthr) {
-			const Pack<V> me = sc[i];
-			const V ui = mulRn(me.r, me.d);
-			const V pi = fma(bV, p[i], ui);
-			const V si = fma(bV, me.s, me.w);
-			const V rni = fma(-aV, si, me.r);
-			const V uni = mulRn(rni, me.d);
-			V wni = dg[i] * uni;
-#pragma unroll
-			for (int k = 0; k < NB; k++) {
-				const auto e = ent[k * S + i];
-				if (e.nb >= 0) {
-					const Pack<V> q = sc[e.nb];
-					const V snb = fma(bV, q.s, q.w);
-					const V rnb = fma(-aV, snb, q.r);
-					wni = fma(-V(e.w), mulRn(rnb, q.d), wni);
-				}
-			}
-			p[i] = pi;
-			x[i] = fma(aV, pi, x[i]);
-			sn[i] = Pack<V>{rni, wni, si, me.d};
-			g = fma(rni, uni, g);
-			d = fma(wni, uni, d);
-			rr = fma(rni, rni, rr);
-		}
-		cur ^= 1;
-		double acc[3] = {double(g), double(d), double(rr)};
+		double acc[3] = {g, d, rr};
 		blockPartials<3>(acc, a.partials, a.maxBlocks, sh);
-		if (!gridSync(a.bar, a.err, epoch)) { *ok = false; return it + 1; }
-		// lane 0: β = γ_new/γ, α = γ_new / (δ_new - β γ_new / α_old); broadcast to the block
+		if (!gridSync(a.bar, a.err, epoch)) { *ok = false; it++; break; }
 		const double gOld = gamma;
 		gridTotals<3, 5>(a.partials, a.maxBlocks, tot, sh, [gOld, alpha](double *t) {
 			t[3] = t[0] / gOld;
@@ -456,6 +437,11 @@ __device__ int pcgCore(const CgArgs &a, int n, const typename EntOf<V>::T *__res
 		*outRR = tot[2];
 		if (tot[2] < threshold) break;
 		gamma = tot[0];
+	}
+	if constexpr (Reg) {
+#pragma unroll
+		for (int c = 0; c < kRegUnknowns; c++)
+			if (own[c]) x[tid + c * nthr] = xx[c];
 	}
 	return it;
 }
@@ -468,7 +454,9 @@ __global__ void __launch_bounds__(kCgBlock) kPcgFp64(CgArgs a) {
 	double rr = 0, b2 = 0;
 	bool ok = true;
 	unsigned epoch = 0;
-	const int mv = pcgCore<NB, double>(a, n, a.ent, a.diag, a.invd, a.b, a.x, a.p64, (Pack<double> *)a.pack64[0], (Pack<double> *)a.pack64[1], a.tol, a.maxIter, sh, epoch, &rr, &b2, &ok);
+	const int64_t nthr = int64_t(gridDim.x) * blockDim.x;
+	const int mv = n <= kRegUnknowns * nthr ? pcgFp64Split<NB, true>(a, n, sh, epoch, &rr, &b2, &ok)
+	                                        : pcgFp64Split<NB, false>(a, n, sh, epoch, &rr, &b2, &ok);
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		a.ints[0] = mv;
 		a.ints[1] = 1;
@@ -572,8 +560,11 @@ __device__ __forceinline__ double unitScale(double sumSq, int n) {
 	return rms > 0 ? ldexp(1.0, -ilogb(rms)) : 1.0;
 }
 
-// Mixed form: one FP32 PCG (the Chronopoulos–Gear iteration of pcgCore, FP32
-// vectors and element arithmetic, double-float dot products widened to FP64 per
+// Mixed form: one FP32 PCG (the Chronopoulos–Gear iteration above in one fused
+// phase per iteration: each thread updates its own unknowns and recomputes, from
+// last iteration's packed {r, w, s} of its neighbours, their new u with the owner's
+// fma/mul sequence, so bit-identically, which gives w = A u without a second
+// barrier; the packed state is double-buffered.  FP32 vectors and element arithmetic, double-float dot products widened to FP64 per
 // block, FP64 scalars) with FP64 residual replacement (van der Vorst & Ye,
 // "Residual replacement strategies for Krylov subspace iterative methods",
 // SIAM J. Sci. Comput. 22, 2000, as used by reliable-update mixed-precision CG).
@@ -667,7 +658,7 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 		}
 	}
 	while (it < a.maxIter) {
-		// ---- one C-G iteration (as pcgCore) ----
+		// ---- one fused C-G iteration ----
 		const double alpha = tot[4];
 		const V bV = V(tot[3]), aV = V(alpha);
 		{
