@@ -196,8 +196,13 @@ __device__ __forceinline__ bool isNegative(double x) {
 __device__ __forceinline__ bool isNegative(float x) { return x < 0.f; }
 
 template <typename T> struct WenoConst {
-	// ε floor: 1e-99 in FP64 (Derivatives.h:144); FP32 takes the smallest comparable normal number
-	static constexpr T floorEps = sizeof(T) == 8 ? T(1e-99) : T(1e-30);
+	// ε = 1e-6 max v_k^2 + 1e-99 in FP64 (Derivatives.h:144); FP32 takes 1e-30 as the floor
+	// The weights depend only on the ratios of the s_k + ε, so the indicators and ε
+	// may carry one common factor.  Every form here uses four times the reference's
+	// (cell and column forms: s_k = 13/3 e^2 + f^2; sweep form: Jiang & Peng's
+	// 13(x-y)^2 + 3 l^2 divided by 3), which makes each indicator one fma.
+	static constexpr T epsScale = T(4e-6);
+	static constexpr T floorEps4 = sizeof(T) == 8 ? T(4e-99) : T(4e-30);
 };
 
 // One one-sided derivative in ratio form.  num/den · 1/(6 dx) is the derivative.
@@ -229,10 +234,12 @@ __device__ __forceinline__ Ratio<T> leftRole(const FaceWeights<T> &w, T R1, T R2
 }
 // Smoothness indicators of (v1, v2, v3) in the three positions of a face set
 // (Derivatives.h:147-149): g = 13/12 (v1-2v2+v3)^2 is common to all three.
-template <typename T> __device__ __forceinline__ T smoothG(T a, T b, T c) { const T e = a - T(2) * b + c; return T(13.0 / 12.0) * e * e; }
-template <typename T> __device__ __forceinline__ T smoothL(T g, T a, T b, T c) { const T f = a - T(4) * b + T(3) * c; return fma(T(0.25) * f, f, g); }
-template <typename T> __device__ __forceinline__ T smoothM(T g, T a, T c) { const T f = a - c; return fma(T(0.25) * f, f, g); }
-template <typename T> __device__ __forceinline__ T smoothR(T g, T a, T b, T c) { const T f = T(3) * a - T(4) * b + c; return fma(T(0.25) * f, f, g); }
+// (Derivatives.h:147-149, all four times the reference's: g = 13/3 (v1-2v2+v3)^2 is
+// common to the three positions, and the second square enters with weight 1.)
+template <typename T> __device__ __forceinline__ T smoothG(T a, T b, T c) { const T e = a - T(2) * b + c; return (T(13.0 / 3.0) * e) * e; }
+template <typename T> __device__ __forceinline__ T smoothL(T g, T a, T b, T c) { const T f = a - T(4) * b + T(3) * c; return fma(f, f, g); }
+template <typename T> __device__ __forceinline__ T smoothM(T g, T a, T c) { const T f = a - c; return fma(f, f, g); }
+template <typename T> __device__ __forceinline__ T smoothR(T g, T a, T b, T c) { const T f = T(3) * a - T(4) * b + c; return fma(f, f, g); }
 // Candidate stencils (6× the third-order one-sided values)
 template <typename T> __device__ __forceinline__ T stencil1(T a, T b, T c) { return T(2) * a - T(7) * b + T(11) * c; }
 template <typename T> __device__ __forceinline__ T stencil2(T a, T b, T c) { return -a + T(5) * b + T(2) * c; }
@@ -245,8 +252,8 @@ template <typename T>
 __device__ __forceinline__ void wenoCell(const T v[7], Ratio<T> &m, Ratio<T> &p) {
 	const T D1 = v[1] - v[0], D2 = v[2] - v[1], D3 = v[3] - v[2], D4 = v[4] - v[3], D5 = v[5] - v[4], D6 = v[6] - v[5];
 	const T M = maxNonNeg(maxNonNeg(D2 * D2, D3 * D3), maxNonNeg(D4 * D4, D5 * D5));
-	const T epsM = fma(maxNonNeg(M, D1 * D1), T(1e-6), WenoConst<T>::floorEps);
-	const T epsP = fma(maxNonNeg(M, D6 * D6), T(1e-6), WenoConst<T>::floorEps);
+	const T epsM = fma(maxNonNeg(M, D1 * D1), WenoConst<T>::epsScale, WenoConst<T>::floorEps4);
+	const T epsP = fma(maxNonNeg(M, D6 * D6), WenoConst<T>::epsScale, WenoConst<T>::floorEps4);
 	const T g1 = smoothG(D1, D2, D3), g2 = smoothG(D2, D3, D4), g3 = smoothG(D3, D4, D5), g4 = smoothG(D4, D5, D6);
 	const FaceWeights<T> wm = faceWeights(smoothL(g1, D1, D2, D3), smoothM(g2, D2, D4), smoothR(g3, D3, D4, D5), epsM);
 	const FaceWeights<T> wp = faceWeights(smoothL(g2, D2, D3, D4), smoothM(g3, D3, D5), smoothR(g4, D4, D5, D6), epsP);
@@ -349,7 +356,7 @@ __global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__rest
 	{
 		const T E1 = v[1] - v[0], E2 = v[2] - v[1], E3 = v[3] - v[2], E4 = v[4] - v[3], E5 = v[5] - v[4];
 		const T Q = maxNonNeg(maxNonNeg(maxNonNeg(E1 * E1, E2 * E2), maxNonNeg(E3 * E3, E4 * E4)), E5 * E5);
-		const T eps = fma(Q, T(1e-6), WenoConst<T>::floorEps);
+		const T eps = fma(Q, WenoConst<T>::epsScale, WenoConst<T>::floorEps4);
 		const FaceWeights<T> fw = faceWeights(smoothL(smoothG(E1, E2, E3), E1, E2, E3), smoothM(smoothG(E2, E3, E4), E2, E4),
 		                                      smoothR(smoothG(E3, E4, E5), E3, E4, E5), eps);
 		mW = rightRole(fw, stencil1(E1, E2, E3), stencil2(E2, E3, E4), stencil3(E3, E4, E5));
@@ -368,7 +375,7 @@ __global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__rest
 		const T gC = smoothG(E3, E4, E5);
 		const T Q = maxNonNeg(maxNonNeg(maxNonNeg(S1, S2), maxNonNeg(S3, S4)), S5);
 		const FaceWeights<T> fw = faceWeights(smoothL(gA, E1, E2, E3), smoothM(gB, E2, E4), smoothR(gC, E3, E4, E5),
-		                                      fma(Q, T(1e-6), WenoConst<T>::floorEps));
+		                                      fma(Q, WenoConst<T>::epsScale, WenoConst<T>::floorEps4));
 		const Ratio<T> pW = leftRole(fw, stencil1(E5, E4, E3), stencil2(E4, E3, E2), stencil3(E3, E2, E1));
 		const Ratio<T> mNext = rightRole(fw, stencil1(E1, E2, E3), stencil2(E2, E3, E4), stencil3(E3, E4, E5));
 		T sum = godunovSq(neg, mW, pW);
@@ -407,14 +414,17 @@ __global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__rest
 // (D_{i-1} + D_{i+2}) shared by both one-sided derivatives of cell i, and a
 // correction in the face's third differences T1 = a-2b+c, T2 = b-2c+d of its
 // second differences a..d, whose smoothness indicators are
-// 13(x-y)^2 + 3(..)^2 (12 times the reference's, with ε scaled by 12 alike):
+// 13(x-y)^2 + 3(..)^2 = 12 times the reference's (computed here divided by 3,
+// 13/3 (x-y)^2 + (..)^2, with ε scaled alike: see WenoConst):
 //   12 φ⁻(i+1) = 12C(i+1) + T2 - (.4 t2t3 T1 + .6 t1t2 T2) / (.1 t2t3 + .6 t1t3 + .3 t1t2)
 //   12 φ⁺(i)   = 12C(i)   - T1 + (.4 t1t2 T2 + .6 t2t3 T1) / (.1 t1t2 + .6 t1t3 + .3 t2t3)
 // Differences, squares, g terms, third differences and central parts slide
 // with the walk, so a face costs about 57 operations against ~116 per axis of
 // the cell form.  The Godunov sum of the first passes goes to `out` (x pass:
 // stored, y pass: added); the last pass adds its own and applies the update.
-template <typename T> __device__ __forceinline__ T g13(T x, T y) { const T d = x - y; return (T(13) * d) * d; }
+// 13/3 (x-y)^2: the indicators here are 13(x-y)^2 + 3 l^2 divided by 3 (with ε
+// alike), so the second square enters with weight 1 (one fma per indicator).
+template <typename T> __device__ __forceinline__ T g13(T x, T y) { const T d = x - y; return (T(13.0 / 3.0) * d) * d; }
 
 template <int D, typename T, int A, int Mode>
 __global__ void __launch_bounds__(256) kWenoSweep(G<D, T> g, const T *__restrict__ in, const T *base, T *out, T dt, int chunk) {
@@ -434,7 +444,7 @@ __global__ void __launch_bounds__(256) kWenoSweep(G<D, T> g, const T *__restrict
 	const T *line = in + lb;
 	const int last = len - 1;
 	auto ld = [&](int w) { return ldg(line + int64_t(min(max(w, 0), last)) * st); };
-	const T epsFloor = sizeof(T) == 8 ? T(1.2e-98) : T(1.2e-29);  // 12 x the reference's ε floor
+	const T epsFloor = WenoConst<T>::floorEps4;  // 12/3 = 4 x the reference's ε
 	// state before the face f0 = w0 - 1 (between cells w0-1 and w0): φ_{f0-2 .. f0+2}
 	const int f0 = w0 - 1;
 	const T p0 = ld(f0 - 2), p1 = ld(f0 - 1);
@@ -455,9 +465,9 @@ __global__ void __launch_bounds__(256) kWenoSweep(G<D, T> g, const T *__restrict
 		const T T2x4 = T(0.4) * T2, T2x6 = T(0.6) * T2;
 		const T gcd = g13(c, d);
 		const T l0 = fma(T(-3), b, a), l1 = b + c, l2 = fma(T(3), c, -d);
-		const T is0 = fma(T(3) * l0, l0, gab), is1 = fma(T(3) * l1, l1, gbc), is2 = fma(T(3) * l2, l2, gcd);
+		const T is0 = fma(l0, l0, gab), is1 = fma(l1, l1, gbc), is2 = fma(l2, l2, gcd);
 		const T Qm = maxNonNeg(maxNonNeg(maxNonNeg(Q1, Q2), maxNonNeg(Q3, Q4)), Q5);
-		const T eps = fma(Qm, T(1.2e-5), epsFloor);
+		const T eps = fma(Qm, WenoConst<T>::epsScale, epsFloor);
 		const T sc = pow2NegExp(eps), es = eps * sc;
 		const T q1 = fma(is0, sc, es), q2 = fma(is1, sc, es), q3 = fma(is2, sc, es);
 		const T t1 = q1 * q1, t2 = q2 * q2, t3 = q3 * q3;
