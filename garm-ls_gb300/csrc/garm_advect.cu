@@ -153,68 +153,85 @@ __global__ void __launch_bounds__(kBlock) kAdvectRefMap(Geom geom, VelView<D, T>
 	}
 
 	T val[D], grad[D * D];  // grad[c*D + a] = ∂ξ_c/∂x_a (before invDx)
+	// The interpolant is Σ over vertices v and term orders o of C(v,o)·Π_a B_a[v_a][o_a],
+	// and its derivative along a replaces B_a by D_a.  It is contracted one axis at a
+	// time, each axis summing over its vertex and its term order together: x for every
+	// (y, z) vertex and order (value and d/dx), then y, then z.  Coefficient order o:
+	// bit 0 d/dx, bit 1 d/dy, bit 2 d/dz (f, Π col 0, Π col 1, mixed xy, Π col 2,
+	// mixed xz, mixed yz, mixed xyz).
 #pragma unroll
 	for (int c = 0; c < D; c++) {
-		val[c] = T(0);
-#pragma unroll
-		for (int a = 0; a < D; a++) grad[c * D + a] = T(0);
-	}
-
-#pragma unroll
-	for (int c = 0; c < D; c++) {
-		// Contract over the vertices and term orders directly: for each vertex v and
-		// term mask o the coefficient is C(v,o); its weight is Π_a B_a[v_a][o_a].
-#pragma unroll
-		for (int v = 0; v < (1 << D); v++) {
-			const int64_t n = nid[v];
-			T coef[1 << D];
-			coef[0] = ldg(io.xi[c] + n);
-			coef[1] = ldg(io.Pi[0 * D + c] + n);
-			coef[2] = ldg(io.Pi[1 * D + c] + n);
-			coef[3] = ldg(io.mixed[0 * D + c] + n);
-			if (D == 3) {
-				coef[4] = ldg(io.Pi[2 * D + c] + n);
-				coef[5] = ldg(io.mixed[1 * D + c] + n);
-				coef[6] = ldg(io.mixed[2 * D + c] + n);
-				coef[7] = ldg(io.mixed[3 * D + c] + n);
+		auto coefOf = [&](int64_t n, int o) -> T {
+			switch (o) {
+			case 0: return ldg(io.xi[c] + n);
+			case 1: return ldg(io.Pi[0 * D + c] + n);
+			case 2: return ldg(io.Pi[1 * D + c] + n);
+			case 3: return ldg(io.mixed[0 * D + c] + n);
+			case 4: return ldg(io.Pi[2 * D + c] + n);
+			case 5: return ldg(io.mixed[1 * D + c] + n);
+			case 6: return ldg(io.mixed[2 * D + c] + n);
+			default: return ldg(io.mixed[3 * D + c] + n);
 			}
-			const int vb[3] = {v & 1, (v >> 1) & 1, (v >> 2) & 1};
-			if (D == 2) {
-				// x-contraction for each y-order
-				T sx[2], sdx[2];
+		};
+		if (D == 2) {
+			T X0[2][2], X1[2][2];  // [vy][oy]: x-contracted value and d/dx
+#pragma unroll
+			for (int vy = 0; vy < 2; vy++) {
+				const int64_t n0 = nid[vy << 1 | 0], n1 = nid[vy << 1 | 1];
 #pragma unroll
 				for (int oy = 0; oy < 2; oy++) {
-					const T c0 = coef[oy << 1 | 0], c1 = coef[oy << 1 | 1];
-					sx[oy] = c0 * B[0][vb[0]][0] + c1 * B[0][vb[0]][1];
-					sdx[oy] = c0 * Dd[0][vb[0]][0] + c1 * Dd[0][vb[0]][1];
+					const T a0 = coefOf(n0, oy << 1 | 0), a1 = coefOf(n0, oy << 1 | 1);
+					const T b0 = coefOf(n1, oy << 1 | 0), b1 = coefOf(n1, oy << 1 | 1);
+					X0[vy][oy] = fma(a0, B[0][0][0], fma(a1, B[0][0][1], fma(b0, B[0][1][0], b1 * B[0][1][1])));
+					X1[vy][oy] = fma(a0, Dd[0][0][0], fma(a1, Dd[0][0][1], fma(b0, Dd[0][1][0], b1 * Dd[0][1][1])));
 				}
-				val[c] += sx[0] * B[1][vb[1]][0] + sx[1] * B[1][vb[1]][1];
-				grad[c * D + 0] += sdx[0] * B[1][vb[1]][0] + sdx[1] * B[1][vb[1]][1];
-				grad[c * D + 1] += sx[0] * Dd[1][vb[1]][0] + sx[1] * Dd[1][vb[1]][1];
-			} else {
-				T syz = T(0), sdxyz = T(0), sdyz = T(0), sdz = T(0);
+			}
+			T v = T(0), gx = T(0), gy = T(0);
+#pragma unroll
+			for (int vy = 0; vy < 2; vy++)
+#pragma unroll
+				for (int oy = 0; oy < 2; oy++) {
+					v = fma(X0[vy][oy], B[1][vy][oy], v);
+					gx = fma(X1[vy][oy], B[1][vy][oy], gx);
+					gy = fma(X0[vy][oy], Dd[1][vy][oy], gy);
+				}
+			val[c] = v; grad[c * D + 0] = gx; grad[c * D + 1] = gy;
+		} else {
+			T Y0[2][2], Yx[2][2], Yy[2][2];  // [vz][oz]: xy-contracted value, d/dx, d/dy
+#pragma unroll
+			for (int vz = 0; vz < 2; vz++)
+#pragma unroll
+				for (int oz = 0; oz < 2; oz++) { Y0[vz][oz] = T(0); Yx[vz][oz] = T(0); Yy[vz][oz] = T(0); }
+#pragma unroll
+			for (int vz = 0; vz < 2; vz++)
+#pragma unroll
+				for (int vy = 0; vy < 2; vy++) {
+					const int64_t n0 = nid[vz << 2 | vy << 1 | 0], n1 = nid[vz << 2 | vy << 1 | 1];
+#pragma unroll
+					for (int oz = 0; oz < 2; oz++)
+#pragma unroll
+						for (int oy = 0; oy < 2; oy++) {
+							const int o = oz << 2 | oy << 1;
+							const T a0 = coefOf(n0, o), a1 = coefOf(n0, o | 1);
+							const T b0 = coefOf(n1, o), b1 = coefOf(n1, o | 1);
+							const T x0 = fma(a0, B[0][0][0], fma(a1, B[0][0][1], fma(b0, B[0][1][0], b1 * B[0][1][1])));
+							const T x1 = fma(a0, Dd[0][0][0], fma(a1, Dd[0][0][1], fma(b0, Dd[0][1][0], b1 * Dd[0][1][1])));
+							Y0[vz][oz] = fma(x0, B[1][vy][oy], Y0[vz][oz]);
+							Yx[vz][oz] = fma(x1, B[1][vy][oy], Yx[vz][oz]);
+							Yy[vz][oz] = fma(x0, Dd[1][vy][oy], Yy[vz][oz]);
+						}
+				}
+			T v = T(0), gx = T(0), gy = T(0), gz = T(0);
+#pragma unroll
+			for (int vz = 0; vz < 2; vz++)
 #pragma unroll
 				for (int oz = 0; oz < 2; oz++) {
-					T sy = T(0), sdxy = T(0), sdy = T(0);
-#pragma unroll
-					for (int oy = 0; oy < 2; oy++) {
-						const T c0 = coef[oz << 2 | oy << 1 | 0], c1 = coef[oz << 2 | oy << 1 | 1];
-						const T sx = c0 * B[0][vb[0]][0] + c1 * B[0][vb[0]][1];
-						const T sdx = c0 * Dd[0][vb[0]][0] + c1 * Dd[0][vb[0]][1];
-						sy += sx * B[1][vb[1]][oy];
-						sdxy += sdx * B[1][vb[1]][oy];
-						sdy += sx * Dd[1][vb[1]][oy];
-					}
-					syz += sy * B[2][vb[2]][oz];
-					sdxyz += sdxy * B[2][vb[2]][oz];
-					sdyz += sdy * B[2][vb[2]][oz];
-					sdz += sy * Dd[2][vb[2]][oz];
+					v = fma(Y0[vz][oz], B[2][vz][oz], v);
+					gx = fma(Yx[vz][oz], B[2][vz][oz], gx);
+					gy = fma(Yy[vz][oz], B[2][vz][oz], gy);
+					gz = fma(Y0[vz][oz], Dd[2][vz][oz], gz);
 				}
-				val[c] += syz;
-				grad[c * D + 0] += sdxyz;
-				grad[c * D + 1] += sdyz;
-				grad[c * D + 2] += sdz;
-			}
+			val[c] = v; grad[c * D + 0] = gx; grad[c * D + 1] = gy; grad[c * D + 2] = gz;
 		}
 	}
 
