@@ -342,6 +342,7 @@ garm_status enqueueStep(State &s, bool timed) {
 	if (timed) GARM_TRY(record(s, 7));
 	GARM_TRY(GARM_DISPATCH(s, extrapolateToAir, s));
 	GARM_TRY(GARM_DISPATCH(s, enforceBoundaryConditions, s));
+	if (s.cfg.record_volume) GARM_TRY(GARM_DISPATCH(s, recordVolumeAsync, s));  // calculateVolume, a diagnostic
 	if (timed) GARM_TRY(record(s, 8));
 	s.stepIndex++;
 	return GARM_OK;
@@ -381,6 +382,7 @@ garm_status readRecords(State &s, int k, garm_step_stats *S) {
 		S->cg_iterations = int(rec[kStCgIters]);
 		S->cg_refinements = int(rec[kStCgRefine]);
 		S->cg_residual = rec[kStCgResidual];
+		S->volume = s.cfg.record_volume ? rec[kStVolume] : 0.0;
 		s.nUnknowns = S->unknowns;
 	}
 	return worst;
@@ -555,6 +557,7 @@ garm_status garm_config_default(garm_config *c) {
 	c->mixed_residual_drop = 0.1;
 	c->mixed_replace_interval = 0;
 	c->cg_cells_per_block = 0;
+	c->record_volume = 0;
 	return GARM_OK;
 }
 
@@ -598,6 +601,7 @@ garm_status garm_sim_create(const garm_grid_desc *gd, const garm_config *cfg, vo
 	if (cfg) c = *cfg; else garm_config_default(&c);
 	if (c.precision != GARM_PRECISION_FP64 && c.precision != GARM_PRECISION_MIXED) return GARM_INVALID;
 	if (c.reinit_iters < 0 || c.cg_max_iters < 0 || !(c.cg_tolerance > 0) || c.cg_cells_per_block < 0) return GARM_INVALID;
+	if (c.record_volume != 0 && c.record_volume != 1) return GARM_INVALID;
 
 	garm_sim *sim = new (std::nothrow) garm_sim();
 	if (!sim) return GARM_OOM;
@@ -643,6 +647,7 @@ garm_status garm_sim_create(const garm_grid_desc *gd, const garm_config *cfg, vo
 	// every grid (cells, nodes, faces) must index with 32-bit integers
 	if (s.NN >= (int64_t(1) << 31) || s.Ftot >= (int64_t(1) << 31)) { freeAll(s); delete sim; return GARM_INVALID; }
 	garm_status r = allocState(s);
+	if (r == GARM_OK && D == 3 && s.cfg.record_volume) r = loadVolumeTables();  // before any step capture
 	if (r == GARM_OK) r = GARM_DISPATCH(s, initBoundary, s);           // Boundary ctor → reset()
 	if (r == GARM_OK) {
 		// _levelSet starts at +inf (LevelSetLiquid.cpp:49); the scene is then uploaded

@@ -110,7 +110,7 @@ __device__ __forceinline__ double *stepRecord(double *base, const unsigned long 
 }
 
 // Layout of one per-step statistics record on the device.
-enum StatSlot { kStDt = 0, kStRestarted, kStRmTotal, kStRmBad, kStUnknowns, kStCgIters, kStCgRefine, kStCgResidual, kStCgTol, kStCgErr, kStatsSlots = 12 };
+enum StatSlot { kStDt = 0, kStRestarted, kStRmTotal, kStRmBad, kStUnknowns, kStCgIters, kStCgRefine, kStCgResidual, kStCgTol, kStCgErr, kStVolume, kStatsSlots = 12 };
 
 // Stage entry points (templated on dimension D and working type T).
 template <int D, typename T> garm_status initBoundary(State &s);
@@ -120,6 +120,10 @@ template <int D, typename T> garm_status generateCurrentFields(State &s);
 template <int D, typename T> garm_status reinitialize(State &s);
 // calculateVolume of tmp (synchronises the stream); evaluatorOrder: 3D corner order (see garm.h).
 template <int D, typename T> garm_status levelSetVolume(State &s, int evaluatorOrder, double *out);
+// The same enqueued on the stream with the result written to the current step record.
+template <int D, typename T> garm_status recordVolumeAsync(State &s);
+// Load the volume tables onto the current device (before any stream capture).
+garm_status loadVolumeTables();
 // Launch plan (form GARM_REINIT_*, threads per block, cells per thread) the
 // reinitialisation autotuner chose for this grid, and its sub-stage time in ms.
 template <int D, typename T> garm_status reinitPlanInfo(State &s, int *form, int *block, int *chunk, float *ms);

@@ -284,33 +284,52 @@ __global__ void __launch_bounds__(kBlock) kVolumeCells(int sx, int sy, int sz, c
 	if (threadIdx.x == 0) partials[blockIdx.x] = b;
 }
 
-__global__ void kVolumeTotal(const double *partials, int n, double scale, double *out) {
+// Fixed-order sum of the block sums; to `out`, or to the current step record.
+__global__ void kVolumeTotal(const double *partials, int n, double scale, double *out, double *stats, const unsigned long long *counter) {
 	if (threadIdx.x != 0 || blockIdx.x != 0) return;
 	double s = 0;
 	for (int b = 0; b < n; b++) s += partials[b];
-	*out = s * scale;
+	if (out) *out = s * scale;
+	if (stats) {
+		double *rec = stepRecord(stats, counter);
+		if (rec) rec[kStVolume] = s * scale;
+	}
+}
+
+// Enqueue the volume of tmp; the result goes to devOut and/or the current step record.
+template <int D, typename T>
+garm_status enqueueVolume(State &s, int evaluatorOrder, double *devOut, bool toRecord) {
+	const int sx = s.geom.n[0], sy = s.geom.n[1], sz = D == 3 ? s.geom.n[2] : 1;
+	const int64_t nc = int64_t(sx - 1) * (sy - 1) * (D == 3 ? sz - 1 : 1);
+	const int cap = s.maxBlocks * 4;  // the partials buffer holds maxBlocks * 4 doubles
+	const int blocks = int(std::max<int64_t>(1, std::min<int64_t>((nc + kBlock - 1) / kBlock, cap)));
+	const double dx = s.geom.dx;
+	kVolumeCells<D, T><<<blocks, kBlock, 0, s.stream>>>(sx, sy, sz, (const T *)s.tmp, evaluatorOrder, s.partials); s.launches++;
+	kVolumeTotal<<<1, 32, 0, s.stream>>>(s.partials, blocks, D == 3 ? dx * dx * dx : dx * dx, devOut,
+	                                      toRecord ? s.statsDev : nullptr, s.stepCounter); s.launches++;
+	GARM_CHECK_LAUNCH();
+	return GARM_OK;
 }
 
 }  // namespace
 
+garm_status loadVolumeTables() { return ensureTables(); }
+
 template <int D, typename T>
 garm_status levelSetVolume(State &s, int evaluatorOrder, double *out) {
 	if (D == 3) GARM_TRY(ensureTables());
-	const int sx = s.geom.n[0], sy = s.geom.n[1], sz = D == 3 ? s.geom.n[2] : 1;
-	const int64_t nc = int64_t(sx - 1) * (sy - 1) * (D == 3 ? sz - 1 : 1);
-	if (nc <= 0) { *out = 0; return GARM_OK; }
-	const int cap = s.maxBlocks * 4;  // the partials buffer holds maxBlocks * 4 doubles
-	const int blocks = int(std::min<int64_t>((nc + kBlock - 1) / kBlock, cap));
-	const double dx = s.geom.dx;
-	kVolumeCells<D, T><<<blocks, kBlock, 0, s.stream>>>(sx, sy, sz, (const T *)s.tmp, evaluatorOrder, s.partials); s.launches++;
-	kVolumeTotal<<<1, 32, 0, s.stream>>>(s.partials, blocks, D == 3 ? dx * dx * dx : dx * dx, s.volumeOut); s.launches++;
-	GARM_CHECK_LAUNCH();
+	GARM_TRY((enqueueVolume<D, T>(s, evaluatorOrder, s.volumeOut, false)));
 	if (cudaMemcpyAsync(out, s.volumeOut, sizeof(double), cudaMemcpyDeviceToHost, s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
 	if (cudaStreamSynchronize(s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
 	return GARM_OK;
 }
 
-#define GARM_INST(D, T) template garm_status levelSetVolume<D, T>(State &, int, double *);
+template <int D, typename T>
+garm_status recordVolumeAsync(State &s) {
+	return enqueueVolume<D, T>(s, 0, nullptr, true);  // tables are loaded at creation
+}
+
+#define GARM_INST(D, T) template garm_status levelSetVolume<D, T>(State &, int, double *); template garm_status recordVolumeAsync<D, T>(State &);
 GARM_INST(2, double)
 GARM_INST(3, double)
 GARM_INST(2, float)

@@ -52,13 +52,13 @@ class Config(C.Structure):
                 ("boundary_extrap_radius", C.c_double), ("air_extrap_radius", C.c_double),
                 ("rm_threshold", C.c_double), ("rm_band", C.c_double), ("rm_ratio", C.c_double),
                 ("enable_gravity", C.c_int), ("mixed_residual_drop", C.c_double),
-                ("mixed_replace_interval", C.c_int), ("cg_cells_per_block", C.c_int)]
+                ("mixed_replace_interval", C.c_int), ("cg_cells_per_block", C.c_int), ("record_volume", C.c_int)]
 
 
 class StepStats(C.Structure):
     _fields_ = [("restarted", C.c_int), ("cg_iterations", C.c_int), ("cg_refinements", C.c_int),
                 ("unknowns", C.c_int), ("cg_residual", C.c_double), ("rm_total", C.c_int), ("rm_bad", C.c_int),
-                ("ms_total", C.c_double), ("ms_stage", C.c_double * 8)]
+                ("ms_total", C.c_double), ("ms_stage", C.c_double * 8), ("volume", C.c_double)]
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "ms_stage"}

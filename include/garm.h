@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define GARM_ABI_VERSION 2
+#define GARM_ABI_VERSION 3
 
 typedef enum garm_status {
     GARM_OK = 0,
@@ -96,6 +96,8 @@ typedef struct garm_config {
     int cg_cells_per_block;           /* pressure solve: one 512-thread block (one SM) per this many interior
                                          cells, at most one per SM; 0 selects 4096.  Larger values leave
                                          SMs free for other scenes' work when scenes run concurrently */
+    int record_volume;                /* 1: every step ends with the volume diagnostic (garm_sim_volume, corner
+                                         order 0) written to its statistics on the device (no host round trip) */
 } garm_config;
 
 /* Per-step statistics returned by garm_sim_advance. */
@@ -110,6 +112,7 @@ typedef struct garm_step_stats {
     double ms_total;          /* device time of the step (CUDA events) */
     double ms_stage[8];       /* advect, compose, reinit, extrap_collider, rm_check+restart,
                                  body_force, project, extrap_air+enforce_bc */
+    double volume;            /* liquid volume after the step when record_volume is set, else 0 */
 } garm_step_stats;
 
 typedef struct garm_sim garm_sim;

@@ -28,6 +28,7 @@ def host_default_config(**kw) -> capi.Config:
     c.mixed_residual_drop = 0.1
     c.mixed_replace_interval = 0
     c.cg_cells_per_block = 0
+    c.record_volume = 0
     for k, v in kw.items():
         setattr(c, k, v)
     return c

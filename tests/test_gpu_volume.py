@@ -46,3 +46,25 @@ def test_volume_rejects_bad_order(garm_lib):
     assert g.lib.garm_sim_volume(g.handle, 2, capi.C.byref(v)) == capi.INVALID
     assert g.lib.garm_sim_volume(g.handle, 0, None) == capi.INVALID
     g.close()
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_volume_recorded_per_step(oracle_mod, garm_lib, dim):
+    """record_volume: every step's statistics carry the volume of tmp, computed on the
+    device inside the step (also inside replayed step graphs) and equal to the volume
+    the synchronous call gives for the same state."""
+    sc = scenes.dam_break(dim, 32 if dim == 3 else 64)
+    cfg = host_default_config(record_volume=1)
+    g = capi.Simulation(sc.grid, cfg)
+    load_scene(g, sc)
+    g.initialize()
+    g.stage("restart")
+    g.set_clock(25, 1.0)
+    vols = []
+    for _ in range(4):
+        st = g.advance_auto(1)
+        vols.append(st["volume"])
+        assert st["volume"] == g.volume()
+    assert all(v > 0 for v in vols)
+    assert g.graph_active()
+    g.close()
