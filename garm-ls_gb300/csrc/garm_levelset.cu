@@ -313,12 +313,18 @@ __global__ void __launch_bounds__(kBlock) kReinitCells(G<D, T> g, const T *__res
 	const int pos[3] = {i, j, k};
 	const int str[3] = {1, sx, sxy};
 	const bool neg = isNegative(f);
+	const bool inner = i >= 3 && i + 3 < sx && j >= 3 && j + 3 < sy && (D == 2 || (k >= 3 && k + 3 < sz));
 	T sum = T(0);
 #pragma unroll
 	for (int a = 0; a < D; a++) {
 		T v[7];
+		if (inner) {
 #pragma unroll
-		for (int t = 0; t < 7; t++) v[t] = ldg(line[a] + min(max(pos[a] + t - 3, 0), lim[a]) * str[a]);
+			for (int t = 0; t < 7; t++) v[t] = ldg(in + id + (t - 3) * int64_t(str[a]));
+		} else {
+#pragma unroll
+			for (int t = 0; t < 7; t++) v[t] = ldg(line[a] + min(max(pos[a] + t - 3, 0), lim[a]) * str[a]);
+		}
 		Ratio<T> m, p;
 		wenoCell<T>(v, m, p);
 		sum += godunovSq(neg, m, p);
@@ -345,6 +351,7 @@ __global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__rest
 	const int w1 = min(w0 + chunk, sw);
 	const int j = D == 3 ? pidx / sx : 0;
 	const int i = pidx - j * sx;
+	const bool inner = i >= 3 && i + 3 < sx && (D == 2 || (j >= 3 && j + 3 < sy));
 	const T *col = in + pidx;
 	const T k6 = g.inv * T(1.0 / 6.0);
 	// window v[t] = φ at w - 3 + t (clamped)
@@ -379,14 +386,19 @@ __global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__rest
 		const Ratio<T> pW = leftRole(fw, stencil1(E5, E4, E3), stencil2(E4, E3, E2), stencil3(E3, E2, E1));
 		const Ratio<T> mNext = rightRole(fw, stencil1(E1, E2, E3), stencil2(E2, E3, E4), stencil3(E3, E4, E5));
 		T sum = godunovSq(neg, mW, pW);
-		// in-plane axes
+		// in-plane axes (threads 3 or more cells from the in-plane edges need no clamping)
 #pragma unroll
 		for (int a = 0; a < D - 1; a++) {
 			const int c = a == 0 ? i : j, lim = (a == 0 ? sx : sy) - 1, str = a == 0 ? 1 : sx;
-			const T *line = in + (id - int64_t(c) * str);
 			T u[7];
+			if (inner) {
 #pragma unroll
-			for (int t = 0; t < 7; t++) u[t] = ldg(line + min(max(c + t - 3, 0), lim) * str);
+				for (int t = 0; t < 7; t++) u[t] = ldg(in + id + (t - 3) * str);
+			} else {
+				const T *line = in + (id - int64_t(c) * str);
+#pragma unroll
+				for (int t = 0; t < 7; t++) u[t] = ldg(line + min(max(c + t - 3, 0), lim) * str);
+			}
 			Ratio<T> m, p;
 			wenoCell<T>(u, m, p);
 			sum += godunovSq(neg, m, p);
