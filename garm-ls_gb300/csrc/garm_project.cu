@@ -3,9 +3,10 @@
 //                                                   x-fastest numbering as the serial loop
 //   buildLinearSystem    (Projector.cpp:30-68)    → matrix-free rows: diag, 2D neighbour ids/weights, rhs
 //   solveLinearSystem    (Projector.cpp:158-163, LinearSystem.h:23-39)
-//                        → one persistent cooperative Jacobi-PCG launch with FP64 dot products
-//                          reduced in a fixed order (deterministic), two grid barriers per
-//                          iteration; mixed mode wraps FP32 inner sweeps in FP64 iterative refinement
+//                        → one persistent cooperative Jacobi-PCG launch (Chronopoulos–Gear form)
+//                          with dot products reduced in a fixed order (deterministic): FP64 in two
+//                          phases and two grid barriers per iteration; mixed as one fused FP32
+//                          phase per iteration with FP64 residual replacement
 //   applyPressureGradient (Projector.cpp:91-123)
 #include "garm_internal.h"
 

@@ -40,8 +40,9 @@ typedef enum garm_status {
 
 typedef enum garm_precision {
     GARM_PRECISION_FP64 = 0,  /* plain form: every stage in FP64, as the reference */
-    GARM_PRECISION_MIXED = 1  /* FP32 storage+math for advection/Hermite/WENO/matvec; FP64 dots,
-                                 residuals, iterative refinement and the reference-map test */
+    GARM_PRECISION_MIXED = 1  /* FP32 storage+math for advection/Hermite/WENO/matvec; FP64-class dot
+                                 products, FP64 true residuals (residual replacement) and the
+                                 reference-map test in FP64 */
 } garm_precision;
 
 /* Field ids for upload/download.  Byte sizes follow the reference's .sav layout. */
