@@ -362,21 +362,27 @@ garm_status advectFields(State &s) {
 	return GARM_OK;
 }
 
-// Cached mixed derivatives of φ0 (HermiteIntrpl ctor via _refLevelSetView.reset()).
 template <int D, typename T>
-garm_status resetRefView(State &s) {
+garm_status scalarMixed(State &s, T *const *grad, T *const *mixed) {
 	Planes<D, T> pg{};
-	for (int a = 0; a < D; a++) pg.p[a] = (const T *)s.refGrad[a];
+	for (int a = 0; a < D; a++) pg.p[a] = grad[a];
 	OutPlanes<D, T> mo{};
-	for (int q = 0; q < 4; q++) mo.p[q] = (T *)s.refMixed[q];
+	for (int q = 0; q < (D == 3 ? 4 : 1); q++) mo.p[q] = mixed[q];
 	kMixedVec<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, pg, mo, 1, s.gate); s.launches++;
 	GARM_CHECK_LAUNCH();
 	return GARM_OK;
 }
 
+// Cached mixed derivatives of φ0 (HermiteIntrpl ctor via _refLevelSetView.reset()).
+template <int D, typename T>
+garm_status resetRefView(State &s) {
+	return scalarMixed<D, T>(s, (T *const *)s.refGrad, (T *const *)s.refMixed);
+}
+
 #define GARM_INST(D, T) \
 	template garm_status advectFields<D, T>(State &); \
-	template garm_status resetRefView<D, T>(State &);
+	template garm_status resetRefView<D, T>(State &); \
+	template garm_status scalarMixed<D, T>(State &, T *const *, T *const *);
 GARM_INST(2, double)
 GARM_INST(3, double)
 GARM_INST(2, float)

@@ -106,6 +106,17 @@ garm_status allocState(State &s) {
 	GARM_TRY(dalloc(s, &s.ref, N * e));
 	GARM_TRY(dalloc(s, &s.rA, N * e));
 	GARM_TRY(dalloc(s, &s.rB, N * e));
+	if (s.cfg.restart_newton) {
+		for (int a = 0; a < D; a++) {
+			GARM_TRY(dalloc(s, &s.lsGrad[a], N * e));
+			GARM_TRY(dalloc(s, &s.hnGrad[a], N * e));
+			GARM_TRY(dalloc(s, &s.hnPoints[a], N * e));
+		}
+		for (int m = 0; m < nm; m++) GARM_TRY(dalloc(s, &s.hnMixed[m], N * e));
+		GARM_TRY(dalloc(s, &s.hnPhi, N * e));
+		GARM_TRY(dalloc(s, (void **)&s.hnMark[0], N));
+		GARM_TRY(dalloc(s, (void **)&s.hnMark[1], N));
+	}
 	GARM_TRY(dalloc(s, &s.cellDist, N * e));
 	GARM_TRY(dalloc(s, &s.nodeDist, size_t(s.NN) * 8));
 	GARM_TRY(dalloc(s, &s.adv, N));
@@ -175,6 +186,7 @@ size_t fieldBytes(const State &s, int field) {
 	case GARM_FIELD_LEVEL_SET: case GARM_FIELD_REF_LEVEL_SET: case GARM_FIELD_ORI_LEVEL_SET: case GARM_FIELD_TMP_LEVEL_SET:
 	case GARM_FIELD_CELL_DIST: case GARM_FIELD_PRESSURE: return N * 8;
 	case GARM_FIELD_REF_MAP: case GARM_FIELD_REF_LEVEL_SET_GRAD: return N * 8 * D;
+	case GARM_FIELD_LEVEL_SET_GRAD: return s.cfg.restart_newton ? N * 8 * D : 0;
 	case GARM_FIELD_REF_MAP_GRAD: return N * 8 * D * D;
 	case GARM_FIELD_ADV_REGION: return N;
 	case GARM_FIELD_NODE_DIST: return size_t(s.NN) * 8;
@@ -247,6 +259,7 @@ garm_status upload(State &s, int field, const void *host, size_t bytes) {
 	if (field == GARM_FIELD_REF_MAP) { for (int c = 0; c < s.dim; c++) pl[c] = s.xi[c]; nc = s.dim; }
 	else if (field == GARM_FIELD_REF_MAP_GRAD) { for (int c = 0; c < s.dim * s.dim; c++) pl[c] = s.Pi[c]; nc = s.dim * s.dim; }
 	else if (field == GARM_FIELD_REF_LEVEL_SET_GRAD) { for (int c = 0; c < s.dim; c++) pl[c] = s.refGrad[c]; nc = s.dim; }
+	else if (field == GARM_FIELD_LEVEL_SET_GRAD) { for (int c = 0; c < s.dim; c++) pl[c] = s.lsGrad[c]; nc = s.dim; }
 	else return GARM_INVALID;
 	GARM_TRY(s.mixed ? toDevicePlanes<float>(s, src, pl, nc, s.N) : toDevicePlanes<double>(s, src, pl, nc, s.N));
 	if (field == GARM_FIELD_REF_LEVEL_SET_GRAD) GARM_TRY(GARM_DISPATCH(s, resetRefView, s));  // the view is reset after a load (LevelSetLiquid.cpp:511)
@@ -282,6 +295,7 @@ garm_status download(State &s, int field, void *host, size_t bytes) {
 			if (field == GARM_FIELD_REF_MAP) { for (int c = 0; c < s.dim; c++) pl[c] = s.xi[c]; nc = s.dim; }
 			else if (field == GARM_FIELD_REF_MAP_GRAD) { for (int c = 0; c < s.dim * s.dim; c++) pl[c] = s.Pi[c]; nc = s.dim * s.dim; }
 			else if (field == GARM_FIELD_REF_LEVEL_SET_GRAD) { for (int c = 0; c < s.dim; c++) pl[c] = s.refGrad[c]; nc = s.dim; }
+			else if (field == GARM_FIELD_LEVEL_SET_GRAD) { for (int c = 0; c < s.dim; c++) pl[c] = s.lsGrad[c]; nc = s.dim; }
 			else return GARM_INVALID;
 			GARM_TRY(s.mixed ? fromDevicePlanes<float>(s, dst, pl, nc, s.N) : fromDevicePlanes<double>(s, dst, pl, nc, s.N));
 		}
@@ -295,10 +309,13 @@ garm_status initialize(State &s) {
 	dropGraphs(s);  // boundary work lists are baked into captured steps
 	GARM_TRY(GARM_DISPATCH(s, finishBoundary, s));                       // _boundary.finish
 	GARM_TRY(GARM_DISPATCH(s, enforceBoundaryLevelSet, s, s.phi, 0.0));  // enforceBoundaryLevelSet(_levelSet)
+	if (s.cfg.restart_newton) GARM_TRY(GARM_DISPATCH(s, levelSetGradient, s));  // computeFirst<4>(_levelSet, _levelSetGrad)
 	GARM_TRY(GARM_DISPATCH(s, reinitialize, s));                         // reinitializeLevelSet
 	GARM_TRY(GARM_DISPATCH(s, copyField, s, s.tmp, s.phi, s.N));         // _tmpLevelSet = _levelSet
 	GARM_TRY(GARM_DISPATCH(s, copyField, s, s.ref, s.phi, s.N));         // _refLevelSet = _levelSet
 	GARM_TRY(GARM_DISPATCH(s, copyField, s, s.ori, s.phi, s.N));         // _oriLevelSet = _levelSet
+	if (s.cfg.restart_newton)                                            // _refLevelSetGrad = _levelSetGrad
+		for (int a = 0; a < s.dim; a++) GARM_TRY(GARM_DISPATCH(s, copyField, s, s.refGrad[a], s.lsGrad[a], s.N));
 	GARM_TRY(GARM_DISPATCH(s, resetRefView, s));                         // _refLevelSetView.reset()
 	GARM_TRY(GARM_DISPATCH(s, initRefMap, s));                           // ξ = x, advRegion = 1, Π = I
 	garm_step_stats st{};
@@ -558,6 +575,7 @@ garm_status garm_config_default(garm_config *c) {
 	c->mixed_replace_interval = 0;
 	c->cg_cells_per_block = 0;
 	c->record_volume = 0;
+	c->restart_newton = 0;
 	return GARM_OK;
 }
 
@@ -602,6 +620,7 @@ garm_status garm_sim_create(const garm_grid_desc *gd, const garm_config *cfg, vo
 	if (c.precision != GARM_PRECISION_FP64 && c.precision != GARM_PRECISION_MIXED) return GARM_INVALID;
 	if (c.reinit_iters < 0 || c.cg_max_iters < 0 || !(c.cg_tolerance > 0) || c.cg_cells_per_block < 0) return GARM_INVALID;
 	if (c.record_volume != 0 && c.record_volume != 1) return GARM_INVALID;
+	if (c.restart_newton != 0 && c.restart_newton != 1) return GARM_INVALID;
 
 	garm_sim *sim = new (std::nothrow) garm_sim();
 	if (!sim) return GARM_OOM;
@@ -701,7 +720,10 @@ garm_status garm_sim_finish_load(garm_sim *sim) {
 	State &s = sim->s;
 	dropGraphs(s);
 	GARM_TRY(GARM_DISPATCH(s, finishBoundary, s));
-	GARM_TRY(GARM_DISPATCH(s, refreshRefGradient, s));
+	// ψ0 is loaded with the frame in the Newton configuration, recomputed otherwise
+	// (LevelSetLiquid.cpp:500-510)
+	if (s.cfg.restart_newton) GARM_TRY(GARM_DISPATCH(s, resetRefView, s));
+	else GARM_TRY(GARM_DISPATCH(s, refreshRefGradient, s));
 	return sync(s);
 }
 

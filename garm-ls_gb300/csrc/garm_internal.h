@@ -42,6 +42,11 @@ struct State {
 	void *refGrad[3] = {};     // ψ0 = ∇φ0 (_refLevelSetGrad)
 	void *refMixed[4] = {};    // cached Hermite mixed derivatives of φ0 (_refLevelSetView)
 	void *rA = nullptr, *rB = nullptr;  // reinitialisation RK stages
+	// Newton configuration only (cfg.restart_newton): ∇φ of the composed level set
+	// (_levelSetGrad) and the HybridNewton work buffers
+	void *lsGrad[3] = {};
+	void *hnPhi = nullptr, *hnGrad[3] = {}, *hnMixed[4] = {}, *hnPoints[3] = {};
+	uint8_t *hnMark[2] = {};
 	uint8_t *adv = nullptr;    // _advRegion
 	uint8_t *vis0 = nullptr, *vis1 = nullptr;       // cell extrapolation masks
 	uint8_t *fvis0 = nullptr, *fvis1 = nullptr;     // face extrapolation masks (all axes, concatenated)
@@ -140,8 +145,11 @@ template <int D, typename T> garm_status extrapolateToAir(State &s);
 template <int D, typename T> garm_status enforceBoundaryConditions(State &s);
 template <int D, typename T> garm_status enforceBoundaryLevelSet(State &s, void *field, double tol);
 template <int D, typename T> garm_status resetRefView(State &s);
+// Hermite mixed derivatives of a scalar field from its gradient planes (gated by s.gate).
+template <int D, typename T> garm_status scalarMixed(State &s, T *const *grad, T *const *mixed);
 template <int D, typename T> garm_status initRefMap(State &s);
 template <int D, typename T> garm_status refreshRefGradient(State &s);
+template <int D, typename T> garm_status levelSetGradient(State &s);
 template <int D, typename T> garm_status maxSpeed(State &s, double *out);
 template <int D, typename T> garm_status maxSpeedAsync(State &s);
 __global__ void kStepDt(const unsigned long long *maxBits, double dx, double *clock, double *dt, double *stats, const unsigned long long *counter);

@@ -25,7 +25,84 @@ struct ComposeIO {
 	const uint8_t *adv;
 	const T *cellDist;
 	T *phi, *tmp, *ori;
+	const T *Pi[9];   // Newton configuration: Π (plane col*D+row) ...
+	T *lsGrad[3];     // ... and ∇φ = Πᵀ ∇H(ξ) written here (null: not kept)
 };
+
+// Scalar Hermite value and gradient at p (HermiteIntrpl::interpolate and
+// interpolateGradient, HermiteIntrpl.h:32-58), contracted one axis at a time over
+// vertex and term order.  Coefficient order o: bit 0 d/dx, bit 1 d/dy, bit 2 d/dz.
+template <int D, typename T>
+__device__ __forceinline__ void hermiteValueGrad(const G<D, T> &g, const T *p, const T *f, const T *const *grad, const T *const *mixed,
+                                                 T &val, T *gout) {
+	int lo[3] = {0, 0, 0};
+	T B[3][2][2], Dd[3][2][2];
+#pragma unroll
+	for (int a = 0; a < D; a++) {
+		lo[a] = g.lower(a, p[a]);
+		hermiteBasis<T>(g.frac(a, p[a], lo[a]), g.dx, B[a], Dd[a]);
+	}
+	auto coefOf = [&](int64_t n, int o) -> T {
+		switch (o) {
+		case 0: return ldg(f + n);
+		case 1: return ldg(grad[0] + n);
+		case 2: return ldg(grad[1] + n);
+		case 3: return ldg(mixed[0] + n);
+		case 4: return ldg(grad[2] + n);
+		case 5: return ldg(mixed[1] + n);
+		case 6: return ldg(mixed[2] + n);
+		default: return ldg(mixed[3] + n);
+		}
+	};
+	if (D == 2) {
+		T v = T(0), gx = T(0), gy = T(0);
+#pragma unroll
+		for (int vy = 0; vy < 2; vy++) {
+			const int64_t n0 = g.cidx(lo[0], lo[1] + vy, 0), n1 = g.cidx(lo[0] + 1, lo[1] + vy, 0);
+#pragma unroll
+			for (int oy = 0; oy < 2; oy++) {
+				const T a0 = coefOf(n0, oy << 1), a1 = coefOf(n0, oy << 1 | 1), b0 = coefOf(n1, oy << 1), b1 = coefOf(n1, oy << 1 | 1);
+				const T x0 = fma(a0, B[0][0][0], fma(a1, B[0][0][1], fma(b0, B[0][1][0], b1 * B[0][1][1])));
+				const T x1 = fma(a0, Dd[0][0][0], fma(a1, Dd[0][0][1], fma(b0, Dd[0][1][0], b1 * Dd[0][1][1])));
+				v = fma(x0, B[1][vy][oy], v);
+				gx = fma(x1, B[1][vy][oy], gx);
+				gy = fma(x0, Dd[1][vy][oy], gy);
+			}
+		}
+		val = v; gout[0] = gx * g.inv; gout[1] = gy * g.inv;
+	} else {
+		T Y0[2][2] = {}, Yx[2][2] = {}, Yy[2][2] = {};
+#pragma unroll
+		for (int vz = 0; vz < 2; vz++)
+#pragma unroll
+			for (int vy = 0; vy < 2; vy++) {
+				const int64_t n0 = g.cidx(lo[0], lo[1] + vy, lo[2] + vz), n1 = g.cidx(lo[0] + 1, lo[1] + vy, lo[2] + vz);
+#pragma unroll
+				for (int oz = 0; oz < 2; oz++)
+#pragma unroll
+					for (int oy = 0; oy < 2; oy++) {
+						const int o = oz << 2 | oy << 1;
+						const T a0 = coefOf(n0, o), a1 = coefOf(n0, o | 1), b0 = coefOf(n1, o), b1 = coefOf(n1, o | 1);
+						const T x0 = fma(a0, B[0][0][0], fma(a1, B[0][0][1], fma(b0, B[0][1][0], b1 * B[0][1][1])));
+						const T x1 = fma(a0, Dd[0][0][0], fma(a1, Dd[0][0][1], fma(b0, Dd[0][1][0], b1 * Dd[0][1][1])));
+						Y0[vz][oz] = fma(x0, B[1][vy][oy], Y0[vz][oz]);
+						Yx[vz][oz] = fma(x1, B[1][vy][oy], Yx[vz][oz]);
+						Yy[vz][oz] = fma(x0, Dd[1][vy][oy], Yy[vz][oz]);
+					}
+			}
+		T v = T(0), gx = T(0), gy = T(0), gz = T(0);
+#pragma unroll
+		for (int vz = 0; vz < 2; vz++)
+#pragma unroll
+			for (int oz = 0; oz < 2; oz++) {
+				v = fma(Y0[vz][oz], B[2][vz][oz], v);
+				gx = fma(Yx[vz][oz], B[2][vz][oz], gx);
+				gy = fma(Yy[vz][oz], B[2][vz][oz], gy);
+				gz = fma(Y0[vz][oz], Dd[2][vz][oz], gz);
+			}
+		val = v; gout[0] = gx * g.inv; gout[1] = gy * g.inv; gout[2] = gz * g.inv;
+	}
+}
 
 // Scalar Hermite value at p (HermiteIntrpl::interpolate, HermiteIntrpl.h:32-41).
 template <int D, typename T>
@@ -68,7 +145,21 @@ __global__ void __launch_bounds__(kBlock) kCompose(Geom geom, ComposeIO<D, T> io
 	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
 	if (id >= g.count()) return;
 	T p[3] = {io.xi[0][id], io.xi[1][id], D == 3 ? io.xi[2][id] : T(0)};
-	T phi = hermiteScalar<D, T>(g, p, io.ref, io.refGrad, io.refMixed);
+	T phi;
+	if (io.lsGrad[0]) {
+		// Newton configuration: _levelSetGrad = Πᵀ ∇H(ξ) (LevelSetLiquid.cpp:1226-1227), before the clamps
+		T gr[3] = {T(0), T(0), T(0)};
+		hermiteValueGrad<D, T>(g, p, io.ref, io.refGrad, io.refMixed, phi, gr);
+#pragma unroll
+		for (int a = 0; a < D; a++) {
+			T s = T(0);
+#pragma unroll
+			for (int r = 0; r < D; r++) s = fma(io.Pi[a * D + r][id], gr[r], s);
+			io.lsGrad[a][id] = s;
+		}
+	} else {
+		phi = hermiteScalar<D, T>(g, p, io.ref, io.refGrad, io.refMixed);
+	}
 	if (io.adv[id] == 0 && phi < airClamp) phi = airClamp;
 	const T cd = io.cellDist[id];
 	if (phi < -cd - solidTol) phi = -cd - solidTol;  // enforceBoundaryLevelSet(φ, 3dx)
@@ -88,6 +179,10 @@ garm_status generateCurrentFields(State &s) {
 	io.adv = s.adv;
 	io.cellDist = (const T *)s.cellDist;
 	io.phi = (T *)s.phi; io.tmp = (T *)s.tmp; io.ori = (T *)s.ori;
+	if (s.cfg.restart_newton) {
+		for (int q = 0; q < D * D; q++) io.Pi[q] = (const T *)s.Pi[q];
+		for (int a = 0; a < D; a++) io.lsGrad[a] = (T *)s.lsGrad[a];
+	}
 	const double airClamp = s.cfg.air_extrap_radius * s.geom.dx;
 	kCompose<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, io, T(airClamp), T(3.0 * s.geom.dx), s.gate); s.launches++;
 	GARM_CHECK_LAUNCH();
@@ -802,8 +897,308 @@ __global__ void __launch_bounds__(kBlock) kRestart(Geom geom, RestartIO<D, T> io
 	for (int q = 0; q < D * D; q++) io.Pi[q][id] = (q % (D + 1) == 0) ? T(1) : T(0);
 }
 
+// ---------------------------------------------------------------------------
+// Newton configuration: restart() by HybridNewton without FMM (LevelSetLiquid.cpp:1290-1308;
+// HybridNewton.h:59-127 and 146-467, ENABLE_MODIFIED branch; HybridNewton.cpp:30-118).
+// Every kernel takes the restart gate, so the branch can sit inside a captured step.
+// ---------------------------------------------------------------------------
+template <int D, typename T>
+struct NewtonIO {
+	const T *phi;                 // the reinitialised level set (starting points)
+	T *ori, *lsGrad[3];           // HybridNewton's φ and ∇φ (in: _oriLevelSet, _levelSetGrad)
+	T *hp, *hg[3];                // second buffer of φ and ∇φ
+	T *mixed[4];                  // Hermite mixed derivatives of the current ∇φ
+	T *pts[3];                    // starting points of the closest-point search
+	uint8_t *mark0, *mark1;       // cells next to a sign change, and one more layer
+	T *ref, *refGrad[3];          // outputs: _refLevelSet, _refLevelSetGrad
+	T *xi[3], *Pi[9];             // ξ = x, Π = I
+};
+
+// Starting points p − φ(p)·∇φ(p) from _levelSetView: the cubic Lagrange value and, as
+// ScalarFieldWrapper::gradient does, the trilinear blend of the central differences at
+// the eight surrounding samples (ScalarField.h:41-47, Derivatives.h:47-57).
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kHnPoints(Geom geom, NewtonIO<D, T> io, const int *gate) {
+	if (gate && !*gate) return;
+	const G<D, T> g = cellGrid<D, T>(geom);
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= g.count()) return;
+	int ci, cj, ck;
+	g.coord(id, ci, cj, ck);
+	const T pos[3] = {g.pos(0, ci), g.pos(1, cj), D == 3 ? g.pos(2, ck) : T(0)};
+	const T *f = io.phi;
+	// cubic value (CubicIntrpl, LagrangeIntrpl.h:137-170)
+	int cl[3] = {0, 0, 0};
+	T w[3][4];
+	const T sixth = T(1.0 / 6.0);
+#pragma unroll
+	for (int a = 0; a < D; a++) {
+		cl[a] = g.lower(a, pos[a]) - 1;
+		const T x = g.frac(a, pos[a], cl[a]);
+		const T x1 = x - T(1), x2 = x - T(2), x3 = x - T(3);
+		w[a][0] = -(x1 * x2 * x3) * sixth;
+		w[a][1] = x * x2 * x3 * T(0.5);
+		w[a][2] = -(x * x1 * x3) * T(0.5);
+		w[a][3] = x * x1 * x2 * sixth;
+	}
+	T v = T(0);
+	for (int c = 0; c < (D == 3 ? 4 : 1); c++) {
+		T sy = T(0);
+		for (int b = 0; b < 4; b++) {
+			T sx = T(0);
+#pragma unroll
+			for (int a = 0; a < 4; a++) sx += ldg(f + g.cidx(cl[0] + a, cl[1] + b, D == 3 ? cl[2] + c : 0)) * w[0][a];
+			sy += sx * w[1][b];
+		}
+		v += D == 3 ? sy * w[2][c] : sy;
+	}
+	// trilinear blend of central differences
+	int ll[3] = {0, 0, 0};
+	T fr[3] = {T(0), T(0), T(0)};
+#pragma unroll
+	for (int a = 0; a < D; a++) { ll[a] = g.lower(a, pos[a]); fr[a] = g.frac(a, pos[a], ll[a]); }
+	T gr[3] = {T(0), T(0), T(0)};
+	const T h = T(0.5) * g.inv;
+	for (int q = 0; q < (1 << D); q++) {
+		const int n[3] = {ll[0] + (q & 1), ll[1] + (q >> 1 & 1), D == 3 ? ll[2] + (q >> 2 & 1) : 0};
+		T wt = T(1);
+#pragma unroll
+		for (int a = 0; a < D; a++) wt *= ((q >> a) & 1) ? fr[a] : T(1) - fr[a];
+#pragma unroll
+		for (int a = 0; a < D; a++) {
+			const int ex = a == 0, ey = a == 1, ez = a == 2;
+			const T d = (ldg(f + g.cidx(n[0] + ex, n[1] + ey, n[2] + ez)) - ldg(f + g.cidx(n[0] - ex, n[1] - ey, n[2] - ez))) * h;
+			gr[a] += d * wt;
+		}
+	}
+#pragma unroll
+	for (int a = 0; a < D; a++) io.pts[a][id] = pos[a] - v * gr[a];
+}
+
+// prepareInterface (HybridNewton.cpp:59-75): cells with a sign change (φ·φ_nb <= 0) to a neighbour.
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kHnMark(Geom geom, const T *phi, uint8_t *mark, const int *gate) {
+	if (gate && !*gate) return;
+	const G<D, T> g = cellGrid<D, T>(geom);
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= g.count()) return;
+	int i, j, k;
+	g.coord(id, i, j, k);
+	const T f = phi[id];
+	uint8_t m = 0;
+	for (int nb = 0; nb < 2 * D && !m; nb++) {
+		const int a = nb >> 1, s = (nb & 1) ? 1 : -1;
+		const int ni = i + (a == 0 ? s : 0), nj = j + (a == 1 ? s : 0), nk = k + (a == 2 ? s : 0);
+		if (g.valid(ni, nj, nk) && f * phi[g.idx(ni, nj, nk)] <= T(0)) m = 1;
+	}
+	mark[id] = m;
+}
+
+// extrapolate(1) (HybridNewton.cpp:96-118): one more layer of marked cells.
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kHnDilate(Geom geom, const uint8_t *in, uint8_t *out, const int *gate) {
+	if (gate && !*gate) return;
+	const G<D, T> g = cellGrid<D, T>(geom);
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= g.count()) return;
+	int i, j, k;
+	g.coord(id, i, j, k);
+	uint8_t m = in[id];
+	for (int nb = 0; nb < 2 * D && !m; nb++) {
+		const int a = nb >> 1, s = (nb & 1) ? 1 : -1;
+		const int ni = i + (a == 0 ? s : 0), nj = j + (a == 1 ? s : 0), nk = k + (a == 2 ? s : 0);
+		if (g.valid(ni, nj, nk) && in[g.idx(ni, nj, nk)]) m = 1;
+	}
+	out[id] = m;
+}
+
+// v/|v|, or (for the velocity of the eikonal trace) the x unit vector when v = 0;
+// normalized() of a zero vector is the zero vector.
+template <int D, typename T>
+__device__ __forceinline__ void normalizeOr(T *v, bool unitIfZero) {
+	T n2 = T(0);
+#pragma unroll
+	for (int a = 0; a < D; a++) n2 = fma(v[a], v[a], n2);
+	if (n2 > T(0)) {
+		const T n = sqrt(n2);
+#pragma unroll
+		for (int a = 0; a < D; a++) v[a] = v[a] / n;
+	} else if (unitIfZero) {
+		v[0] = T(1);
+	}
+}
+
+// initializeInterface with the given starting points (HybridNewton.h:102-127): on marked
+// cells the modified Newton closest point (HybridNewton.h:146-467): 20 steps of
+// delta = -φ ψ/|ψ|² + (s - x) - ψ ((s - x)·ψ)/|ψ|², each at most 0.9 dx long, stopping
+// after a step shorter than 1e-3 dx² (2D) or 1e-3 dx³ (3D); φ = ±|s - x|, ψ = ∇H(x)/|∇H(x)|.
+// Unmarked cells are copied.
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kHnInterface(Geom geom, NewtonIO<D, T> io, const int *gate) {
+	if (gate && !*gate) return;
+	const G<D, T> g = cellGrid<D, T>(geom);
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= g.count()) return;
+	const T f = io.ori[id];
+	if (!io.mark1[id]) {
+		io.hp[id] = f;
+#pragma unroll
+		for (int a = 0; a < D; a++) io.hg[a][id] = io.lsGrad[a][id];
+		return;
+	}
+	int ci, cj, ck;
+	g.coord(id, ci, cj, ck);
+	const T start[3] = {g.pos(0, ci), g.pos(1, cj), D == 3 ? g.pos(2, ck) : T(0)};
+	T pos[3] = {io.pts[0][id], io.pts[1][id], D == 3 ? io.pts[2][id] : T(0)};
+	const T dx = g.dx;
+	const T tolerance = T(1e-3) * dx * dx * (D == 2 ? T(1) : dx);
+	const T radius = T(0.9) * dx;
+	const T *const grad[3] = {io.lsGrad[0], io.lsGrad[1], io.lsGrad[2]};
+	const T *const mixed[4] = {io.mixed[0], io.mixed[1], io.mixed[2], io.mixed[3]};
+	for (int iter = 0; iter < 20; iter++) {
+		T phiv, psi[3] = {T(0), T(0), T(0)};
+		hermiteValueGrad<D, T>(g, pos, io.ori, grad, mixed, phiv, psi);
+		T s2 = T(0), dot = T(0);
+#pragma unroll
+		for (int a = 0; a < D; a++) { s2 = fma(psi[a], psi[a], s2); dot = fma(start[a] - pos[a], psi[a], dot); }
+		T delta[3], n2 = T(0);
+#pragma unroll
+		for (int a = 0; a < D; a++) {
+			delta[a] = -phiv * psi[a] / s2 + ((start[a] - pos[a]) - psi[a] * dot / s2);
+			n2 = fma(delta[a], delta[a], n2);
+		}
+		T norm = sqrt(n2);
+		if (norm > radius) {
+#pragma unroll
+			for (int a = 0; a < D; a++) delta[a] *= radius / norm;
+			norm = radius;
+		}
+#pragma unroll
+		for (int a = 0; a < D; a++) pos[a] += delta[a];
+		if (norm < tolerance) break;
+	}
+	T d2 = T(0);
+#pragma unroll
+	for (int a = 0; a < D; a++) d2 = fma(start[a] - pos[a], start[a] - pos[a], d2);
+	io.hp[id] = sqrt(d2) * (f < T(0) ? T(-1) : T(1));
+	T v, gr[3] = {T(0), T(0), T(0)};
+	hermiteValueGrad<D, T>(g, pos, io.ori, grad, mixed, v, gr);
+	normalizeOr<D, T>(gr, false);
+#pragma unroll
+	for (int a = 0; a < D; a++) io.hg[a][id] = gr[a];
+}
+
+// One step of HybridNewton::advect (HybridNewton.cpp:30-48) on unmarked cells: a TVD-RK3
+// trace (Advection.h:44-49) along the normalised ∇H for -sgn·dt, then φ = H(x) + sgn·dt,
+// ψ = ∇H(x)/|∇H(x)|.  Marked cells are copied.
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kHnAdvect(Geom geom, const T *fin, const T *g0, const T *g1, const T *g2, NewtonIO<D, T> io,
+                                                    T *fout, T *o0, T *o1, T *o2, T dt, const int *gate) {
+	if (gate && !*gate) return;
+	const G<D, T> g = cellGrid<D, T>(geom);
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= g.count()) return;
+	const T *const grad[3] = {g0, g1, g2};
+	T *const gout[3] = {o0, o1, o2};
+	const T f = fin[id];
+	if (io.mark1[id]) {
+		fout[id] = f;
+#pragma unroll
+		for (int a = 0; a < D; a++) gout[a][id] = grad[a][id];
+		return;
+	}
+	const T *const mixed[4] = {io.mixed[0], io.mixed[1], io.mixed[2], io.mixed[3]};
+	int ci, cj, ck;
+	g.coord(id, ci, cj, ck);
+	const T pos[3] = {g.pos(0, ci), g.pos(1, cj), D == 3 ? g.pos(2, ck) : T(0)};
+	const T sgn = f < T(0) ? T(-1) : T(1);
+	const T h = -sgn * dt;
+	auto vel = [&](const T *p, T *out) {
+		T v;
+		out[0] = out[1] = out[2] = T(0);
+		hermiteValueGrad<D, T>(g, p, fin, grad, mixed, v, out);
+		normalizeOr<D, T>(out, true);
+	};
+	T v0[3], v1[3], v2[3], p1[3] = {T(0), T(0), T(0)}, p2[3] = {T(0), T(0), T(0)}, tp[3] = {T(0), T(0), T(0)};
+	vel(pos, v0);
+#pragma unroll
+	for (int a = 0; a < D; a++) p1[a] = pos[a] + v0[a] * h;
+	vel(p1, v1);
+#pragma unroll
+	for (int a = 0; a < D; a++) p2[a] = pos[a] + (v0[a] + v1[a]) * h / T(4);
+	vel(p2, v2);
+#pragma unroll
+	for (int a = 0; a < D; a++) tp[a] = pos[a] + (v0[a] + v1[a] + T(4) * v2[a]) * h / T(6);
+	T val, gr[3] = {T(0), T(0), T(0)};
+	hermiteValueGrad<D, T>(g, tp, fin, grad, mixed, val, gr);
+	fout[id] = val + sgn * dt;
+	normalizeOr<D, T>(gr, false);
+#pragma unroll
+	for (int a = 0; a < D; a++) gout[a][id] = gr[a];
+}
+
+// The result into _oriLevelSet/_levelSetGrad and _refLevelSet/_refLevelSetGrad; ξ = x, Π = I.
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kHnFinish(Geom geom, NewtonIO<D, T> io, const int *gate) {
+	if (gate && !*gate) return;
+	const G<D, T> g = cellGrid<D, T>(geom);
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= g.count()) return;
+	int i, j, k;
+	g.coord(id, i, j, k);
+	const T f = io.hp[id];
+	io.ori[id] = f;
+	io.ref[id] = f;
+#pragma unroll
+	for (int a = 0; a < D; a++) { const T v = io.hg[a][id]; io.lsGrad[a][id] = v; io.refGrad[a][id] = v; }
+	io.xi[0][id] = g.pos(0, i);
+	io.xi[1][id] = g.pos(1, j);
+	if (D == 3) io.xi[2][id] = g.pos(2, k);
+#pragma unroll
+	for (int q = 0; q < D * D; q++) io.Pi[q][id] = (q % (D + 1) == 0) ? T(1) : T(0);
+}
+
+template <int D, typename T>
+static garm_status newtonRestart(State &s) {
+	NewtonIO<D, T> io{};
+	io.phi = (const T *)s.phi;
+	io.ori = (T *)s.ori; io.hp = (T *)s.hnPhi; io.ref = (T *)s.ref;
+	for (int a = 0; a < D; a++) {
+		io.lsGrad[a] = (T *)s.lsGrad[a]; io.hg[a] = (T *)s.hnGrad[a]; io.pts[a] = (T *)s.hnPoints[a];
+		io.refGrad[a] = (T *)s.refGrad[a]; io.xi[a] = (T *)s.xi[a];
+	}
+	for (int q = 0; q < 4; q++) io.mixed[q] = (T *)s.hnMixed[q];
+	for (int q = 0; q < D * D; q++) io.Pi[q] = (T *)s.Pi[q];
+	io.mark0 = s.hnMark[0]; io.mark1 = s.hnMark[1];
+	const unsigned nb = gridFor(s.N);
+	kHnPoints<D, T><<<nb, kBlock, 0, s.stream>>>(s.geom, io, s.gate); s.launches++;
+	kHnMark<D, T><<<nb, kBlock, 0, s.stream>>>(s.geom, io.ori, io.mark0, s.gate); s.launches++;
+	kHnDilate<D, T><<<nb, kBlock, 0, s.stream>>>(s.geom, io.mark0, io.mark1, s.gate); s.launches++;
+	GARM_CHECK_LAUNCH();
+	GARM_TRY((scalarMixed<D, T>(s, io.lsGrad, io.mixed)));
+	kHnInterface<D, T><<<nb, kBlock, 0, s.stream>>>(s.geom, io, s.gate); s.launches++;
+	GARM_CHECK_LAUNCH();
+	// advect, maxSteps 20, cfl 0.9 (LevelSetLiquid.cpp:1301): the buffers alternate, so after
+	// an even number of steps the result is back in (hp, hg)
+	const T dt = T(s.geom.dx * 0.9);
+	for (int it = 0; it < 20; it++) {
+		const bool fromH = (it & 1) == 0;
+		T *fin = fromH ? io.hp : io.ori, *fout = fromH ? io.ori : io.hp;
+		T *const *gin = fromH ? io.hg : io.lsGrad;
+		T *const *gout = fromH ? io.lsGrad : io.hg;
+		GARM_TRY((scalarMixed<D, T>(s, gin, io.mixed)));
+		kHnAdvect<D, T><<<nb, kBlock, 0, s.stream>>>(s.geom, fin, gin[0], gin[1], D == 3 ? gin[2] : gin[0], io, fout, gout[0], gout[1],
+		                                             D == 3 ? gout[2] : gout[0], dt, s.gate); s.launches++;
+		GARM_CHECK_LAUNCH();
+	}
+	kHnFinish<D, T><<<nb, kBlock, 0, s.stream>>>(s.geom, io, s.gate); s.launches++;
+	GARM_CHECK_LAUNCH();
+	return resetRefView<D, T>(s);
+}
+
 template <int D, typename T>
 garm_status restart(State &s) {
+	if (s.cfg.restart_newton) return newtonRestart<D, T>(s);
 	RestartIO<D, T> io{};
 	io.phi = (const T *)s.phi;
 	io.ref = (T *)s.ref;
@@ -833,6 +1228,14 @@ __global__ void __launch_bounds__(kBlock) kRefGrad4(Geom geom, const T *ref, T *
 		const T v4 = ldg(ref + g.cidx(i + 2 * ex, j + 2 * ey, k + 2 * ez));
 		out[a][id] = (v0 - T(8) * v1 + T(8) * v3 - v4) * h;
 	}
+}
+
+// ∇φ of the level set, computeFirst<4>(_levelSet, _levelSetGrad) (LevelSetLiquid.cpp:546-548)
+template <int D, typename T>
+garm_status levelSetGradient(State &s) {
+	kRefGrad4<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, (const T *)s.phi, (T *)s.lsGrad[0], (T *)s.lsGrad[1], (T *)(D == 3 ? s.lsGrad[2] : nullptr)); s.launches++;
+	GARM_CHECK_LAUNCH();
+	return GARM_OK;
 }
 
 template <int D, typename T>
@@ -896,6 +1299,7 @@ garm_status enforceBoundaryLevelSet(State &s, void *field, double tol) {
 	template garm_status restart<D, T>(State &); \
 	template garm_status initRefMap<D, T>(State &); \
 	template garm_status refreshRefGradient<D, T>(State &); \
+	template garm_status levelSetGradient<D, T>(State &); \
 	template garm_status enforceBoundaryLevelSet<D, T>(State &, void *, double);
 GARM_INST(2, double)
 GARM_INST(3, double)

@@ -25,13 +25,13 @@ REINIT_FORMS = ["cells", "columns", "sweeps"]  # GARM_REINIT_CELLS, _COLUMNS, _S
 # garm_field
 (FIELD_VELOCITY, FIELD_LEVEL_SET, FIELD_REF_MAP, FIELD_REF_MAP_GRAD, FIELD_REF_LEVEL_SET, FIELD_REF_LEVEL_SET_GRAD,
  FIELD_ADV_REGION, FIELD_ORI_LEVEL_SET, FIELD_TMP_LEVEL_SET, FIELD_CELL_DIST, FIELD_NODE_DIST, FIELD_FRACTION,
- FIELD_BOUNDARY_VELOCITY, FIELD_BOUNDARY_NORMAL, FIELD_PRESSURE) = range(15)
+ FIELD_BOUNDARY_VELOCITY, FIELD_BOUNDARY_NORMAL, FIELD_PRESSURE, FIELD_LEVEL_SET_GRAD) = range(16)
 FIELD_NAMES = {
     FIELD_VELOCITY: "velocity", FIELD_LEVEL_SET: "levelSet", FIELD_REF_MAP: "refMap", FIELD_REF_MAP_GRAD: "refMapGrad",
     FIELD_REF_LEVEL_SET: "refLevelSet", FIELD_REF_LEVEL_SET_GRAD: "refLevelSetGrad", FIELD_ADV_REGION: "advRegion",
     FIELD_ORI_LEVEL_SET: "oriLevelSet", FIELD_TMP_LEVEL_SET: "tmpLevelSet", FIELD_CELL_DIST: "cellDist",
     FIELD_NODE_DIST: "nodeDist", FIELD_FRACTION: "fraction", FIELD_BOUNDARY_VELOCITY: "boundaryVelocity",
-    FIELD_BOUNDARY_NORMAL: "boundaryNormal", FIELD_PRESSURE: "pressure",
+    FIELD_BOUNDARY_NORMAL: "boundaryNormal", FIELD_PRESSURE: "pressure", FIELD_LEVEL_SET_GRAD: "levelSetGrad",
 }
 
 
@@ -52,7 +52,7 @@ class Config(C.Structure):
                 ("boundary_extrap_radius", C.c_double), ("air_extrap_radius", C.c_double),
                 ("rm_threshold", C.c_double), ("rm_band", C.c_double), ("rm_ratio", C.c_double),
                 ("enable_gravity", C.c_int), ("mixed_residual_drop", C.c_double),
-                ("mixed_replace_interval", C.c_int), ("cg_cells_per_block", C.c_int), ("record_volume", C.c_int)]
+                ("mixed_replace_interval", C.c_int), ("cg_cells_per_block", C.c_int), ("record_volume", C.c_int), ("restart_newton", C.c_int)]
 
 
 class StepStats(C.Structure):

@@ -144,13 +144,14 @@ public:
 		writeField(frameDir + "/levelSet.bin", GARM_FIELD_TMP_LEVEL_SET);
 	}
 
-	// LevelSetLiquid::saveFrame (LevelSetLiquid.cpp:425-471), RM+GA, Newton off
+	// LevelSetLiquid::saveFrame (LevelSetLiquid.cpp:425-471), RM+GA; ψ0 too in the Newton configuration
 	void saveFrame(const std::string &frameDir) const override {
 		writeField(frameDir + "/velocity.sav", GARM_FIELD_VELOCITY);
 		writeField(frameDir + "/refMap.sav", GARM_FIELD_REF_MAP);
 		writeField(frameDir + "/refLevelSet.sav", GARM_FIELD_REF_LEVEL_SET);
 		writeField(frameDir + "/advRegion.sav", GARM_FIELD_ADV_REGION);
 		writeField(frameDir + "/refMapGrad.sav", GARM_FIELD_REF_MAP_GRAD);
+		if (_cfg.restart_newton) writeField(frameDir + "/refLevelSetGrad.sav", GARM_FIELD_REF_LEVEL_SET_GRAD);
 	}
 
 	// LevelSetLiquid::loadFrame (LevelSetLiquid.cpp:474-526)
@@ -160,6 +161,7 @@ public:
 		readField(frameDir + "/refLevelSet.sav", GARM_FIELD_REF_LEVEL_SET);
 		readField(frameDir + "/advRegion.sav", GARM_FIELD_ADV_REGION);
 		readField(frameDir + "/refMapGrad.sav", GARM_FIELD_REF_MAP_GRAD);
+		if (_cfg.restart_newton) readField(frameDir + "/refLevelSetGrad.sav", GARM_FIELD_REF_LEVEL_SET_GRAD);
 		check(garm_sim_finish_load(_sim), "garm_sim_finish_load");
 	}
 

@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define GARM_ABI_VERSION 3
+#define GARM_ABI_VERSION 4
 
 typedef enum garm_status {
     GARM_OK = 0,
@@ -62,7 +62,8 @@ typedef enum garm_field {
     GARM_FIELD_BOUNDARY_VELOCITY = 12,  /* D face arrays (Boundary::velocity)                            */
     GARM_FIELD_BOUNDARY_NORMAL = 13,    /* D face arrays (Boundary::normal)                              */
     GARM_FIELD_PRESSURE = 14,           /* cell double: last solved pressure, 0 off the unknown set      */
-    GARM_FIELD_COUNT = 15
+    GARM_FIELD_LEVEL_SET_GRAD = 15,     /* cell double[D] (_levelSetGrad; restart_newton only)           */
+    GARM_FIELD_COUNT = 16
 } garm_field;
 
 /* StaggeredGrid(boundaryWidth, spacing, resolution, center)
@@ -99,6 +100,10 @@ typedef struct garm_config {
                                          SMs free for other scenes' work when scenes run concurrently */
     int record_volume;                /* 1: every step ends with the volume diagnostic (garm_sim_volume, corner
                                          order 0) written to its statistics on the device (no host round trip) */
+    int restart_newton;               /* 1: the reference's Newton configuration (_ENABLE_NEWTON_, without FMM):
+                                         compose also keeps ∇φ = Πᵀ∇φ₀(ξ), initialize takes ψ₀ from the 4th-order
+                                         gradient of φ, and restart() is the HybridNewton closest-point restart
+                                         (LevelSetLiquid.cpp:1290-1308); 0: the plain WENO restart */
 } garm_config;
 
 /* Per-step statistics returned by garm_sim_advance. */
@@ -143,13 +148,15 @@ garm_status garm_sim_field_bytes(const garm_sim *sim, int field, size_t *bytes);
 garm_status garm_sim_upload(garm_sim *sim, int field, const void *host, size_t bytes);
 garm_status garm_sim_download(garm_sim *sim, int field, void *host, size_t bytes);
 
-/* LevelSetLiquid::initialize (Source/Core/LevelSetLiquid.cpp:528-598), RM+GA,
- * Newton/FMM off.  Expects the velocity and level set uploaded first. */
+/* LevelSetLiquid::initialize (Source/Core/LevelSetLiquid.cpp:528-598), RM+GA, FMM off;
+ * the Newton branches when restart_newton is set.  Expects the velocity and level set
+ * uploaded first. */
 garm_status garm_sim_initialize(garm_sim *sim);
 
 /* The non-I/O part of LevelSetLiquid::loadFrame (Source/Core/LevelSetLiquid.cpp:474-526),
- * to call after uploading velocity, refMap, refLevelSet, advRegion and refMapGrad:
- * Boundary::finish, ψ0 = computeFirst<4>(φ0) and the Hermite view reset. */
+ * to call after uploading velocity, refMap, refLevelSet, advRegion and refMapGrad (and, with
+ * restart_newton, refLevelSetGrad): Boundary::finish, ψ0 = computeFirst<4>(φ0) unless
+ * restart_newton is set, and the Hermite view reset. */
 garm_status garm_sim_finish_load(garm_sim *sim);
 
 /* LevelSetLiquid::advance (Source/Core/LevelSetLiquid.cpp:608-698). `stats` may be NULL. */

@@ -29,6 +29,7 @@ def host_default_config(**kw) -> capi.Config:
     c.mixed_replace_interval = 0
     c.cg_cells_per_block = 0
     c.record_volume = 0
+    c.restart_newton = 0
     for k, v in kw.items():
         setattr(c, k, v)
     return c
@@ -147,3 +148,60 @@ def band_l1(phi, truth, dx, band: float = 3.0) -> float:
     """Mean |φ - truth| over cells with |truth| <= band·dx (TestAdvect2D.cpp:236-251)."""
     m = np.abs(truth) <= band * dx
     return float(np.mean(np.abs(phi - truth)[m]))
+
+
+def newton_sphere_case(n: int, dim: int = 3, r0: float = 0.3):
+    """A level set that is not a distance function, φ = (|x-c|² - r0²)/(2 r0), with the
+    sphere (circle) of radius r0 as zero set and ∇φ = (x-c)/r0, on an n^dim grid of the
+    unit box.  Returns (grid, φ, ∇φ as per-cell vectors, exact signed distance)."""
+    dx = 1.0 / n
+    grid = capi.grid_desc(dim, [n] * dim, dx, [0.5] * dim)
+    c = np.array([0.5 + 0.13 * dx, 0.5 - 0.29 * dx, 0.5 + 0.41 * dx][:dim])
+    x = (np.arange(n) + 0.5) * dx
+    mesh = np.meshgrid(*([x] * dim), indexing="ij")          # axis a varies along mesh[a]
+    d = [np.transpose(m, tuple(reversed(range(dim)))) - c[a] for a, m in enumerate(mesh)]  # x-fastest layout
+    r2 = sum(v * v for v in d)
+    phi = (r2 - r0 * r0) / (2 * r0)
+    grad = np.stack([v.ravel() / r0 for v in d], axis=-1)
+    return grid, phi, grad, np.sqrt(r2) - r0
+
+
+def perturbed(v, rel_size: float, seed: int):
+    """v with every element scaled by 1 + rel_size·U(-1, 1): a few ulps for rel_size ~ 1e-15."""
+    v = np.asarray(v, dtype=np.float64)
+    return v * (1 + rel_size * np.random.default_rng(seed).uniform(-1, 1, v.shape))
+
+
+PERTURBATIONS = ((1e-15, 11), (2e-15, 12), (-1e-15, 13))
+
+
+def oracle_spread(run):
+    """Conditioning of an oracle computation: run(rel_size, seed) -> array, called unperturbed
+    and under PERTURBATIONS.  Returns (unperturbed result, per-element max deviation)."""
+    base = run(0.0, 0)
+    spread = np.zeros_like(base)
+    for size, seed in PERTURBATIONS:
+        spread = np.maximum(spread, np.abs(run(size, seed) - base))
+    return base, spread
+
+
+def conditioning_parity(gpu, base, spread, scale, tight: float = 1e-9) -> dict:
+    """Compare a GPU result with an oracle result whose own ulp-level sensitivity is
+    `spread`: where the oracle is stable the two must agree to tight·scale; the share of
+    such elements and the 99th percentile of the deviation are measured against the
+    oracle's own."""
+    d = np.abs(np.asarray(gpu, dtype=np.float64) - base)
+    return {
+        "agree_gpu": float(np.mean(d <= tight * scale)),
+        "agree_oracle": float(np.mean(spread <= tight * scale)),
+        "q99_gpu": float(np.quantile(d, 0.99)) / scale,
+        "q99_oracle": float(np.quantile(spread, 0.99)) / scale,
+        "max_gpu": float(d.max()) / scale,
+        "max_oracle": float(spread.max()) / scale,
+    }
+
+
+def assert_conditioning_parity(stats: dict, tight: float = 1e-9, share_slack: float = 0.03, q_factor: float = 10.0) -> None:
+    assert stats["agree_gpu"] >= stats["agree_oracle"] - share_slack, stats
+    assert stats["q99_gpu"] <= max(q_factor * stats["q99_oracle"], tight), stats
+    assert stats["max_gpu"] <= max(q_factor * stats["max_oracle"], tight), stats

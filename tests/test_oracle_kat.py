@@ -250,3 +250,81 @@ def test_volume_diagnostic_known_answers(oracle_mod):
     assert ref_err[0] / ref_err[1] > 1.8 and ref_err[1] / ref_err[2] > 1.8      # first order
     assert own_err[0] / own_err[1] > 3.2 and own_err[1] / own_err[2] > 3.2      # second order
     assert disk_err[0] < 1e-2 and disk_err[1] / disk_err[2] > 3.0
+
+
+@pytest.mark.parametrize("dim,n", [(3, 24), (2, 48)])
+def test_newton_restart_redistances_a_sphere(oracle_mod, dim, n):
+    """Newton configuration restart (HybridNewton without FMM, LevelSetLiquid.cpp:1290-1308)
+    on φ = (|x-c|² - r0²)/(2 r0), whose zero set is a sphere but which is not a distance
+    function: the reference level set it produces is the signed distance (closest points
+    by Newton next to the interface, eikonal advection beyond), ψ0 has unit length, and
+    ξ = x, Π = I afterwards."""
+    from helpers import newton_sphere_case
+    grid, phi, grad, sdf = newton_sphere_case(n, dim)
+    o = oracle_mod.OracleSim(grid, host_default_config(restart_newton=1))
+    o.upload(capi.FIELD_LEVEL_SET, phi.ravel())
+    o.upload(capi.FIELD_ORI_LEVEL_SET, phi.ravel())
+    o.upload(capi.FIELD_LEVEL_SET_GRAD, grad.ravel())
+    o.stage("restart")
+    dx = 1.0 / n
+    ref = o.download(capi.FIELD_REF_LEVEL_SET)
+    s = sdf.ravel()
+    near, band = np.abs(s) <= 1.5 * dx, np.abs(s) <= 6 * dx
+    assert np.mean(np.abs(ref - s)[near]) < 1e-5 * dx
+    assert np.max(np.abs(ref - s)[band]) < 1e-3 * dx
+    assert np.max(np.abs(phi.ravel() - s)[band]) > 0.1 * dx  # the input was far from a distance function
+    norms = np.linalg.norm(o.download(capi.FIELD_REF_LEVEL_SET_GRAD).reshape(-1, dim), axis=1)
+    assert np.max(np.abs(norms - 1)) < 1e-12
+    assert np.array_equal(o.download(capi.FIELD_LEVEL_SET_GRAD), o.download(capi.FIELD_REF_LEVEL_SET_GRAD))
+    assert np.array_equal(o.download(capi.FIELD_ORI_LEVEL_SET), ref)
+    pi = o.download(capi.FIELD_REF_MAP_GRAD).reshape(-1, dim * dim)
+    assert np.array_equal(pi, np.tile(np.eye(dim).ravel(), (len(pi), 1)))
+
+
+def test_newton_initialize_takes_psi0_from_the_level_set(oracle_mod):
+    """initialize in the Newton configuration: ∇φ by the 4th-order difference of the
+    level set before reinitialisation becomes ψ0 (LevelSetLiquid.cpp:546-558); the field
+    is absent without it."""
+    sc = scenes.drop(16, seed=4)
+    o = oracle_mod.OracleSim(sc.grid, host_default_config(restart_newton=1))
+    load_scene(o, sc)
+    o.initialize()
+    lg = o.download(capi.FIELD_LEVEL_SET_GRAD).reshape(-1, 3)
+    assert np.array_equal(lg.ravel(), o.download(capi.FIELD_REF_LEVEL_SET_GRAD))
+    # interior cells: (f(-2) - 8 f(-1) + 8 f(1) - f(2)) / 12dx along x, of the level set
+    # after enforceBoundaryLevelSet (φ >= -cellDist)
+    phi0 = np.maximum(sc.phi, -o.download(capi.FIELD_CELL_DIST).reshape(sc.phi.shape))
+    dx = sc.grid.spacing
+    gx = (phi0[:, :, 0:-4] - 8 * phi0[:, :, 1:-3] + 8 * phi0[:, :, 3:-1] - phi0[:, :, 4:]) / 12 / dx
+    assert np.max(np.abs(lg[:, 0].reshape(phi0.shape)[:, :, 2:-2] - gx)) < 1e-9
+    plain = oracle_mod.OracleSim(sc.grid, host_default_config())
+    with pytest.raises(ValueError):
+        plain.download(capi.FIELD_LEVEL_SET_GRAD)
+
+
+def test_newton_restart_is_ill_conditioned_on_a_simulated_scene(oracle_mod):
+    """The reference's Newton restart on a simulated level set is sensitive to ulp-level
+    input changes (closest-point iterations that stop after 20 capped steps, eikonal traces
+    along a vanishing gradient), while on a smooth one it is not.  This is why GPU parity
+    in that configuration is measured against the oracle's own perturbation spread."""
+    from helpers import STATE_FIELDS, perturbed
+    sc = scenes.drop(20, seed=3)
+    o = oracle_mod.OracleSim(sc.grid, host_default_config(restart_newton=1))
+    load_scene(o, sc)
+    o.initialize()
+    o.stage("restart")
+    for dt in scenes.frame_time_steps(o.max_speed, 3, 25, 1.0, sc.grid.spacing):
+        o.advance(dt)
+    fields = STATE_FIELDS + [capi.FIELD_LEVEL_SET_GRAD]
+    snap = {f: o.download(f) for f in fields}
+
+    def run(size):
+        s = oracle_mod.OracleSim(sc.grid, host_default_config(restart_newton=1))
+        for f, v in snap.items():
+            moved = f in (capi.FIELD_LEVEL_SET, capi.FIELD_ORI_LEVEL_SET, capi.FIELD_LEVEL_SET_GRAD)
+            s.upload(f, perturbed(v, size, f) if moved else v)
+        s.stage("restart")
+        return s.download(capi.FIELD_REF_LEVEL_SET)
+
+    dx = sc.grid.spacing
+    assert np.max(np.abs(run(1e-15) - run(0.0))) > 1e-3 * dx
