@@ -117,6 +117,13 @@ garm_status allocState(State &s) {
 		GARM_TRY(dalloc(s, (void **)&s.hnMark[0], N));
 		GARM_TRY(dalloc(s, (void **)&s.hnMark[1], N));
 	}
+	if (s.cfg.fast_marching) {
+		GARM_TRY(dalloc(s, &s.marchTent, N * e));
+		GARM_TRY(dalloc(s, &s.marchTent2, N * e));
+		GARM_TRY(dalloc(s, (void **)&s.marchFixed, N));
+		GARM_TRY(dalloc(s, (void **)&s.marchBar, 64));
+		GARM_TRY(dalloc(s, (void **)&s.marchInts, 64));
+	}
 	GARM_TRY(dalloc(s, &s.cellDist, N * e));
 	GARM_TRY(dalloc(s, &s.nodeDist, size_t(s.NN) * 8));
 	GARM_TRY(dalloc(s, &s.adv, N));
@@ -304,13 +311,23 @@ garm_status download(State &s, int field, void *host, size_t bytes) {
 	return sync(s);
 }
 
+// Outside a step the fast-marching relaxation reports its status on the host.
+garm_status reinitChecked(State &s) {
+	GARM_TRY(GARM_DISPATCH(s, reinitialize, s));
+	return s.cfg.fast_marching ? marchStatus(s, nullptr) : GARM_OK;
+}
+garm_status restartChecked(State &s) {
+	GARM_TRY(GARM_DISPATCH(s, restart, s));
+	return s.cfg.fast_marching && s.cfg.restart_newton ? marchStatus(s, nullptr) : GARM_OK;
+}
+
 // LevelSetLiquid::initialize (LevelSetLiquid.cpp:528-598)
 garm_status initialize(State &s) {
 	dropGraphs(s);  // boundary work lists are baked into captured steps
 	GARM_TRY(GARM_DISPATCH(s, finishBoundary, s));                       // _boundary.finish
 	GARM_TRY(GARM_DISPATCH(s, enforceBoundaryLevelSet, s, s.phi, 0.0));  // enforceBoundaryLevelSet(_levelSet)
 	if (s.cfg.restart_newton) GARM_TRY(GARM_DISPATCH(s, levelSetGradient, s));  // computeFirst<4>(_levelSet, _levelSetGrad)
-	GARM_TRY(GARM_DISPATCH(s, reinitialize, s));                         // reinitializeLevelSet
+	GARM_TRY(reinitChecked(s));                                          // reinitializeLevelSet
 	GARM_TRY(GARM_DISPATCH(s, copyField, s, s.tmp, s.phi, s.N));         // _tmpLevelSet = _levelSet
 	GARM_TRY(GARM_DISPATCH(s, copyField, s, s.ref, s.phi, s.N));         // _refLevelSet = _levelSet
 	GARM_TRY(GARM_DISPATCH(s, copyField, s, s.ori, s.phi, s.N));         // _oriLevelSet = _levelSet
@@ -334,7 +351,16 @@ garm_status record(State &s, int i) { return cudaEventRecord(s.ev[i], s.stream) 
 // s.dtDev.  No host synchronisation: the reference-map decision is a device flag
 // that gates the restart branch, and statistics go to the step's device record.
 // `timed` records the stage events (not allowed inside a graph capture).
+garm_status enqueueStepBody(State &s, bool timed);
+
 garm_status enqueueStep(State &s, bool timed) {
+	s.inStep = true;
+	const garm_status r = enqueueStepBody(s, timed);
+	s.inStep = false;
+	return r;
+}
+
+garm_status enqueueStepBody(State &s, bool timed) {
 	if (timed) GARM_TRY(record(s, 0));
 	GARM_TRY(GARM_DISPATCH(s, advectFields, s));
 	if (timed) GARM_TRY(record(s, 1));
@@ -387,7 +413,8 @@ garm_status readRecords(State &s, int k, garm_step_stats *S) {
 	garm_status worst = GARM_OK;
 	for (int q = 0; q < k; q++) {
 		const double *rec = s.statsHost + ((s.hostSteps - 1 - q + kStatsCap) % kStatsCap) * kStatsSlots;
-		if (rec[kStCgErr] != 0) return GARM_TIMEOUT;
+		if (rec[kStCgErr] != 0 || rec[kStMarchErr] == 1) return GARM_TIMEOUT;
+		if (rec[kStMarchErr] != 0) return GARM_NUMERIC;
 		if (rec[kStUnknowns] > 0 && !(rec[kStCgResidual] <= rec[kStCgTol])) worst = GARM_NOT_CONVERGED;
 	}
 	if (S) {
@@ -576,6 +603,7 @@ garm_status garm_config_default(garm_config *c) {
 	c->cg_cells_per_block = 0;
 	c->record_volume = 0;
 	c->restart_newton = 0;
+	c->fast_marching = 0;
 	return GARM_OK;
 }
 
@@ -621,6 +649,7 @@ garm_status garm_sim_create(const garm_grid_desc *gd, const garm_config *cfg, vo
 	if (c.reinit_iters < 0 || c.cg_max_iters < 0 || !(c.cg_tolerance > 0) || c.cg_cells_per_block < 0) return GARM_INVALID;
 	if (c.record_volume != 0 && c.record_volume != 1) return GARM_INVALID;
 	if (c.restart_newton != 0 && c.restart_newton != 1) return GARM_INVALID;
+	if (c.fast_marching != 0 && c.fast_marching != 1) return GARM_INVALID;
 
 	garm_sim *sim = new (std::nothrow) garm_sim();
 	if (!sim) return GARM_OOM;
@@ -843,10 +872,10 @@ garm_status garm_stage_advect(garm_sim *sim, double dt) {
 	STAGE_BODY(GARM_DISPATCH(s, advectFields, s));
 }
 garm_status garm_stage_compose(garm_sim *sim) { STAGE_BODY(GARM_DISPATCH(s, generateCurrentFields, s)); }
-garm_status garm_stage_reinit(garm_sim *sim) { STAGE_BODY(GARM_DISPATCH(s, reinitialize, s)); }
+garm_status garm_stage_reinit(garm_sim *sim) { STAGE_BODY(reinitChecked(s)); }
 garm_status garm_stage_extrap_collider(garm_sim *sim) { STAGE_BODY(GARM_DISPATCH(s, extrapolateToCollider, s)); }
 garm_status garm_stage_rm_check(garm_sim *sim, int *keep, int *total, int *bad) { STAGE_BODY(GARM_DISPATCH(s, checkReferenceMap, s, keep, total, bad)); }
-garm_status garm_stage_restart(garm_sim *sim) { STAGE_BODY(GARM_DISPATCH(s, restart, s)); }
+garm_status garm_stage_restart(garm_sim *sim) { STAGE_BODY(restartChecked(s)); }
 garm_status garm_stage_body_force(garm_sim *sim, double dt) {
 	if (!sim) return GARM_INVALID;
 	kSetScalar<<<1, 1, 0, sim->s.stream>>>(sim->s.dtDev, dt);

@@ -47,6 +47,12 @@ struct State {
 	void *lsGrad[3] = {};
 	void *hnPhi = nullptr, *hnGrad[3] = {}, *hnMixed[4] = {}, *hnPoints[3] = {};
 	uint8_t *hnMark[2] = {};
+	// fast-marching configuration only (cfg.fast_marching): tentative distances, seed
+	// flags, the relaxation's barrier and control words
+	void *marchTent = nullptr, *marchTent2 = nullptr;
+	uint8_t *marchFixed = nullptr;
+	unsigned *marchBar = nullptr;
+	int *marchInts = nullptr;
 	uint8_t *adv = nullptr;    // _advRegion
 	uint8_t *vis0 = nullptr, *vis1 = nullptr;       // cell extrapolation masks
 	uint8_t *fvis0 = nullptr, *fvis1 = nullptr;     // face extrapolation masks (all axes, concatenated)
@@ -94,6 +100,7 @@ struct State {
 	double *clockDev = nullptr;
 	int *restartFlag = nullptr;
 	const int *gate = nullptr;
+	bool inStep = false;               // enqueueing a step: stage errors go to its device record
 	double *statsDev = nullptr;        // kStatsSlots doubles per recorded step
 	unsigned long long *stepCounter = nullptr;  // device count of started steps
 	unsigned long long hostSteps = 0;           // host mirror of the counter
@@ -115,7 +122,7 @@ __device__ __forceinline__ double *stepRecord(double *base, const unsigned long 
 }
 
 // Layout of one per-step statistics record on the device.
-enum StatSlot { kStDt = 0, kStRestarted, kStRmTotal, kStRmBad, kStUnknowns, kStCgIters, kStCgRefine, kStCgResidual, kStCgTol, kStCgErr, kStVolume, kStatsSlots = 12 };
+enum StatSlot { kStDt = 0, kStRestarted, kStRmTotal, kStRmBad, kStUnknowns, kStCgIters, kStCgRefine, kStCgResidual, kStCgTol, kStCgErr, kStVolume, kStMarchErr, kStatsSlots = 12 };
 
 // Stage entry points (templated on dimension D and working type T).
 template <int D, typename T> garm_status initBoundary(State &s);
@@ -150,6 +157,11 @@ template <int D, typename T> garm_status scalarMixed(State &s, T *const *grad, T
 template <int D, typename T> garm_status initRefMap(State &s);
 template <int D, typename T> garm_status refreshRefGradient(State &s);
 template <int D, typename T> garm_status levelSetGradient(State &s);
+// FastMarching::perform on a cell plane: seeds from the sign changes of φ (mark null) or
+// the marked cells, then the relaxation and the sign; errors go to the step record when
+// `record` is set, else marchStatus reads them.
+template <int D, typename T> garm_status fastMarch(State &s, void *phi, const uint8_t *mark, int maxSteps, bool record);
+garm_status marchStatus(State &s, int *sweeps);
 template <int D, typename T> garm_status maxSpeed(State &s, double *out);
 template <int D, typename T> garm_status maxSpeedAsync(State &s);
 __global__ void kStepDt(const unsigned long long *maxBits, double dx, double *clock, double *dt, double *stats, const unsigned long long *counter);

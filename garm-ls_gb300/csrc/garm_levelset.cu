@@ -757,6 +757,8 @@ static garm_status reinitLoop(cudaStream_t st, const G<D, T> &g, T *phi, T *A, T
 
 template <int D, typename T>
 garm_status reinitialize(State &s) {
+	// fast-marching configuration: FastMarching over a band of 15 cells (LevelSetLiquid.cpp:1151-1152)
+	if (s.cfg.fast_marching) return fastMarch<D, T>(s, s.phi, nullptr, 15, s.inStep);
 	const G<D, T> g = cellGrid<D, T>(s.geom);
 	return reinitLoop<D, T>(s.stream, g, (T *)s.phi, (T *)s.rA, (T *)s.rB, s.cfg.reinit_iters, s.cfg.reinit_cfl, &s.launches);
 }
@@ -914,6 +916,29 @@ struct NewtonIO {
 	T *xi[3], *Pi[9];             // ξ = x, Π = I
 };
 
+// ScalarFieldWrapper::gradient (ScalarField.h:41-47): the trilinear blend of the central
+// differences (Derivatives.h:47-57) at the 2^D samples around p.
+template <int D, typename T>
+__device__ __forceinline__ void blendGradient(const G<D, T> &g, const T *f, const T *pos, T *gr) {
+	int ll[3] = {0, 0, 0};
+	T fr[3] = {T(0), T(0), T(0)};
+#pragma unroll
+	for (int a = 0; a < D; a++) { ll[a] = g.lower(a, pos[a]); fr[a] = g.frac(a, pos[a], ll[a]); }
+	const T h = T(0.5) * g.inv;
+	for (int q = 0; q < (1 << D); q++) {
+		const int n[3] = {ll[0] + (q & 1), ll[1] + (q >> 1 & 1), D == 3 ? ll[2] + (q >> 2 & 1) : 0};
+		T wt = T(1);
+#pragma unroll
+		for (int a = 0; a < D; a++) wt *= ((q >> a) & 1) ? fr[a] : T(1) - fr[a];
+#pragma unroll
+		for (int a = 0; a < D; a++) {
+			const int ex = a == 0, ey = a == 1, ez = a == 2;
+			const T d = (ldg(f + g.cidx(n[0] + ex, n[1] + ey, n[2] + ez)) - ldg(f + g.cidx(n[0] - ex, n[1] - ey, n[2] - ez))) * h;
+			gr[a] += d * wt;
+		}
+	}
+}
+
 // Starting points p − φ(p)·∇φ(p) from _levelSetView: the cubic Lagrange value and, as
 // ScalarFieldWrapper::gradient does, the trilinear blend of the central differences at
 // the eight surrounding samples (ScalarField.h:41-47, Derivatives.h:47-57).
@@ -952,25 +977,8 @@ __global__ void __launch_bounds__(kBlock) kHnPoints(Geom geom, NewtonIO<D, T> io
 		}
 		v += D == 3 ? sy * w[2][c] : sy;
 	}
-	// trilinear blend of central differences
-	int ll[3] = {0, 0, 0};
-	T fr[3] = {T(0), T(0), T(0)};
-#pragma unroll
-	for (int a = 0; a < D; a++) { ll[a] = g.lower(a, pos[a]); fr[a] = g.frac(a, pos[a], ll[a]); }
 	T gr[3] = {T(0), T(0), T(0)};
-	const T h = T(0.5) * g.inv;
-	for (int q = 0; q < (1 << D); q++) {
-		const int n[3] = {ll[0] + (q & 1), ll[1] + (q >> 1 & 1), D == 3 ? ll[2] + (q >> 2 & 1) : 0};
-		T wt = T(1);
-#pragma unroll
-		for (int a = 0; a < D; a++) wt *= ((q >> a) & 1) ? fr[a] : T(1) - fr[a];
-#pragma unroll
-		for (int a = 0; a < D; a++) {
-			const int ex = a == 0, ey = a == 1, ez = a == 2;
-			const T d = (ldg(f + g.cidx(n[0] + ex, n[1] + ey, n[2] + ez)) - ldg(f + g.cidx(n[0] - ex, n[1] - ey, n[2] - ez))) * h;
-			gr[a] += d * wt;
-		}
-	}
+	blendGradient<D, T>(g, f, pos, gr);
 #pragma unroll
 	for (int a = 0; a < D; a++) io.pts[a][id] = pos[a] - v * gr[a];
 }
@@ -1137,6 +1145,24 @@ __global__ void __launch_bounds__(kBlock) kHnAdvect(Geom geom, const T *fin, con
 	for (int a = 0; a < D; a++) gout[a][id] = gr[a];
 }
 
+// The end of HybridNewton::sweep (HybridNewton.cpp:56-63): on unmarked cells ψ is the
+// normalised gradient of the cubic view of the marched φ.
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kHnSweepGrad(Geom geom, NewtonIO<D, T> io, const int *gate) {
+	if (gate && !*gate) return;
+	const G<D, T> g = cellGrid<D, T>(geom);
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= g.count() || io.mark1[id]) return;
+	int ci, cj, ck;
+	g.coord(id, ci, cj, ck);
+	const T pos[3] = {g.pos(0, ci), g.pos(1, cj), D == 3 ? g.pos(2, ck) : T(0)};
+	T gr[3] = {T(0), T(0), T(0)};
+	blendGradient<D, T>(g, io.hp, pos, gr);
+	normalizeOr<D, T>(gr, false);
+#pragma unroll
+	for (int a = 0; a < D; a++) io.hg[a][id] = gr[a];
+}
+
 // The result into _oriLevelSet/_levelSetGrad and _refLevelSet/_refLevelSetGrad; ξ = x, Π = I.
 template <int D, typename T>
 __global__ void __launch_bounds__(kBlock) kHnFinish(Geom geom, NewtonIO<D, T> io, const int *gate) {
@@ -1178,6 +1204,15 @@ static garm_status newtonRestart(State &s) {
 	GARM_TRY((scalarMixed<D, T>(s, io.lsGrad, io.mixed)));
 	kHnInterface<D, T><<<nb, kBlock, 0, s.stream>>>(s.geom, io, s.gate); s.launches++;
 	GARM_CHECK_LAUNCH();
+	if (s.cfg.fast_marching) {
+		// sweep, maxSteps 20 (HybridNewton.cpp:51-64): fast marching from the marked cells
+		GARM_TRY((fastMarch<D, T>(s, io.hp, io.mark1, 20, s.inStep)));
+		kHnSweepGrad<D, T><<<nb, kBlock, 0, s.stream>>>(s.geom, io, s.gate); s.launches++;
+		GARM_CHECK_LAUNCH();
+		kHnFinish<D, T><<<nb, kBlock, 0, s.stream>>>(s.geom, io, s.gate); s.launches++;
+		GARM_CHECK_LAUNCH();
+		return resetRefView<D, T>(s);
+	}
 	// advect, maxSteps 20, cfl 0.9 (LevelSetLiquid.cpp:1301): the buffers alternate, so after
 	// an even number of steps the result is back in (hp, hg)
 	const T dt = T(s.geom.dx * 0.9);

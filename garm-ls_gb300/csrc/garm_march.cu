@@ -1,0 +1,229 @@
+// garm_march.cu — fast-marching reinitialisation, FastMarching<Dim>::perform
+// (Source/Core/FastMarching.cpp:10-128), on the GPU.
+//
+// The reference accepts cells one at a time from a binary heap.  Each accepted value is the
+// root of the upwind quadratic over the smallest accepted neighbour per axis, and only
+// values below the band width are ever accepted.  Its result is therefore the solution of
+// the discrete system
+//     u_i = fixed value                              on the interface (seed) cells,
+//     u_i = min(band, Q(min_x u, min_y u, min_z u))  elsewhere,
+// where min_a u is the smaller of the two neighbours along axis a.  Neighbours whose value
+// is not below u_i drop out of Q through its own case tests, so using all neighbours gives
+// the same root as using the accepted ones.  This file computes that solution without a
+// heap: one persistent cooperative launch relaxes every cell, always towards smaller values
+// and never below the solution, until a whole sweep changes nothing.  The sweeps are
+// Jacobi sweeps between two buffers, so the result does not depend on the order in which
+// blocks run (an in-place relaxation can settle on different last bits where a neighbour
+// ties with a root).  Each cell's update is the reference's quadratic in the same operation
+// order, so the result is the reference's up to the last bits in exact ties, where a
+// neighbour equal to the root enters or drops out of Q.
+#include "garm_internal.h"
+#include "garm_sync.cuh"
+
+#include <algorithm>
+
+namespace garm {
+
+constexpr int kMarchBlock = 256;
+constexpr int kMarchSweepCap = 4096;   // never reached on level sets; past it → GARM_NUMERIC
+constexpr int kMarchCellsPerThread = 8; // blocks in proportion to the grid, so that small scenes leave SMs free
+
+
+// solveQuadratic (FastMarching.cpp:112-128).  The 3-term form orders its arguments with
+// the reference's two swaps, which leave p2 the largest and p0, p1 in either order.
+template <typename T>
+__device__ __forceinline__ T marchQuad2(T p0, T p1, T dx) {
+	if (p0 > p1) { const T t = p0; p0 = p1; p1 = t; }
+	if (isinf(p1) || p1 - p0 > dx) return p0 + dx;
+	return ((p0 + p1) + sqrt(T(2) * dx * dx - (p0 - p1) * (p0 - p1))) * T(0.5);
+}
+template <typename T>
+__device__ __forceinline__ T marchQuad3(T p0, T p1, T p2, T dx) {
+	if (p0 > p1) { const T t = p0; p0 = p1; p1 = t; }
+	if (p1 > p2) { const T t = p1; p1 = p2; p2 = t; }
+	if (isinf(p2) || (p2 - p0) * (p2 - p0) + (p2 - p1) * (p2 - p1) > dx * dx) return marchQuad2(p0, p1, dx);
+	const T s = p0 + p1 + p2;
+	return (s + sqrt(s * s - T(3) * (p0 * p0 + p1 * p1 + p2 * p2 - dx * dx))) / T(3);
+}
+
+// std::min(a, b) as the reference uses it: b only when b < a (a NaN candidate never enters).
+template <typename T>
+__device__ __forceinline__ T minKeep(T a, T b) { return b < a ? b : a; }
+
+// Seeds of perform(phi, maxSteps) (FastMarching.cpp:14-30): cells with a sign change to a
+// neighbour start at the harmonic combination 1/|(1/d_x, 1/d_y, 1/d_z)| of the per-axis
+// crossing distances d_a = φ/(φ - φ_nb)·dx; the others at the band width.  Both sweep
+// buffers start with these values.
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kMarchSeedSigns(Geom geom, const T *phi, T *tent, T *tent2, uint8_t *fixed, T band, const int *gate) {
+	if (gate && !*gate) return;
+	const G<D, T> g = cellGrid<D, T>(geom);
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= g.count()) return;
+	int i, j, k;
+	g.coord(id, i, j, k);
+	const T f = phi[id];
+	const T inf = T(INFINITY);
+	T t[3] = {inf, inf, inf};
+#pragma unroll
+	for (int nb = 0; nb < 2 * D; nb++) {
+		const int a = nb >> 1, s = (nb & 1) ? 1 : -1;
+		const int ni = i + (a == 0 ? s : 0), nj = j + (a == 1 ? s : 0), nk = k + (a == 2 ? s : 0);
+		if (!g.valid(ni, nj, nk)) continue;
+		const T fn = phi[g.idx(ni, nj, nk)];
+		if (f * fn <= T(0)) t[a] = minKeep(t[a], f / (f - fn) * g.dx);
+	}
+	bool any = false;
+#pragma unroll
+	for (int a = 0; a < D; a++) any = any || isfinite(t[a]);
+	if (any) {
+		T sum = T(0);
+#pragma unroll
+		for (int a = 0; a < D; a++) { const T r = T(1) / t[a]; sum += r * r; }
+		const T v = T(1) / sqrt(sum);
+		tent[id] = v;
+		tent2[id] = v;
+		fixed[id] = 1;
+	} else {
+		tent[id] = band;
+		tent2[id] = band;
+		fixed[id] = 0;
+	}
+}
+
+// Seeds of perform(phi, maxSteps, mark) (FastMarching.cpp:46-58): marked cells keep |φ|.
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kMarchSeedMarked(int64_t n, const T *phi, const uint8_t *mark, T *tent, T *tent2, uint8_t *fixed, T band, const int *gate) {
+	if (gate && !*gate) return;
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= n) return;
+	const uint8_t m = mark[id];
+	const T v = m ? fabs(phi[id]) : band;
+	tent[id] = v;
+	tent2[id] = v;
+	fixed[id] = m;
+}
+
+struct MarchCtl {
+	unsigned *bar;   // grid barrier counter
+	int *ints;       // [0..2] per-sweep change flags (rotating), [3] error (1 barrier timeout, 2 sweep cap), [4] sweeps
+	double *stats;   // step records (null outside a recorded step)
+	const unsigned long long *counter;
+};
+
+// The relaxation: Jacobi sweeps over all cells, sweep s reading buffer s%2 and writing
+// min(u, Q(neighbours)) into the other, until a sweep changes nothing anywhere; then both
+// buffers hold the solution.  Seed cells hold the same value in both and are not written.
+// Change flags rotate over three slots: slot s%3 collects sweep s, is read by every block
+// after that sweep's barrier, and is cleared by block 0 during sweep s+2, when every block
+// has passed the barrier after its read.  Values written by other blocks are read with
+// L2-coherent loads after the barrier.
+template <int D, typename T>
+__global__ void __launch_bounds__(kMarchBlock) kMarch(Geom geom, T *tentA, T *tentB, const uint8_t *fixed, MarchCtl ctl, const int *gate) {
+	if (gate && !*gate) return;
+	const G<D, T> g = cellGrid<D, T>(geom);
+	const int64_t n = g.count();
+	const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+	const T dx = g.dx;
+	const T inf = T(INFINITY);
+	__shared__ int blockChanged;
+	unsigned epoch = 0;
+	int sweep = 0;
+	int *err = ctl.ints + 3;
+	bool converged = false;
+	for (; sweep < kMarchSweepCap; sweep++) {
+		if (threadIdx.x == 0) blockChanged = 0;
+		if (blockIdx.x == 0 && threadIdx.x == 0) ctl.ints[(sweep + 1) % 3] = 0;
+		__syncthreads();
+		const T *src = (sweep & 1) ? tentB : tentA;
+		T *dst = (sweep & 1) ? tentA : tentB;
+		bool mine = false;
+		for (int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; id < n; id += stride) {
+			if (fixed[id]) continue;
+			int i, j, k;
+			g.coord(id, i, j, k);
+			T m[3] = {inf, inf, inf};
+#pragma unroll
+			for (int nb = 0; nb < 2 * D; nb++) {
+				const int a = nb >> 1, s = (nb & 1) ? 1 : -1;
+				const int ni = i + (a == 0 ? s : 0), nj = j + (a == 1 ? s : 0), nk = k + (a == 2 ? s : 0);
+				if (g.valid(ni, nj, nk)) m[a] = minKeep(m[a], __ldcg(src + g.idx(ni, nj, nk)));
+			}
+			const T cand = D == 2 ? marchQuad2(m[0], m[1], dx) : marchQuad3(m[0], m[1], m[2], dx);
+			const T cur = __ldcg(src + id);
+			if (cand < cur) { dst[id] = cand; mine = true; }
+			else dst[id] = cur;
+		}
+		if (mine) blockChanged = 1;
+		__syncthreads();
+		if (threadIdx.x == 0 && blockChanged) atomicExch(ctl.ints + sweep % 3, 1);
+		if (!gridSync(ctl.bar, err, epoch)) break;
+		if (*(volatile int *)(ctl.ints + sweep % 3) == 0) { converged = true; break; }
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		ctl.ints[4] = sweep + 1;
+		if (!converged && *(volatile int *)err == 0) atomicExch(err, 2);
+		const int code = *(volatile int *)err;
+		double *rec = stepRecord(ctl.stats, ctl.counter);
+		if (rec && code) rec[kStMarchErr] = code;
+	}
+}
+
+// φ = sign(φ)·tent (FastMarching.cpp:40-42, 69-71): the sign of the input, with 0 negative.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) kMarchSign(int64_t n, T *phi, const T *tent, const int *gate) {
+	if (gate && !*gate) return;
+	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+	if (id >= n) return;
+	phi[id] = (phi[id] <= T(0) ? T(-1) : T(1)) * tent[id];
+}
+
+template <int D, typename T>
+garm_status fastMarch(State &s, void *phiPlane, const uint8_t *mark, int maxSteps, bool record) {
+	T *phi = (T *)phiPlane;
+	T *tent = (T *)s.marchTent, *tent2 = (T *)s.marchTent2;
+	const double bandD = maxSteps * s.geom.dx;
+	// bandWidth > 0 without a mark, >= 0 with one; otherwise unbounded (FastMarching.cpp:13, 49)
+	const T band = (mark ? bandD >= 0 : bandD > 0) ? T(bandD) : T(INFINITY);
+	const unsigned nb = gridFor(s.N);
+	if (mark) kMarchSeedMarked<D, T><<<nb, kBlock, 0, s.stream>>>(s.N, phi, mark, tent, tent2, s.marchFixed, band, s.gate);
+	else kMarchSeedSigns<D, T><<<nb, kBlock, 0, s.stream>>>(s.geom, phi, tent, tent2, s.marchFixed, band, s.gate);
+	s.launches++;
+	GARM_CHECK_LAUNCH();
+	cudaError_t e = cudaMemsetAsync(s.marchBar, 0, 2 * sizeof(unsigned), s.stream);
+	if (e == cudaSuccess) e = cudaMemsetAsync(s.marchInts, 0, 8 * sizeof(int), s.stream);
+	if (e != cudaSuccess) return GARM_CUDA_ERROR;
+	int perSM = 0;
+	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kMarch<D, T>, kMarchBlock, 0);
+	if (e != cudaSuccess || perSM <= 0) return GARM_CUDA_ERROR;
+	const int64_t want = (s.N + kMarchBlock * kMarchCellsPerThread - 1) / (kMarchBlock * kMarchCellsPerThread);
+	const int blocks = int(std::max<int64_t>(1, std::min<int64_t>(want, int64_t(perSM) * s.numSMs)));
+	MarchCtl ctl{s.marchBar, s.marchInts, record ? s.statsDev : nullptr, s.stepCounter};
+	Geom geom = s.geom;
+	const int *gate = s.gate;
+	void *args[] = {&geom, &tent, &tent2, &s.marchFixed, &ctl, &gate};
+	e = cudaLaunchCooperativeKernel((void *)kMarch<D, T>, dim3(blocks), dim3(kMarchBlock), args, 0, s.stream);
+	if (e != cudaSuccess) return GARM_CUDA_ERROR;
+	s.launches++;
+	kMarchSign<T><<<nb, kBlock, 0, s.stream>>>(s.N, phi, tent, s.gate); s.launches++;
+	GARM_CHECK_LAUNCH();
+	return GARM_OK;
+}
+
+// Status and sweep count of the last relaxation (synchronises the stream).
+garm_status marchStatus(State &s, int *sweeps) {
+	int h[5] = {};
+	if (cudaMemcpyAsync(h, s.marchInts, sizeof(h), cudaMemcpyDeviceToHost, s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
+	if (cudaStreamSynchronize(s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
+	if (sweeps) *sweeps = h[4];
+	return h[3] == 1 ? GARM_TIMEOUT : h[3] == 2 ? GARM_NUMERIC : GARM_OK;
+}
+
+#define GARM_INST(D, T) template garm_status fastMarch<D, T>(State &, void *, const uint8_t *, int, bool);
+GARM_INST(2, double)
+GARM_INST(3, double)
+GARM_INST(2, float)
+GARM_INST(3, float)
+#undef GARM_INST
+
+}  // namespace garm

@@ -9,6 +9,7 @@
 //                          phase per iteration with FP64 residual replacement
 //   applyPressureGradient (Projector.cpp:91-123)
 #include "garm_internal.h"
+#include "garm_sync.cuh"
 
 #include <algorithm>
 
@@ -18,8 +19,6 @@ namespace garm {
 
 constexpr int kCgBlock = 512;
 constexpr int kRegUnknowns = 4;  // unknowns per thread held in registers by the PCG
-constexpr unsigned long long kBarrierWaitNs = 2000000000ull;     // one barrier wait longer than 2 s → GARM_TIMEOUT
-constexpr unsigned long long kBarrierSpinLimit = 1ull << 32;     // backstop on the number of polls
 
 // ---------------------------------------------------------------------------
 // unknown set and numbering
@@ -178,45 +177,6 @@ struct CgArgs {
 // other blocks' stores; the read-only texture path (__ldg) is never used for them.
 __device__ __forceinline__ double ldcg(const double *p) { return *p; }
 __device__ __forceinline__ float ldcg(const float *p) { return *p; }
-
-__device__ __forceinline__ unsigned ldAcquire(const unsigned *ptr) {
-	unsigned v;
-	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ptr) : "memory");
-	return v;
-}
-__device__ __forceinline__ unsigned long long globalNs() {
-	unsigned long long t;
-	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-	return t;
-}
-__device__ __forceinline__ void addRelease(unsigned *ptr, unsigned v) {
-	asm volatile("red.release.gpu.global.add.u32 [%0], %1;" :: "l"(ptr), "r"(v) : "memory");
-}
-
-// Grid-wide barrier with a bounded wait.  Each block adds 1 to a counter with
-// release semantics once its threads have passed __syncthreads; a block waits
-// (acquire loads) until the counter reaches gridDim.x times the number of
-// barriers passed so far.  The wait is bounded in time (checked every 1024
-// polls against the global nanosecond timer): past the limit the block sets the
-// error flag and every block leaves at its next barrier.  Returns false then.
-__device__ bool gridSync(unsigned *bar, int *err, unsigned &epoch) {
-	__syncthreads();
-	if (threadIdx.x == 0) {
-		epoch += gridDim.x;
-		addRelease(bar, 1u);
-		unsigned long long spins = 0, start = 0;
-		while (ldAcquire(bar) < epoch) {
-			if ((++spins & 1023ull) == 0) {
-				if (*(volatile int *)err) break;
-				const unsigned long long now = globalNs();
-				if (start == 0) start = now;
-				if (now - start > kBarrierWaitNs || spins > kBarrierSpinLimit) { atomicExch(err, 1); break; }
-			}
-		}
-	}
-	__syncthreads();
-	return *(volatile int *)err == 0;
-}
 
 // Block partial sums of NV values → partials[v*maxBlocks + blockIdx]
 template <int NV>

@@ -52,7 +52,8 @@ class Config(C.Structure):
                 ("boundary_extrap_radius", C.c_double), ("air_extrap_radius", C.c_double),
                 ("rm_threshold", C.c_double), ("rm_band", C.c_double), ("rm_ratio", C.c_double),
                 ("enable_gravity", C.c_int), ("mixed_residual_drop", C.c_double),
-                ("mixed_replace_interval", C.c_int), ("cg_cells_per_block", C.c_int), ("record_volume", C.c_int), ("restart_newton", C.c_int)]
+                ("mixed_replace_interval", C.c_int), ("cg_cells_per_block", C.c_int), ("record_volume", C.c_int), ("restart_newton", C.c_int),
+                ("fast_marching", C.c_int)]
 
 
 class StepStats(C.Structure):

@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define GARM_ABI_VERSION 4
+#define GARM_ABI_VERSION 5
 
 typedef enum garm_status {
     GARM_OK = 0,
@@ -100,10 +100,16 @@ typedef struct garm_config {
                                          SMs free for other scenes' work when scenes run concurrently */
     int record_volume;                /* 1: every step ends with the volume diagnostic (garm_sim_volume, corner
                                          order 0) written to its statistics on the device (no host round trip) */
-    int restart_newton;               /* 1: the reference's Newton configuration (_ENABLE_NEWTON_, without FMM):
+    int restart_newton;               /* 1: the reference's Newton configuration (_ENABLE_NEWTON_):
                                          compose also keeps ∇φ = Πᵀ∇φ₀(ξ), initialize takes ψ₀ from the 4th-order
                                          gradient of φ, and restart() is the HybridNewton closest-point restart
-                                         (LevelSetLiquid.cpp:1290-1308); 0: the plain WENO restart */
+                                         (LevelSetLiquid.cpp:1290-1308); 0: the plain restart */
+    int fast_marching;                /* 1: the reference's fast-marching configuration (_ENABLE_FMM_):
+                                         reinitializeLevelSet is fast marching over a band of 15 cells
+                                         (LevelSetLiquid.cpp:1151-1152) instead of WENO5, and the Newton
+                                         restart ends with a fast-marching sweep (HybridNewton.cpp:51-64)
+                                         instead of eikonal advection.  Both flags set is the reference's
+                                         default build (xmake.lua:41-55) */
 } garm_config;
 
 /* Per-step statistics returned by garm_sim_advance. */

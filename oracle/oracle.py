@@ -59,6 +59,7 @@ def load() -> C.CDLL:
     lib.orc_set_threads.argtypes = [C.c_int]
     lib.orc_max_threads.restype = C.c_int
     lib.orc_reinit.argtypes = [C.c_int, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int, C.c_double]
+    lib.orc_fast_marching.argtypes = [C.c_int, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int, C.c_void_p]
     lib.orc_hermite_eval.argtypes = [C.c_int, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.orc_cubic_eval.argtypes = [C.c_int, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
@@ -153,6 +154,17 @@ def reinit(phi: np.ndarray, spacing: float, iters: int, cfl: float) -> np.ndarra
     size = (C.c_int * 3)(*([int(x) for x in reversed(a.shape)] + [1] * (3 - a.ndim)))
     if load().orc_reinit(a.ndim, size, float(spacing), _dp(a), int(iters), float(cfl)) != OK:
         raise ValueError("orc_reinit")
+    return a
+
+
+def fast_marching(phi: np.ndarray, spacing: float, max_steps: int, mark: np.ndarray | None = None) -> np.ndarray:
+    """FastMarching::perform on a cell field (numpy order, x fastest): seeds from the sign
+    changes, or the cells where `mark` is non-zero keep |φ|."""
+    a = np.ascontiguousarray(phi, dtype=np.float64).copy()
+    size = (C.c_int * 3)(*([int(x) for x in reversed(a.shape)] + [1] * (3 - a.ndim)))
+    m = None if mark is None else np.ascontiguousarray(mark, dtype=np.uint8)
+    if load().orc_fast_marching(a.ndim, size, float(spacing), _dp(a), int(max_steps), None if m is None else m.ctypes.data) != OK:
+        raise ValueError("orc_fast_marching")
     return a
 
 

@@ -30,6 +30,7 @@ def host_default_config(**kw) -> capi.Config:
     c.cg_cells_per_block = 0
     c.record_volume = 0
     c.restart_newton = 0
+    c.fast_marching = 0
     for k, v in kw.items():
         setattr(c, k, v)
     return c
@@ -173,6 +174,23 @@ def perturbed(v, rel_size: float, seed: int):
 
 
 PERTURBATIONS = ((1e-15, 11), (2e-15, 12), (-1e-15, 13))
+
+
+def perturbed_steps(oracle_mod, scene, cfg, dts, size: float, seed: int):
+    """Oracle state after initialize, restart and the steps `dts`, with the initial level set
+    and, before every step, the reference map and the velocity scaled by 1 + size·U(-1, 1):
+    rounding-sized changes entering at every step, as a different evaluation order does."""
+    o = oracle_mod.OracleSim(scene.grid, cfg)
+    o.upload(capi.FIELD_LEVEL_SET, perturbed(scene.phi.ravel(), size, seed))
+    o.upload(capi.FIELD_VELOCITY, scene.velocity)
+    o.initialize()
+    o.stage("restart")
+    for q, dt in enumerate(dts):
+        if size:
+            for f in (capi.FIELD_REF_MAP, capi.FIELD_VELOCITY):
+                o.upload(f, perturbed(o.download(f), size, seed * 1000 + q * 10 + f))
+        assert o.advance(dt)["restarted"] == 1
+    return o
 
 
 def oracle_spread(run):

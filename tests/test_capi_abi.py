@@ -42,12 +42,12 @@ def test_struct_layout_matches_header(tmp_path):
     probe = tmp_path / "probe.c"
     probe.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "garm.h"\n'
                      'int main(void){printf("%zu %zu %zu %zu %zu\\n", sizeof(garm_grid_desc), sizeof(garm_config),'
-                     ' sizeof(garm_step_stats), offsetof(garm_config, restart_newton), offsetof(garm_step_stats, volume));return 0;}\n')
+                     ' sizeof(garm_step_stats), offsetof(garm_config, fast_marching), offsetof(garm_step_stats, volume));return 0;}\n')
     exe = tmp_path / "probe"
     subprocess.run(["gcc", "-I", str(REPO / "include"), str(probe), "-o", str(exe)], check=True)
     vals = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     assert vals == [C.sizeof(capi.GridDesc), C.sizeof(capi.Config), C.sizeof(capi.StepStats),
-                    capi.Config.restart_newton.offset, capi.StepStats.volume.offset]
+                    capi.Config.fast_marching.offset, capi.StepStats.volume.offset]
 
 
 def test_config_defaults_equal_reference_constants(garm_lib):
@@ -61,7 +61,7 @@ def test_config_defaults_equal_reference_constants(garm_lib):
 
 
 def test_status_strings_and_abi_version(garm_lib):
-    assert garm_lib.garm_abi_version() == 4
+    assert garm_lib.garm_abi_version() == 5
     assert garm_lib.garm_status_string(capi.NOT_CONVERGED) == b"pressure solve did not converge"
 
 

@@ -328,3 +328,119 @@ def test_newton_restart_is_ill_conditioned_on_a_simulated_scene(oracle_mod):
 
     dx = sc.grid.spacing
     assert np.max(np.abs(run(1e-15) - run(0.0))) > 1e-3 * dx
+
+
+def upwind_fixed_point(seed_val, fixed, spacing, band):
+    """Independent numpy restatement of the fast-marching equations: every non-seed cell holds
+    min(band, Q(per-axis smaller neighbour)) with Q the upwind quadratic of
+    FastMarching.cpp:112-128; solved by Jacobi relaxation from above."""
+    u = np.where(fixed, seed_val, band).astype(np.float64)
+    dim = u.ndim
+    dx = spacing
+
+    def axis_min(v, ax):
+        lo = np.full_like(v, np.inf)
+        hi = np.full_like(v, np.inf)
+        sl = [slice(None)] * dim
+        sr = [slice(None)] * dim
+        sl[ax], sr[ax] = slice(1, None), slice(None, -1)
+        lo[tuple(sl)] = v[tuple(sr)]
+        hi[tuple(sr)] = v[tuple(sl)]
+        return np.where(hi < lo, hi, lo)
+
+    def q2(p0, p1):
+        a, b = np.minimum(p0, p1), np.maximum(p0, p1)
+        with np.errstate(invalid="ignore"):
+            two = ((a + b) + np.sqrt(2 * dx * dx - (a - b) * (a - b))) * .5
+        return np.where(np.isinf(b) | (b - a > dx), a + dx, two)
+
+    def q3(p0, p1, p2):
+        s0 = np.where(p0 > p1, p1, p0); s1 = np.where(p0 > p1, p0, p1)
+        t1 = np.where(s1 > p2, p2, s1); t2 = np.where(s1 > p2, s1, p2)
+        drop = np.isinf(t2) | ((t2 - s0) * (t2 - s0) + (t2 - t1) * (t2 - t1) > dx * dx)
+        s = s0 + t1 + t2
+        with np.errstate(invalid="ignore"):
+            three = (s + np.sqrt(s * s - 3 * (s0 * s0 + t1 * t1 + t2 * t2 - dx * dx))) / 3
+        return np.where(drop, q2(s0, t1), three)
+
+    # numpy axis 0 is z (3D) or y (2D): the quadratic is symmetric in its per-axis arguments
+    # except for the operation order, so pass them in x, y, z order as the reference does
+    for _ in range(10000):
+        m = [axis_min(u, dim - 1 - a) for a in range(dim)]
+        cand = q2(m[0], m[1]) if dim == 2 else q3(m[0], m[1], m[2])
+        new = np.where(fixed | ~(cand < u), u, cand)
+        if np.array_equal(new, u):
+            return u
+        u = new
+    raise AssertionError("no convergence")
+
+
+@pytest.mark.parametrize("dim,n", [(2, 64), (3, 24)])
+def test_fast_marching_equals_the_upwind_fixed_point(oracle_mod, dim, n):
+    """The heap-ordered fast marching of the reference (restated in the oracle) and the fixed
+    point of its upwind equations agree, both from sign-change seeds and from marked seeds.
+    This is what lets the GPU solve the same equations by parallel relaxation instead of a
+    serial heap."""
+    from helpers import newton_sphere_case
+    grid, phi, _, _ = newton_sphere_case(n, dim)
+    dx = 1.0 / n
+    phi = phi + 0.05 * dx * np.sin(np.arange(phi.size) * 0.7).reshape(phi.shape)  # break symmetries
+    band = 15 * dx
+    out = oracle_mod.fast_marching(phi, dx, 15)
+    # seeds as FastMarching.cpp:14-30 computes them
+    t = [np.full(phi.shape, np.inf) for _ in range(dim)]
+    for a in range(dim):
+        ax = dim - 1 - a
+        for s in (-1, 1):
+            nb = np.roll(phi, -s, axis=ax)
+            valid = np.ones(phi.shape, bool)
+            idx = [slice(None)] * dim
+            idx[ax] = -1 if s == 1 else 0
+            valid[tuple(idx)] = False
+            with np.errstate(divide="ignore", invalid="ignore"):
+                cand = phi / (phi - nb) * dx
+            use = valid & (phi * nb <= 0) & (cand < t[a])
+            t[a] = np.where(use, cand, t[a])
+    fixed = np.zeros(phi.shape, bool)
+    for a in range(dim):
+        fixed |= np.isfinite(t[a])
+    with np.errstate(divide="ignore"):
+        seed = 1 / np.sqrt(sum((1 / ta) ** 2 for ta in t))
+    ref = upwind_fixed_point(seed, fixed, dx, band)
+    expect = np.where(phi <= 0, -1.0, 1.0) * ref
+    assert np.max(np.abs(out - expect)) <= 1e-12 * dx
+    assert np.max(np.abs(out)) <= band
+    # marked seeds keep |φ| there
+    mark = (np.abs(phi) < 1.5 * dx).astype(np.uint8)
+    out2 = oracle_mod.fast_marching(phi, dx, 20, mark)
+    ref2 = upwind_fixed_point(np.abs(phi), mark.astype(bool), dx, 20 * dx)
+    assert np.max(np.abs(out2 - np.where(phi <= 0, -1.0, 1.0) * ref2)) <= 1e-12 * dx
+
+
+def test_fast_marching_plane_is_exact(oracle_mod):
+    """An axis-aligned plane: the crossing seeds are exact, so are the marched distances
+    (p + dx per cell) up to the band width, which caps the rest."""
+    n, dx = 40, 1.0 / 40
+    x = (np.arange(n) + 0.5) * dx
+    x0 = 0.3137
+    phi = np.broadcast_to((x - x0)[None, None, :], (8, 8, n)).copy() * 3.0  # not a distance function
+    out = oracle_mod.fast_marching(phi, dx, 15)
+    exact = np.broadcast_to((x - x0)[None, None, :], (8, 8, n))
+    inband = np.abs(exact) < 14.5 * dx
+    assert np.max(np.abs(out - exact)[inband]) < 1e-12
+    assert np.all(np.abs(out[~inband]) <= 15 * dx + 1e-15)
+
+
+def test_fast_marching_configuration_steps(oracle_mod):
+    """The fast-marching configuration runs initialize and steps (WENO5 replaced by fast
+    marching over 15 cells); the level set is a distance function near the interface."""
+    sc = scenes.dam_break(3, 20)
+    o = oracle_mod.OracleSim(sc.grid, host_default_config(fast_marching=1))
+    load_scene(o, sc)
+    assert o.initialize() == capi.OK
+    o.stage("restart")
+    for dt in scenes.frame_time_steps(o.max_speed, 3, 25, 1.0, sc.grid.spacing):
+        assert o.advance(dt)["status"] == capi.OK
+    phi = o.download(capi.FIELD_LEVEL_SET).reshape(sc.phi.shape)
+    assert np.all(np.isfinite(phi))
+    assert np.max(np.abs(phi)) <= 15 * sc.grid.spacing * (1 + 1e-12)
