@@ -128,9 +128,11 @@ garm_status allocState(State &s) {
 	GARM_TRY(dalloc(s, &s.nodeDist, size_t(s.NN) * 8));
 	GARM_TRY(dalloc(s, &s.adv, N));
 	GARM_TRY(dalloc(s, &s.vis0, N));
-	GARM_TRY(dalloc(s, &s.vis1, N));
 	GARM_TRY(dalloc(s, &s.fvis0, size_t(s.Ftot)));
-	GARM_TRY(dalloc(s, &s.fvis1, size_t(s.Ftot)));
+	GARM_TRY(dalloc(s, (void **)&s.frontBits, (size_t(s.Ftot) + 31) / 32 * 4));
+	GARM_TRY(dalloc(s, (void **)&s.frontList[0], size_t(s.Ftot) * 4));
+	GARM_TRY(dalloc(s, (void **)&s.frontList[1], size_t(s.Ftot) * 4));
+	GARM_TRY(dalloc(s, (void **)&s.frontCount, size_t(kFrontMaxPasses + 2) * 4));
 	GARM_TRY(dalloc(s, &s.bcList, size_t(s.Ftot) * 8));
 	GARM_TRY(dalloc(s, &s.bcTmp, size_t(s.Ftot) * e));
 	// projection
@@ -413,8 +415,8 @@ garm_status readRecords(State &s, int k, garm_step_stats *S) {
 	garm_status worst = GARM_OK;
 	for (int q = 0; q < k; q++) {
 		const double *rec = s.statsHost + ((s.hostSteps - 1 - q + kStatsCap) % kStatsCap) * kStatsSlots;
-		if (rec[kStCgErr] != 0 || rec[kStMarchErr] == 1) return GARM_TIMEOUT;
-		if (rec[kStMarchErr] != 0) return GARM_NUMERIC;
+		if (rec[kStCgErr] != 0 || rec[kStPersistErr] == 1) return GARM_TIMEOUT;
+		if (rec[kStPersistErr] != 0) return GARM_NUMERIC;
 		if (rec[kStUnknowns] > 0 && !(rec[kStCgResidual] <= rec[kStCgTol])) worst = GARM_NOT_CONVERGED;
 	}
 	if (S) {
@@ -650,6 +652,8 @@ garm_status garm_sim_create(const garm_grid_desc *gd, const garm_config *cfg, vo
 	if (c.record_volume != 0 && c.record_volume != 1) return GARM_INVALID;
 	if (c.restart_newton != 0 && c.restart_newton != 1) return GARM_INVALID;
 	if (c.fast_marching != 0 && c.fast_marching != 1) return GARM_INVALID;
+	// extrapolation passes are counted in a level byte
+	if (!(c.boundary_extrap_radius <= 240.0) || !(c.air_extrap_radius <= 240.0)) return GARM_INVALID;
 
 	garm_sim *sim = new (std::nothrow) garm_sim();
 	if (!sim) return GARM_OOM;

@@ -8,6 +8,8 @@
 //   GridBasedData::normMax                   (Source/Core/GridBasedData.h:55-68)
 #include "garm_internal.h"
 
+#include <algorithm>
+
 namespace garm {
 
 // ---------------------------------------------------------------------------
@@ -181,175 +183,281 @@ garm_status finishBoundary(State &s) {
 }
 
 // ---------------------------------------------------------------------------
-// Extrapolation passes.  Values are updated in place: a pass reads only cells
-// already in the visited set and writes only cells outside it, so it has the
-// reference's Jacobi semantics; the visited mask is double-buffered.
+// Extrapolation (Extrapolation.h:42-218) as a frontier march.
+//
+// The reference runs maxSteps Jacobi passes over the whole grid.  In pass p, every cell
+// outside the visited set that has a visited neighbour becomes the mean of its visited
+// neighbours, taken in the order -x,+x,-y,+y,-z,+z (Grid.h:59-60), and joins the set.  The
+// cells that change in pass p are exactly the unvisited neighbours of the cells that joined
+// in pass p-1 (of the seeds, for p = 1).  So one cooperative launch keeps that frontier as
+// a list and touches only it:
+//   phase A (all elements): seed levels, and the final value of elements that may never be
+//           reached (ξ = x, u = 0, advRegion = 0); those values are never read before the
+//           element joins and overwrites them;
+//   phase B (all elements): the first frontier, the unvisited neighbours of seeds;
+//   pass p (one small launch over the frontier): each frontier element takes the mean of
+//           its neighbours with level < p, sets its level to p and queues its unvisited
+//           neighbours (each element once, by a bit claimed with atomicOr) as the frontier
+//           of pass p+1.
+// level = 0 for seeds, p for elements that joined in pass p, 255 otherwise.  A pass reads
+// only neighbours with level < p, which no thread of that pass writes, so the passes keep
+// the reference's Jacobi semantics; the values and the summation order are the reference's,
+// and the result does not depend on the list order.
 // ---------------------------------------------------------------------------
-enum FixedKind { kFixedCellDistPos = 0, kFixedAdvPos = 1, kFixedOriNonPos = 2 };
+enum FrontKind { kFrontCollider = 0, kFrontRefMap = 1, kFrontAdv = 2, kFrontFaces = 3 };
+
+constexpr int kFrontElemsPerBlock = 32768;  // grid elements per block of the pass launch
 
 template <typename T>
-__global__ void kCellMask(int64_t N, int kind, const T *cellDist, const uint8_t *adv, const T *ori, uint8_t *vis, const int *gate) {
-	if (gate && !*gate) return;
-	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-	if (id >= N) return;
-	bool f;
-	if (kind == kFixedCellDistPos) f = cellDist[id] > T(0);
-	else if (kind == kFixedAdvPos) f = adv[id] > 0;
-	else f = ori[id] <= T(0);
-	vis[id] = f ? 1 : 0;
+struct FrontArgs {
+	Geom geom;
+	int nsub;              // sub-grids: 1 (cells) or D (face grids)
+	int off[4];            // first element of each sub-grid (off[nsub] = total)
+	int size[3][3];        // sub-grid sizes
+	T *val[3];             // collider: ori, φ; reference map: ξ components; faces: u per axis
+	uint8_t *flag;         // advRegion
+	const T *cellDist, *ori, *fr[3];
+	const uint8_t *adv;
+	uint8_t *level;
+	unsigned *bits;        // queued-once bits, one per element
+	int *list[2];          // frontier of pass p in list[p & 1]
+	int *count;            // [p]: frontier size of pass p
+	int passes;
+};
+
+struct FrontPos { int sub, local, i, j, k; };
+
+template <int D, typename T>
+__device__ __forceinline__ FrontPos frontPos(const FrontArgs<T> &a, int gid) {
+	FrontPos p;
+	p.sub = 0;
+	if (a.nsub > 1 && gid >= a.off[1]) p.sub = (a.nsub > 2 && gid >= a.off[2]) ? 2 : 1;
+	p.local = gid - a.off[p.sub];
+	const unsigned sx = unsigned(a.size[p.sub][0]), r = unsigned(p.local) / sx;
+	p.i = p.local - int(r * sx);
+	if (D == 2) { p.j = int(r); p.k = 0; }
+	else { const unsigned sy = unsigned(a.size[p.sub][1]); const unsigned q = r / sy; p.j = int(r - q * sy); p.k = int(q); }
+	return p;
 }
 
-// Kind 0: NS scalar planes (cell double, Extrapolation.h:86-126)
-// Kind 1: D-vector reference map; unreached cells get their position (Extrapolation.h:176-218)
-// Kind 2: flag (uchar) (Extrapolation.h:128-174)
-// Neighbours are visited in the reference's order -x,+x,-y,+y,-z,+z (Grid.h:59-60).
-template <int D, typename T, int Kind, int NS>
-__global__ void __launch_bounds__(kBlock) kExtrapCellPass(Geom geom, T *f0, T *f1, T *f2, uint8_t *flag, const uint8_t *__restrict__ vis0, uint8_t *vis1, const int *gate) {
-	if (gate && !*gate) return;
-	const int sx = geom.n[0], sy = geom.n[1], sz = D == 3 ? geom.n[2] : 1;
-	const int N = sx * sy * sz;
-	const int id = int(blockIdx.x) * blockDim.x + threadIdx.x;
-	if (id >= N) return;
-	if (vis0[id]) { vis1[id] = 1; return; }
-	const unsigned r = unsigned(id) / unsigned(sx);
-	const int i = id - int(r) * sx;
-	const int j = D == 3 ? int(r % unsigned(sy)) : int(r);
-	const int k = D == 3 ? int(r / unsigned(sy)) : 0;
-	const int sxy = sx * sy;
-	const int off[6] = {-1, 1, -sx, sx, -sxy, sxy};
-	const bool ok[6] = {i > 0, i < sx - 1, j > 0, j < sy - 1, k > 0, k < sz - 1};
-	int cnt = 0;
-	T s0 = T(0), s1 = T(0), s2 = T(0);
+// Neighbour q (-x,+x,-y,+y,-z,+z) of an element in its own sub-grid, or -1 outside it.
+template <int D, typename T>
+__device__ __forceinline__ int frontNeighbour(const FrontArgs<T> &a, const FrontPos &p, int gid, int q) {
+	const int sx = a.size[p.sub][0], sy = a.size[p.sub][1], sz = D == 3 ? a.size[p.sub][2] : 1;
+	switch (q) {
+	case 0: return p.i > 0 ? gid - 1 : -1;
+	case 1: return p.i < sx - 1 ? gid + 1 : -1;
+	case 2: return p.j > 0 ? gid - sx : -1;
+	case 3: return p.j < sy - 1 ? gid + sx : -1;
+	case 4: return p.k > 0 ? gid - sx * sy : -1;
+	default: return p.k < sz - 1 ? gid + sx * sy : -1;
+	}
+}
+
+__device__ __forceinline__ uint8_t ldLevel(const uint8_t *p) { return *(const volatile uint8_t *)p; }
+
+// Appends this lane's `n` entries (ids[0..n)) to list/count with one atomic per warp.
+// Every lane of the warp must call it.
+__device__ __forceinline__ void warpAppend(int *list, int *count, const int *ids, int n) {
+	const unsigned lane = threadIdx.x & 31;
+	int incl = n;
 #pragma unroll
-	for (int q = 0; q < 2 * D; q++) {
-		if (!ok[q]) continue;
-		const int n = id + off[q];
-		if (!vis0[n]) continue;
-		cnt++;
-		if (Kind == 0) { s0 += f0[n]; if (NS > 1) s1 += f1[n]; }
-		else if (Kind == 1) { s0 += f0[n]; s1 += f1[n]; if (D == 3) s2 += f2[n]; }
+	for (int o = 1; o < 32; o <<= 1) {
+		const int v = __shfl_up_sync(0xffffffffu, incl, o);
+		if (lane >= unsigned(o)) incl += v;
 	}
-	if (cnt > 0) {
-		const T c = T(cnt);
-		if (Kind == 0) { f0[id] = s0 / c; if (NS > 1) f1[id] = s1 / c; }
-		else if (Kind == 1) { f0[id] = s0 / c; f1[id] = s1 / c; if (D == 3) f2[id] = s2 / c; }
-		else flag[id] = 1;
-		vis1[id] = 1;
-	} else {
-		if (Kind == 1) {
-			const G<D, T> g = cellGrid<D, T>(geom);
-			f0[id] = g.pos(0, i); f1[id] = g.pos(1, j); if (D == 3) f2[id] = g.pos(2, k);
-		}
-		vis1[id] = 0;
-	}
+	const int total = __shfl_sync(0xffffffffu, incl, 31);
+	int base = 0;
+	if (lane == 31 && total > 0) base = atomicAdd(count, total);
+	base = __shfl_sync(0xffffffffu, base, 31);
+	const int start = base + incl - n;
+	for (int q = 0; q < n; q++) list[start + q] = ids[q];
 }
 
-__global__ void kFlagFinal(int64_t N, uint8_t *flag, const uint8_t *vis0) {
-	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-	if (id < N && !vis0[id]) flag[id] = 0;
+// Claims element `nb` for the next frontier; true when this thread set its bit.
+__device__ __forceinline__ bool claim(unsigned *bits, int nb) {
+	const unsigned m = 1u << (nb & 31);
+	return (atomicOr(bits + (nb >> 5), m) & m) == 0;
 }
 
-template <typename T>
-__global__ void kAdvFromOri(int64_t N, const T *ori, uint8_t *adv) {
-	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-	if (id < N) adv[id] = ori[id] <= T(0) ? 1 : 0;
-}
-
-// Liquid faces of extrapolateFieldsToAir (LevelSetLiquid.cpp:1074-1082)
+// Seed test of a face: a liquid face of extrapolateFieldsToAir (LevelSetLiquid.cpp:1074-1082),
+// fraction < 1 and the level set <= 0 in one of the two cells beside it.
 template <int D, typename T>
-__global__ void kFaceMask(Geom geom, const T *fr0, const T *fr1, const T *fr2, const T *ori, uint8_t *vis, int64_t F0, int64_t F1, int64_t Ftot) {
-	int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-	if (id >= Ftot) return;
-	const int64_t gid = id;
-	int axis = 0;
-	if (id >= F0) { id -= F0; axis = 1; if (id >= F1) { id -= F1; axis = 2; } }
-	const T *fr = axis == 0 ? fr0 : (axis == 1 ? fr1 : fr2);
-	uint8_t m = 0;
-	if (fr[id] < T(1)) {
-		const G<D, T> fg = faceGrid<D, T>(geom, axis);
-		const G<D, T> cg = cellGrid<D, T>(geom);
-		int i, j, k; fg.coord(id, i, j, k);
-		const int i0 = i - (axis == 0), j0 = j - (axis == 1), k0 = k - (axis == 2);
-		if (cg.valid(i, j, k) && cg.valid(i0, j0, k0))  // always true for interior faces (fraction < 1)
-			m = (ori[cg.idx(i0, j0, k0)] <= T(0) || ori[cg.idx(i, j, k)] <= T(0)) ? 1 : 0;
-	}
-	vis[gid] = m;
+__device__ __forceinline__ bool liquidFace(const FrontArgs<T> &a, const FrontPos &p) {
+	if (!(a.fr[p.sub][p.local] < T(1))) return false;
+	const G<D, T> cg = cellGrid<D, T>(a.geom);
+	const int axis = p.sub;
+	const int i0 = p.i - (axis == 0), j0 = p.j - (axis == 1), k0 = p.k - (axis == 2);
+	if (!cg.valid(p.i, p.j, p.k) || !cg.valid(i0, j0, k0)) return false;  // never for interior faces (fraction < 1)
+	return a.ori[cg.idx(i0, j0, k0)] <= T(0) || a.ori[cg.idx(p.i, p.j, p.k)] <= T(0);
 }
 
-template <int D, typename T>
-__global__ void __launch_bounds__(kBlock) kExtrapFacePass(Geom geom, T *u0, T *u1, T *u2, const uint8_t *__restrict__ vis0, uint8_t *vis1, int64_t F0, int64_t F1, int64_t Ftot) {
+// Phase A: levels and the values of elements that may never be reached; the queued bits
+// and the frontier sizes start at zero (kernel stores, not memset nodes, which serialise
+// concurrent scenes' graphs).
+template <int D, typename T, int Kind>
+__global__ void __launch_bounds__(kBlock) kFrontSeed(FrontArgs<T> a, const int *gate) {
+	if (gate && !*gate) return;
 	const int gid = int(blockIdx.x) * blockDim.x + threadIdx.x;
-	if (gid >= int(Ftot)) return;
-	if (vis0[gid]) { vis1[gid] = 1; return; }
-	int id = gid, axis = 0, base = 0;
-	if (id >= int(F0)) { id -= int(F0); axis = 1; base = int(F0); if (id >= int(F1)) { id -= int(F1); axis = 2; base = int(F0 + F1); } }
-	const int sx = geom.n[0] + (axis == 0), sy = geom.n[1] + (axis == 1), sz = D == 3 ? geom.n[2] + (axis == 2) : 1;
-	T *u = axis == 0 ? u0 : (axis == 1 ? u1 : u2);
-	const unsigned r = unsigned(id) / unsigned(sx);
-	const int i = id - int(r) * sx;
-	const int j = D == 3 ? int(r % unsigned(sy)) : int(r);
-	const int k = D == 3 ? int(r / unsigned(sy)) : 0;
-	const int sxy = sx * sy;
-	const int off[6] = {-1, 1, -sx, sx, -sxy, sxy};
-	const bool ok[6] = {i > 0, i < sx - 1, j > 0, j < sy - 1, k > 0, k < sz - 1};
-	int cnt = 0; T s = T(0);
-#pragma unroll
-	for (int q = 0; q < 2 * D; q++) {
-		if (!ok[q]) continue;
-		const int n = id + off[q];
-		if (!vis0[base + n]) continue;
-		cnt++; s += u[n];
+	if (gid < (a.off[a.nsub] + 31) / 32) a.bits[gid] = 0u;
+	if (gid < a.passes + 2) a.count[gid] = 0;
+	if (gid >= a.off[a.nsub]) return;
+	bool seed;
+	if (Kind == kFrontCollider) seed = a.cellDist[gid] > T(0);
+	else if (Kind == kFrontRefMap) {
+		seed = a.adv[gid] > 0;
+		if (!seed) {
+			const FrontPos p = frontPos<D, T>(a, gid);
+			const G<D, T> g = cellGrid<D, T>(a.geom);
+			a.val[0][gid] = g.pos(0, p.i); a.val[1][gid] = g.pos(1, p.j); if (D == 3) a.val[2][gid] = g.pos(2, p.k);
+		}
+	} else if (Kind == kFrontAdv) {
+		seed = a.ori[gid] <= T(0);
+		a.flag[gid] = seed ? 1 : 0;
+	} else {
+		const FrontPos p = frontPos<D, T>(a, gid);
+		seed = liquidFace<D, T>(a, p);
+		if (!seed) a.val[p.sub][p.local] = T(0);
 	}
-	if (cnt > 0) { u[id] = s / T(cnt); vis1[gid] = 1; }
-	else { u[id] = T(0); vis1[gid] = 0; }
+	a.level[gid] = seed ? 0 : 255;
 }
 
-template <int D, typename T, int Kind, int NS>
-static garm_status cellExtrap(State &s, T *f0, T *f1, T *f2, uint8_t *flag, int passes) {
-	uint8_t *v0 = s.vis0, *v1 = s.vis1;
-	for (int it = 0; it < passes; it++) {
-		kExtrapCellPass<D, T, Kind, NS><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, f0, f1, f2, flag, v0, v1, s.gate); s.launches++;
-		uint8_t *t = v0; v0 = v1; v1 = t;
+// Phase B: the first frontier, the unvisited neighbours of seeds.
+template <int D, typename T>
+__global__ void __launch_bounds__(kBlock) kFrontFirst(FrontArgs<T> a, const int *gate) {
+	if (gate && !*gate) return;
+	const int total = a.off[a.nsub];
+	const int gid = int(blockIdx.x) * blockDim.x + threadIdx.x;
+	int ids[1];
+	int n = 0;
+	if (gid < total && a.level[gid] == 255) {
+		const FrontPos p = frontPos<D, T>(a, gid);
+		bool touch = false;
+#pragma unroll
+		for (int q = 0; q < 2 * D; q++) {
+			const int nb = frontNeighbour<D, T>(a, p, gid, q);
+			if (nb >= 0 && a.level[nb] == 0) touch = true;
+		}
+		if (touch && claim(a.bits, gid)) ids[n++] = gid;
 	}
-	GARM_CHECK_LAUNCH();
-	if (Kind == 2) { kFlagFinal<<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, flag, v0); s.launches++; GARM_CHECK_LAUNCH(); }
-	return GARM_OK;
+	warpAppend(a.list[1], a.count + 1, ids, n);
+}
+
+// Pass `pass`: every element of its frontier joins; its unvisited neighbours form the next
+// frontier.  A small grid strides over the frontier, whose size is on the device.
+template <int D, typename T, int Kind>
+__global__ void __launch_bounds__(kBlock) kFrontPass(FrontArgs<T> a, int pass, const int *gate) {
+	if (gate && !*gate) return;
+	const int stride = int(gridDim.x) * blockDim.x;
+	const int n = a.count[pass];
+	const int *cur = a.list[pass & 1];
+	int *next = a.list[(pass + 1) & 1];
+	for (int base = int(blockIdx.x) * blockDim.x; base < n; base += stride) {
+		const int t = base + int(threadIdx.x);
+		int ids[6];
+		int m = 0;
+		if (t < n) {
+			const int gid = cur[t];
+			const FrontPos p = frontPos<D, T>(a, gid);
+			int nbs[6];
+			int cnt = 0;
+			T s0 = T(0), s1 = T(0), s2 = T(0);
+#pragma unroll
+			for (int q = 0; q < 2 * D; q++) {
+				nbs[q] = frontNeighbour<D, T>(a, p, gid, q);
+				if (nbs[q] < 0 || ldLevel(a.level + nbs[q]) >= pass) continue;
+				cnt++;
+				if (Kind == kFrontCollider) { s0 += a.val[0][nbs[q]]; s1 += a.val[1][nbs[q]]; }
+				else if (Kind == kFrontRefMap) { s0 += a.val[0][nbs[q]]; s1 += a.val[1][nbs[q]]; if (D == 3) s2 += a.val[2][nbs[q]]; }
+				else if (Kind == kFrontFaces) s0 += a.val[p.sub][nbs[q] - a.off[p.sub]];
+			}
+			// cnt > 0: every frontier element neighbours an element that joined in the previous pass
+			const T c = T(cnt);
+			if (Kind == kFrontCollider) { a.val[0][gid] = s0 / c; a.val[1][gid] = s1 / c; }
+			else if (Kind == kFrontRefMap) { a.val[0][gid] = s0 / c; a.val[1][gid] = s1 / c; if (D == 3) a.val[2][gid] = s2 / c; }
+			else if (Kind == kFrontAdv) a.flag[gid] = 1;
+			else a.val[p.sub][p.local] = s0 / c;
+			*(volatile uint8_t *)(a.level + gid) = uint8_t(pass);
+			if (pass < a.passes) {
+#pragma unroll
+				for (int q = 0; q < 2 * D; q++)
+					if (nbs[q] >= 0 && ldLevel(a.level + nbs[q]) == 255 && claim(a.bits, nbs[q])) ids[m++] = nbs[q];
+			}
+		}
+		warpAppend(next, a.count + pass + 1, ids, m);
+	}
 }
 
 static inline int passCount(double r) { int n = 0; while (n < r) n++; return n; }  // `for (iter = 0; iter < maxSteps; ...)`
 
-template <int D, typename T>
-garm_status extrapolateToCollider(State &s) {
-	kCellMask<T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, kFixedCellDistPos, (const T *)s.cellDist, s.adv, (const T *)s.ori, s.vis0, s.gate); s.launches++;
+template <int D, typename T, int Kind>
+static garm_status front(State &s, int passes) {
+	FrontArgs<T> a{};
+	a.geom = s.geom;
+	if (Kind == kFrontFaces) {
+		a.nsub = D;
+		int o = 0;
+		for (int ax = 0; ax < D; ax++) {
+			a.off[ax] = o;
+			for (int b = 0; b < 3; b++) a.size[ax][b] = s.geom.n[b] + (b == ax ? 1 : 0);
+			if (D == 2) a.size[ax][2] = 1;
+			o += int(s.F[ax]);
+			a.val[ax] = (T *)s.u[ax];
+			a.fr[ax] = (const T *)s.fraction[ax];
+		}
+		a.off[D] = o;
+		a.level = s.fvis0;
+	} else {
+		a.nsub = 1;
+		a.off[0] = 0;
+		a.off[1] = int(s.N);
+		for (int b = 0; b < 3; b++) a.size[0][b] = s.geom.n[b];
+		if (D == 2) a.size[0][2] = 1;
+		a.level = s.vis0;
+		if (Kind == kFrontCollider) { a.val[0] = (T *)s.ori; a.val[1] = (T *)s.phi; }
+		if (Kind == kFrontRefMap) for (int c = 0; c < D; c++) a.val[c] = (T *)s.xi[c];
+	}
+	a.flag = s.adv;
+	a.adv = s.adv;
+	a.cellDist = (const T *)s.cellDist;
+	a.ori = (const T *)s.ori;
+	a.bits = s.frontBits;
+	a.list[0] = s.frontList[0];
+	a.list[1] = s.frontList[1];
+	a.count = s.frontCount;
+	a.passes = passes;
+	if (passes > kFrontMaxPasses) return GARM_INVALID;
+	const int total = a.off[a.nsub];
+	const int *gate = s.gate;
+	kFrontSeed<D, T, Kind><<<gridFor(total), kBlock, 0, s.stream>>>(a, gate); s.launches++;
 	GARM_CHECK_LAUNCH();
-	// ori and φ share the fixed set cellDist > 0, so one pass extrapolates both
-	return cellExtrap<D, T, 0, 2>(s, (T *)s.ori, (T *)s.phi, nullptr, nullptr, passCount(s.cfg.boundary_extrap_radius));
-}
-
-template <int D, typename T>
-garm_status extrapolateToAir(State &s) {
-	const int R = passCount(s.cfg.air_extrap_radius);
-	// ξ from cells with advRegion > 0
-	kCellMask<T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, kFixedAdvPos, (const T *)s.cellDist, s.adv, (const T *)s.ori, s.vis0, s.gate); s.launches++;
+	if (passes <= 0) return GARM_OK;
+	kFrontFirst<D, T><<<gridFor(total), kBlock, 0, s.stream>>>(a, gate); s.launches++;
 	GARM_CHECK_LAUNCH();
-	GARM_TRY((cellExtrap<D, T, 1, 1>(s, (T *)s.xi[0], (T *)s.xi[1], (T *)(D == 3 ? s.xi[2] : nullptr), nullptr, R)));
-	// advRegion = (ori <= 0), then dilate
-	kAdvFromOri<T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, (const T *)s.ori, s.adv); s.launches++;
-	kCellMask<T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, kFixedOriNonPos, (const T *)s.cellDist, s.adv, (const T *)s.ori, s.vis0, s.gate); s.launches++;
-	GARM_CHECK_LAUNCH();
-	GARM_TRY((cellExtrap<D, T, 2, 1>(s, nullptr, nullptr, nullptr, s.adv, R)));
-	// velocity, airExtrapolationRadius + 2 passes
-	kFaceMask<D, T><<<gridFor(s.Ftot), kBlock, 0, s.stream>>>(s.geom, (const T *)s.fraction[0], (const T *)s.fraction[1], (const T *)s.fraction[2],
-		(const T *)s.ori, s.fvis0, s.F[0], s.F[1], s.Ftot); s.launches++;
-	GARM_CHECK_LAUNCH();
-	uint8_t *v0 = s.fvis0, *v1 = s.fvis1;
-	const int Ru = passCount(s.cfg.air_extrap_radius + 2);
-	for (int it = 0; it < Ru; it++) {
-		kExtrapFacePass<D, T><<<gridFor(s.Ftot), kBlock, 0, s.stream>>>(s.geom, (T *)s.u[0], (T *)s.u[1], (T *)s.u[2], v0, v1, s.F[0], s.F[1], s.Ftot); s.launches++;
-		uint8_t *t = v0; v0 = v1; v1 = t;
+	// the frontiers are thin shells: at most one block per SM, fewer for small grids
+	const unsigned blocks = unsigned(std::max<int64_t>(1, std::min<int64_t>((int64_t(total) + kFrontElemsPerBlock - 1) / kFrontElemsPerBlock, s.numSMs)));
+	for (int pass = 1; pass <= passes; pass++) {
+		kFrontPass<D, T, Kind><<<blocks, kBlock, 0, s.stream>>>(a, pass, gate); s.launches++;
 	}
 	GARM_CHECK_LAUNCH();
 	return GARM_OK;
+}
+
+// extrapolateFieldsToCollider (LevelSetLiquid.cpp:1086-1117): ori and φ from cellDist > 0.
+template <int D, typename T>
+garm_status extrapolateToCollider(State &s) {
+	return front<D, T, kFrontCollider>(s, passCount(s.cfg.boundary_extrap_radius));
+}
+
+// extrapolateFieldsToAir (LevelSetLiquid.cpp:1059-1084): ξ from advRegion > 0 (unreached
+// cells get ξ = x); advRegion = (ori <= 0) dilated (unreached cells 0); u from the liquid
+// faces over airExtrapolationRadius + 2 passes (unreached faces 0).
+template <int D, typename T>
+garm_status extrapolateToAir(State &s) {
+	const int R = passCount(s.cfg.air_extrap_radius);
+	GARM_TRY((front<D, T, kFrontRefMap>(s, R)));
+	GARM_TRY((front<D, T, kFrontAdv>(s, R)));
+	return front<D, T, kFrontFaces>(s, passCount(s.cfg.air_extrap_radius + 2));
 }
 
 // ---------------------------------------------------------------------------
@@ -471,10 +579,15 @@ __global__ void kStepDt(const unsigned long long *maxBits, double dx, double *cl
 	if (rec) rec[kStDt] = d;
 }
 
+__global__ void kClearWords(unsigned *a, int na, unsigned *b, int nb) {
+	const int t = int(threadIdx.x);
+	if (t < na) a[t] = 0u;
+	if (t < nb) b[t] = 0u;
+}
+
 template <int D, typename T>
 garm_status maxSpeedAsync(State &s) {
-	cudaError_t e = cudaMemsetAsync(s.redU64, 0, sizeof(unsigned long long), s.stream);
-	if (e != cudaSuccess) return GARM_CUDA_ERROR;
+	kClearWords<<<1, 32, 0, s.stream>>>((unsigned *)s.redU64, 2, nullptr, 0); s.launches++;
 	const unsigned nb = unsigned(s.numSMs > 0 ? s.numSMs * 8 : 1024);
 	kMaxAbs<T><<<nb, kBlock, 0, s.stream>>>((const T *)s.u[0], (const T *)s.u[1], (const T *)(D == 3 ? s.u[2] : s.u[0]), s.F[0], s.F[1], s.Ftot, s.redU64); s.launches++;
 	GARM_CHECK_LAUNCH();

@@ -54,8 +54,12 @@ struct State {
 	unsigned *marchBar = nullptr;
 	int *marchInts = nullptr;
 	uint8_t *adv = nullptr;    // _advRegion
-	uint8_t *vis0 = nullptr, *vis1 = nullptr;       // cell extrapolation masks
-	uint8_t *fvis0 = nullptr, *fvis1 = nullptr;     // face extrapolation masks (all axes, concatenated)
+	uint8_t *vis0 = nullptr;   // cell extrapolation levels (seed 0, joined in pass p, 255 unreached)
+	uint8_t *fvis0 = nullptr;  // face extrapolation levels (all axes, concatenated)
+	// frontier extrapolation: queued-once bits, the two frontier lists, per-pass sizes
+	unsigned *frontBits = nullptr;
+	int *frontList[2] = {};
+	int *frontCount = nullptr;
 	// boundary (Boundary<Dim>, Source/Core/Boundary.h:16-24)
 	void *cellDist = nullptr, *nodeDist = nullptr;
 	void *fraction[3] = {}, *bvel[3] = {}, *normal[3] = {};
@@ -122,7 +126,7 @@ __device__ __forceinline__ double *stepRecord(double *base, const unsigned long 
 }
 
 // Layout of one per-step statistics record on the device.
-enum StatSlot { kStDt = 0, kStRestarted, kStRmTotal, kStRmBad, kStUnknowns, kStCgIters, kStCgRefine, kStCgResidual, kStCgTol, kStCgErr, kStVolume, kStMarchErr, kStatsSlots = 12 };
+enum StatSlot { kStDt = 0, kStRestarted, kStRmTotal, kStRmBad, kStUnknowns, kStCgIters, kStCgRefine, kStCgResidual, kStCgTol, kStCgErr, kStVolume, kStPersistErr, kStatsSlots = 12 };
 
 // Stage entry points (templated on dimension D and working type T).
 template <int D, typename T> garm_status initBoundary(State &s);
@@ -149,6 +153,7 @@ template <int D, typename T> garm_status project(State &s, garm_step_stats *st);
 template <int D, typename T> garm_status projectAsync(State &s, bool record);
 garm_status projectStats(State &s, garm_step_stats *st);
 template <int D, typename T> garm_status extrapolateToAir(State &s);
+constexpr int kFrontMaxPasses = 250;  // extrapolation passes fit a level byte (255 = unreached)
 template <int D, typename T> garm_status enforceBoundaryConditions(State &s);
 template <int D, typename T> garm_status enforceBoundaryLevelSet(State &s, void *field, double tol);
 template <int D, typename T> garm_status resetRefView(State &s);
@@ -164,6 +169,10 @@ template <int D, typename T> garm_status fastMarch(State &s, void *phi, const ui
 garm_status marchStatus(State &s, int *sweeps);
 template <int D, typename T> garm_status maxSpeed(State &s, double *out);
 template <int D, typename T> garm_status maxSpeedAsync(State &s);
+// Zeroes the first na words of a and nb words of b (one block of 32 threads).  Steps clear
+// their counters with this kernel, not with memset nodes: memset nodes of concurrently
+// replayed step graphs serialise against each other.
+__global__ void kClearWords(unsigned *a, int na, unsigned *b, int nb);
 __global__ void kStepDt(const unsigned long long *maxBits, double dx, double *clock, double *dt, double *stats, const unsigned long long *counter);
 template <int D, typename T> garm_status copyField(State &s, void *dst, const void *src, int64_t n);
 

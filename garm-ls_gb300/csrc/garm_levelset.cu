@@ -835,8 +835,7 @@ __global__ void kRestartDecision(const int *counts, double ratio, int *flag, dou
 // Counts and decision on the device, no host synchronisation.
 template <int D, typename T>
 garm_status checkReferenceMapAsync(State &s, bool record) {
-	cudaError_t e = cudaMemsetAsync(s.redI32, 0, 2 * sizeof(int), s.stream);
-	if (e != cudaSuccess) return GARM_CUDA_ERROR;
+	kClearWords<<<1, 32, 0, s.stream>>>((unsigned *)s.redI32, 2, nullptr, 0); s.launches++;
 	PiPtrs<D, T> pp{};
 	for (int q = 0; q < D * D; q++) pp.p[q] = (const T *)s.Pi[q];
 	kCheckRefMap<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.N, (const T *)s.ori, (const T *)s.cellDist, pp,

@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(kMarchBlock) kMarch(Geom geom, T *tentA, T *te
 		if (!converged && *(volatile int *)err == 0) atomicExch(err, 2);
 		const int code = *(volatile int *)err;
 		double *rec = stepRecord(ctl.stats, ctl.counter);
-		if (rec && code) rec[kStMarchErr] = code;
+		if (rec && code) rec[kStPersistErr] = code;
 	}
 }
 
@@ -190,8 +190,8 @@ garm_status fastMarch(State &s, void *phiPlane, const uint8_t *mark, int maxStep
 	else kMarchSeedSigns<D, T><<<nb, kBlock, 0, s.stream>>>(s.geom, phi, tent, tent2, s.marchFixed, band, s.gate);
 	s.launches++;
 	GARM_CHECK_LAUNCH();
-	cudaError_t e = cudaMemsetAsync(s.marchBar, 0, 2 * sizeof(unsigned), s.stream);
-	if (e == cudaSuccess) e = cudaMemsetAsync(s.marchInts, 0, 8 * sizeof(int), s.stream);
+	kClearWords<<<1, 32, 0, s.stream>>>(s.marchBar, 2, (unsigned *)s.marchInts, 8); s.launches++;
+	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return GARM_CUDA_ERROR;
 	int perSM = 0;
 	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kMarch<D, T>, kMarchBlock, 0);

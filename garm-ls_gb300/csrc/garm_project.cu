@@ -861,8 +861,8 @@ garm_status projectAsync(State &s, bool record) {
 	a.drop = s.cfg.mixed_residual_drop; a.replaceEvery = s.cfg.mixed_replace_interval;
 	a.scal = s.cgScalars; a.ints = s.cgInts;
 
-	cudaError_t e = cudaMemsetAsync(s.barrier, 0, 2 * sizeof(unsigned), s.stream);
-	if (e == cudaSuccess) e = cudaMemsetAsync(s.cgInts, 0, 8 * sizeof(int), s.stream);
+	kClearWords<<<1, 32, 0, s.stream>>>(s.barrier, 2, (unsigned *)s.cgInts, 8); s.launches++;
+	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return GARM_CUDA_ERROR;
 
 	void *kfn;
