@@ -392,6 +392,75 @@ __device__ __forceinline__ T rkUpdate(T f, T rawSum, T k, T dx, T dt, const T *b
 	return fma(adv, T(2), base[id]) * T(1.0 / 3.0);
 }
 
+// ---- Paired FP32 evaluation (FFMA2 / FADD2 / FMUL2 of sm_100 and later): the column form
+// evaluates the two in-plane axes of a 3D cell as the two lanes of one float2, so each
+// paired instruction does the work of two.  Same formulas as wenoCell / godunovSq; the
+// constants are folded into fma forms, so the lanes round differently from the scalar FP32
+// code (not from each other).
+struct F2 { float2 v; };
+__device__ __forceinline__ F2 f2(float a) { return {make_float2(a, a)}; }
+__device__ __forceinline__ F2 f2(float a, float b) { return {make_float2(a, b)}; }
+__device__ __forceinline__ F2 add2(F2 a, F2 b) { return {__fadd2_rn(a.v, b.v)}; }
+__device__ __forceinline__ F2 mul2(F2 a, F2 b) { return {__fmul2_rn(a.v, b.v)}; }
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) { return {__ffma2_rn(a.v, b.v, c.v)}; }
+__device__ __forceinline__ F2 sub2(F2 a, F2 b) { return fma2(b, f2(-1.f), a); }  // a - b, exact as a subtraction
+__device__ __forceinline__ F2 maxNonNeg2(F2 a, F2 b) { return f2(maxNonNeg(a.v.x, b.v.x), maxNonNeg(a.v.y, b.v.y)); }
+__device__ __forceinline__ F2 pow2NegExp2(F2 a) { return f2(pow2NegExp(a.v.x), pow2NegExp(a.v.y)); }
+// -1/x per lane: the hardware approximation and one Newton–Raphson step y(2 - x y)
+// (Muller et al., Handbook of Floating-Point Arithmetic, ch. 4), with the sign folded
+// into the step: y·(x y - 2).  Only the square of the quotient is used.
+__device__ __forceinline__ F2 negRecip2(F2 x) {
+	float a, b;
+	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(a) : "f"(x.v.x));
+	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(b) : "f"(x.v.y));
+	const F2 y = f2(a, b);
+	return mul2(y, fma2(x, y, f2(-2.f)));
+}
+struct Ratio2 { F2 num, den; };
+__device__ __forceinline__ F2 smoothG2(F2 a, F2 b, F2 c) { const F2 e = add2(fma2(b, f2(-2.f), a), c); return mul2(mul2(e, f2(float(13.0 / 3.0))), e); }
+__device__ __forceinline__ F2 smoothL2(F2 g, F2 a, F2 b, F2 c) { const F2 f = fma2(c, f2(3.f), fma2(b, f2(-4.f), a)); return fma2(f, f, g); }
+__device__ __forceinline__ F2 smoothM2(F2 g, F2 a, F2 c) { const F2 f = sub2(a, c); return fma2(f, f, g); }
+__device__ __forceinline__ F2 smoothR2(F2 g, F2 a, F2 b, F2 c) { const F2 f = fma2(b, f2(-4.f), fma2(a, f2(3.f), c)); return fma2(f, f, g); }
+__device__ __forceinline__ F2 stencil1_2(F2 a, F2 b, F2 c) { return fma2(a, f2(2.f), fma2(b, f2(-7.f), mul2(c, f2(11.f)))); }
+__device__ __forceinline__ F2 stencil2_2(F2 a, F2 b, F2 c) { return fma2(a, f2(-1.f), fma2(b, f2(5.f), mul2(c, f2(2.f)))); }
+__device__ __forceinline__ F2 stencil3_2(F2 a, F2 b, F2 c) { return fma2(c, f2(-1.f), fma2(b, f2(5.f), mul2(a, f2(2.f)))); }
+struct FaceWeights2 { F2 a, b, c; };
+__device__ __forceinline__ FaceWeights2 faceWeights2(F2 s1, F2 s2, F2 s3, F2 eps) {
+	const F2 sc = pow2NegExp2(eps);
+	const F2 q1 = mul2(add2(s1, eps), sc), q2 = mul2(add2(s2, eps), sc), q3 = mul2(add2(s3, eps), sc);
+	const F2 t1 = mul2(q1, q1), t2 = mul2(q2, q2), t3 = mul2(q3, q3);
+	return {mul2(t2, t3), mul2(f2(0.6f), mul2(t1, t3)), mul2(t1, t2)};
+}
+__device__ __forceinline__ Ratio2 rightRole2(const FaceWeights2 &w, F2 P1, F2 P2, F2 P3) {
+	const F2 w1 = mul2(f2(0.1f), w.a), w3 = mul2(f2(0.3f), w.c);
+	return {fma2(w1, P1, fma2(w.b, P2, mul2(w3, P3))), add2(add2(w1, w.b), w3)};
+}
+__device__ __forceinline__ Ratio2 leftRole2(const FaceWeights2 &w, F2 R1, F2 R2, F2 R3) {
+	const F2 w1 = mul2(f2(0.1f), w.c), w3 = mul2(f2(0.3f), w.a);
+	return {fma2(w1, R1, fma2(w.b, R2, mul2(w3, R3))), add2(add2(w1, w.b), w3)};
+}
+__device__ __forceinline__ void wenoCell2(const F2 v[7], Ratio2 &m, Ratio2 &p) {
+	const F2 D1 = sub2(v[1], v[0]), D2 = sub2(v[2], v[1]), D3 = sub2(v[3], v[2]), D4 = sub2(v[4], v[3]), D5 = sub2(v[5], v[4]), D6 = sub2(v[6], v[5]);
+	const F2 M = maxNonNeg2(maxNonNeg2(mul2(D2, D2), mul2(D3, D3)), maxNonNeg2(mul2(D4, D4), mul2(D5, D5)));
+	const F2 scale = f2(WenoConst<float>::epsScale), floor4 = f2(WenoConst<float>::floorEps4);
+	const F2 epsM = fma2(maxNonNeg2(M, mul2(D1, D1)), scale, floor4);
+	const F2 epsP = fma2(maxNonNeg2(M, mul2(D6, D6)), scale, floor4);
+	const F2 g1 = smoothG2(D1, D2, D3), g2 = smoothG2(D2, D3, D4), g3 = smoothG2(D3, D4, D5), g4 = smoothG2(D4, D5, D6);
+	const FaceWeights2 wm = faceWeights2(smoothL2(g1, D1, D2, D3), smoothM2(g2, D2, D4), smoothR2(g3, D3, D4, D5), epsM);
+	const FaceWeights2 wp = faceWeights2(smoothL2(g2, D2, D3, D4), smoothM2(g3, D3, D5), smoothR2(g4, D4, D5, D6), epsP);
+	const F2 P2 = stencil2_2(D2, D3, D4), P3 = stencil3_2(D3, D4, D5);
+	m = rightRole2(wm, stencil1_2(D1, D2, D3), P2, P3);
+	p = leftRole2(wp, stencil1_2(D6, D5, D4), P3, P2);
+}
+// godunovSq of both lanes, summed.
+__device__ __forceinline__ float godunovSq2(bool neg, const Ratio2 &m, const Ratio2 &p) {
+	const F2 a = mul2(m.num, negRecip2(m.den)), b = mul2(p.num, negRecip2(p.den));
+	const F2 x = f2(signBit(m.num.v.x) == neg ? a.v.x : 0.f, signBit(m.num.v.y) == neg ? a.v.y : 0.f);
+	const F2 y = f2(signBit(p.num.v.x) != neg ? b.v.x : 0.f, signBit(p.num.v.y) != neg ? b.v.y : 0.f);
+	const F2 s = fma2(x, x, mul2(y, y));
+	return s.v.x + s.v.y;
+}
+
 // Cell form: one thread per cell, seven clamped loads per axis (clamp-to-edge,
 // GridBasedData.h:47).  Used where columns give too little parallelism.
 template <int D, typename T, int Mode>
@@ -410,8 +479,19 @@ __global__ void __launch_bounds__(kBlock) kReinitCells(G<D, T> g, const T *__res
 	const bool neg = isNegative(f);
 	const bool inner = i >= 3 && i + 3 < sx && j >= 3 && j + 3 < sy && (D == 2 || (k >= 3 && k + 3 < sz));
 	T sum = T(0);
+	constexpr bool paired = D == 3 && sizeof(T) == 4;  // FP32 in 3D: x and y as the two lanes
+	if constexpr (paired) {
+		F2 u[7];
 #pragma unroll
-	for (int a = 0; a < D; a++) {
+		for (int t = 0; t < 7; t++)
+			u[t] = inner ? f2(ldg(in + id + (t - 3)), ldg(in + id + (t - 3) * int64_t(sx)))
+			             : f2(ldg(line[0] + min(max(i + t - 3, 0), lim[0])), ldg(line[1] + min(max(j + t - 3, 0), lim[1]) * sx));
+		Ratio2 m, p;
+		wenoCell2(u, m, p);
+		sum = godunovSq2(neg, m, p);
+	}
+#pragma unroll
+	for (int a = paired ? 2 : 0; a < D; a++) {
 		T v[7];
 		if (inner) {
 #pragma unroll
@@ -482,6 +562,21 @@ __global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__rest
 		const Ratio<T> mNext = rightRole(fw, stencil1(E1, E2, E3), stencil2(E2, E3, E4), stencil3(E3, E4, E5));
 		T sum = godunovSq(neg, mW, pW);
 		// in-plane axes (threads 3 or more cells from the in-plane edges need no clamping)
+		if constexpr (D == 3 && sizeof(T) == 4) {
+			// FP32 in 3D: x and y as the two lanes of paired instructions
+			F2 u[7];
+			if (inner) {
+#pragma unroll
+				for (int t = 0; t < 7; t++) u[t] = f2(ldg(in + id + (t - 3)), ldg(in + id + (t - 3) * sx));
+			} else {
+				const T *lx = in + (id - i), *ly = in + (id - int64_t(j) * sx);
+#pragma unroll
+				for (int t = 0; t < 7; t++) u[t] = f2(ldg(lx + min(max(i + t - 3, 0), sx - 1)), ldg(ly + min(max(j + t - 3, 0), sy - 1) * sx));
+			}
+			Ratio2 m, p;
+			wenoCell2(u, m, p);
+			sum += godunovSq2(neg, m, p);
+		} else
 #pragma unroll
 		for (int a = 0; a < D - 1; a++) {
 			const int c = a == 0 ? i : j, lim = (a == 0 ? sx : sy) - 1, str = a == 0 ? 1 : sx;

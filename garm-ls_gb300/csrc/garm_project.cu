@@ -460,25 +460,41 @@ __device__ __forceinline__ DF dfWarpSum(DF v) {
 	for (int o = 16; o > 0; o >>= 1) v = dfMerge(v, DF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)});
 	return v;
 }
+// NV warp sums level by level, so the shuffles and merges of the values overlap.
+template <int NV>
+__device__ __forceinline__ void dfWarpSumN(DF (&v)[NV]) {
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		DF w[NV];
+#pragma unroll
+		for (int q = 0; q < NV; q++) w[q] = DF{__shfl_xor_sync(0xffffffffu, v[q].hi, o), __shfl_xor_sync(0xffffffffu, v[q].lo, o)};
+#pragma unroll
+		for (int q = 0; q < NV; q++) v[q] = dfMerge(v[q], w[q]);
+	}
+}
 // Block sums of NV double-float values → partials (as float pairs) [v*maxBlocks + blockIdx].
 template <int NV>
 __device__ __forceinline__ void blockPartialsDF(DF (&acc)[NV], double *partials, int maxBlocks, double *sh) {
 	float2 *s2 = reinterpret_cast<float2 *>(sh);
 	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	dfWarpSumN<NV>(acc);
+	if (lane == 0) {
 #pragma unroll
-	for (int v = 0; v < NV; v++) {
-		const DF x = dfWarpSum(acc[v]);
-		if (lane == 0) s2[v * 16 + w] = make_float2(x.hi, x.lo);
+		for (int v = 0; v < NV; v++) s2[v * 16 + w] = make_float2(acc[v].hi, acc[v].lo);
 	}
 	__syncthreads();
 	if (w == 0) {
 		float2 *p2 = reinterpret_cast<float2 *>(partials);
+		DF x[NV];
 #pragma unroll
 		for (int v = 0; v < NV; v++) {
-			DF x{0.f, 0.f};
-			if (lane < nw) { const float2 q = s2[v * 16 + lane]; x = DF{q.x, q.y}; }
-			x = dfWarpSum(x);
-			if (lane == 0) p2[v * maxBlocks + blockIdx.x] = make_float2(x.hi, x.lo);
+			x[v] = DF{0.f, 0.f};
+			if (lane < nw) { const float2 q = s2[v * 16 + lane]; x[v] = DF{q.x, q.y}; }
+		}
+		dfWarpSumN<NV>(x);
+		if (lane == 0) {
+#pragma unroll
+			for (int v = 0; v < NV; v++) p2[v * maxBlocks + blockIdx.x] = make_float2(x[v].hi, x[v].lo);
 		}
 	}
 	__syncthreads();
@@ -491,16 +507,21 @@ __device__ __forceinline__ void gridTotalsDF(const double *partials, int maxBloc
 	if (threadIdx.x < 32) {
 		const float2 *p2 = reinterpret_cast<const float2 *>(partials);
 		double t[NOUT];
+		// the NV partials of one block are loaded together, so the L2 round trips of the
+		// values overlap
+		DF x[NV];
 #pragma unroll
-		for (int v = 0; v < NV; v++) {
-			DF x{0.f, 0.f};
-			for (int b = lane; b < (int)gridDim.x; b += 32) {
-				const float2 q = p2[v * maxBlocks + b];  // ordered by gridSync, as ldcg
-				x = dfMerge(x, DF{q.x, q.y});
-			}
-			x = dfWarpSum(x);
-			t[v] = double(x.hi) + double(x.lo);
+		for (int v = 0; v < NV; v++) x[v] = DF{0.f, 0.f};
+		for (int b = lane; b < (int)gridDim.x; b += 32) {
+			float2 q[NV];
+#pragma unroll
+			for (int v = 0; v < NV; v++) q[v] = p2[v * maxBlocks + b];  // ordered by gridSync, as ldcg
+#pragma unroll
+			for (int v = 0; v < NV; v++) x[v] = dfMerge(x[v], DF{q[v].x, q[v].y});
 		}
+		dfWarpSumN<NV>(x);
+#pragma unroll
+		for (int v = 0; v < NV; v++) t[v] = double(x[v].hi) + double(x[v].lo);
 		if (lane == 0) {
 			fin(t);
 #pragma unroll
@@ -668,11 +689,14 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 			cur ^= 1;
 			blockPartialsDF<3>(acc, a.partials, a.maxBlocks, sh);
 		}
-		if (!gridSync(a.bar, a.err, epoch)) break;
+		// β = γ/γ_old and α = γ/(δ - βγ/α_old) with the reciprocals of the known
+		// γ_old and γ_old·α_old formed before the barrier: one division after it
 		const double gOld = gamma;
-		gridTotalsDF<3, 5>(a.partials, a.maxBlocks, tot, sh, [gOld, alpha](double *t) {
-			t[3] = t[0] / gOld;
-			t[4] = t[0] / (t[1] - t[3] * t[0] / alpha);
+		const double invG = 1.0 / gOld, invGA = invG / alpha;
+		if (!gridSync(a.bar, a.err, epoch)) break;
+		gridTotalsDF<3, 5>(a.partials, a.maxBlocks, tot, sh, [invG, invGA](double *t) {
+			t[3] = t[0] * invG;
+			t[4] = t[0] / fma(-t[0] * t[0], invGA, t[1]);
 		});
 		it++;
 		gamma = tot[0];
