@@ -43,9 +43,12 @@ struct G {
 	T dx, inv;
 
 	__host__ __device__ __forceinline__ int64_t count() const { return int64_t(s[0]) * s[1] * (D == 3 ? s[2] : 1); }
+	// Grids hold fewer than 2^31 points (checked at creation), so the linear index of a
+	// point of the grid fits 32-bit arithmetic: cheaper than 64-bit multiplies in the
+	// gathers that form it for every tap.
 	__device__ __forceinline__ int64_t idx(int i, int j, int k) const {
-		if (D == 2) return int64_t(i) + int64_t(s[0]) * j;
-		return int64_t(i) + int64_t(s[0]) * (int64_t(j) + int64_t(s[1]) * k);
+		if (D == 2) return int64_t(i + s[0] * j);
+		return int64_t(i + s[0] * (j + s[1] * k));
 	}
 	__device__ __forceinline__ int cx(int i) const { return min(max(i, 0), s[0] - 1); }
 	__device__ __forceinline__ int cy(int j) const { return min(max(j, 0), s[1] - 1); }

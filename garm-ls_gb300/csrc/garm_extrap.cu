@@ -206,7 +206,7 @@ garm_status finishBoundary(State &s) {
 // ---------------------------------------------------------------------------
 enum FrontKind { kFrontCollider = 0, kFrontRefMap = 1, kFrontAdv = 2, kFrontFaces = 3 };
 
-constexpr int kFrontElemsPerBlock = 32768;  // grid elements per block of the pass launch
+constexpr int kFrontElemsPerBlock = 4096;   // grid elements per block of the pass launches (at most 8 blocks per SM)
 
 template <typename T>
 struct FrontArgs {
@@ -434,8 +434,9 @@ static garm_status front(State &s, int passes) {
 	if (passes <= 0) return GARM_OK;
 	kFrontFirst<D, T><<<gridFor(total), kBlock, 0, s.stream>>>(a, gate); s.launches++;
 	GARM_CHECK_LAUNCH();
-	// the frontiers are thin shells: at most one block per SM, fewer for small grids
-	const unsigned blocks = unsigned(std::max<int64_t>(1, std::min<int64_t>((int64_t(total) + kFrontElemsPerBlock - 1) / kFrontElemsPerBlock, s.numSMs)));
+	// the frontiers are thin shells: a grid in proportion to the grid size, at most 8 blocks
+	// per SM, enough warps to hide the latency of the scattered shell
+	const unsigned blocks = unsigned(std::max<int64_t>(1, std::min<int64_t>((int64_t(total) + kFrontElemsPerBlock - 1) / kFrontElemsPerBlock, 8 * int64_t(s.numSMs))));
 	for (int pass = 1; pass <= passes; pass++) {
 		kFrontPass<D, T, Kind><<<blocks, kBlock, 0, s.stream>>>(a, pass, gate); s.launches++;
 	}
