@@ -412,6 +412,7 @@ garm_status enqueueAutoDt(State &s) {
 garm_status readRecords(State &s, int k, garm_step_stats *S) {
 	if (cudaMemcpyAsync(s.statsHost, s.statsDev, size_t(kStatsCap) * kStatsSlots * 8, cudaMemcpyDeviceToHost, s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
 	if (cudaStreamSynchronize(s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
+	GARM_TRY(tiledReinitStatus(s.stream));
 	garm_status worst = GARM_OK;
 	for (int q = 0; q < k; q++) {
 		const double *rec = s.statsHost + ((s.hostSteps - 1 - q + kStatsCap) % kStatsCap) * kStatsSlots;
@@ -842,7 +843,7 @@ garm_status garm_sim_reinit_plan(garm_sim *sim, int *form, int *threads, int *ce
 garm_status garm_reinit_plan_set(int dim, int precision, const int *size, int form, int threads, int cells_per_thread) {
 	if ((dim != 2 && dim != 3) || !size || (precision != GARM_PRECISION_FP64 && precision != GARM_PRECISION_MIXED)) return GARM_INVALID;
 	for (int a = 0; a < dim; a++) if (size[a] <= 0) return GARM_INVALID;
-	if (form != GARM_REINIT_CELLS && form != GARM_REINIT_COLUMNS && form != GARM_REINIT_SWEEPS) return GARM_INVALID;
+	if (form != GARM_REINIT_CELLS && form != GARM_REINIT_COLUMNS && form != GARM_REINIT_SWEEPS && form != GARM_REINIT_TILED) return GARM_INVALID;
 	if (threads != 0 && form != GARM_REINIT_CELLS) {
 		if (cells_per_thread < 1) return GARM_INVALID;
 		if (threads < 32 || threads > 256 || threads % 32 != 0) return GARM_INVALID;

@@ -144,6 +144,9 @@ garm_status loadVolumeTables();
 // reinitialisation autotuner chose for this grid, and its sub-stage time in ms.
 template <int D, typename T> garm_status reinitPlanInfo(State &s, int *form, int *block, int *chunk, float *ms);
 garm_status pinReinitPlan(int dim, int esz, const int *size, int form, int block, int chunk);
+// GARM_TIMEOUT once a TMA-staged plane of the tiled reinitialisation form did not arrive
+// within its bounded wait (sticky); synchronises the stream.
+garm_status tiledReinitStatus(cudaStream_t st);
 template <int D, typename T> garm_status extrapolateToCollider(State &s);
 template <int D, typename T> garm_status checkReferenceMap(State &s, int *keep, int *tot, int *bad);
 template <int D, typename T> garm_status checkReferenceMapAsync(State &s, bool record);

@@ -5,6 +5,10 @@
 //   restart, plain branch   (LevelSetLiquid.cpp:1320-1352)
 //   enforceBoundaryLevelSet (LevelSetLiquid.cpp:966-975)
 #include "garm_internal.h"
+#include "garm_sync.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <map>
@@ -513,17 +517,23 @@ __global__ void __launch_bounds__(kBlock) kReinitCells(G<D, T> g, const T *__res
 // φ⁺ of the cell below and φ⁻ of the cell above; the in-plane axes use the cell
 // form's clamped loads.  Consecutive threads hold consecutive plane points, so
 // every load and store is coalesced.
-template <int D, typename T, int Mode>
-__global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__restrict__ in, const T *base, T *out, T dt, int chunk) {
+// In-plane values of the column form read from global memory (clamp-to-edge).
+struct GlobalPlanes {
+	static constexpr bool kStaged = false;
+	__device__ __forceinline__ bool ready(int) { return true; }
+	__device__ __forceinline__ void release(int) {}
+	__device__ __forceinline__ float at(int, int) const { return 0.f; }
+};
+
+// The walk of one column (pidx) over cells [w0, w1) of the last axis.  The plane source
+// P provides the in-plane stencil values: from global memory, or (3D FP32) from a tile of
+// the plane staged in shared memory, for which ready(w) waits and release(w) frees it.
+template <int D, typename T, int Mode, class P>
+__device__ __forceinline__ void columnWalk(const G<D, T> &g, const T *__restrict__ in, const T *base, T *out, T dt, int pidx, int w0, int w1, P &src) {
 	constexpr int W = D - 1;
 	const int sx = g.s[0], sy = D == 3 ? g.s[1] : 1;
 	const int plane = sx * sy;
-	const int pidx = blockIdx.x * blockDim.x + threadIdx.x;
-	if (pidx >= plane) return;
 	const int sw = g.s[W];
-	const int w0 = blockIdx.y * chunk;
-	if (w0 >= sw) return;
-	const int w1 = min(w0 + chunk, sw);
 	const int j = D == 3 ? pidx / sx : 0;
 	const int i = pidx - j * sx;
 	const bool inner = i >= 3 && i + 3 < sx && (D == 2 || (j >= 3 && j + 3 < sy));
@@ -550,6 +560,7 @@ __global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__rest
 	T gA = smoothG(E1, E2, E3), gB = smoothG(E2, E3, E4);
 	const int64_t pstride = plane;
 	for (int w = w0; w < w1; w++) {
+		if (!src.ready(w)) return;  // a staged plane that never arrived (block-uniform)
 		const int64_t id = int64_t(w) * pstride + pidx;
 		const T f = v[3];
 		const bool neg = isNegative(f);
@@ -565,7 +576,10 @@ __global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__rest
 		if constexpr (D == 3 && sizeof(T) == 4) {
 			// FP32 in 3D: x and y as the two lanes of paired instructions
 			F2 u[7];
-			if (inner) {
+			if constexpr (P::kStaged) {
+#pragma unroll
+				for (int t = 0; t < 7; t++) u[t] = f2(src.at(t - 3, 0), src.at(0, t - 3));
+			} else if (inner) {
 #pragma unroll
 				for (int t = 0; t < 7; t++) u[t] = f2(ldg(in + id + (t - 3)), ldg(in + id + (t - 3) * sx));
 			} else {
@@ -594,6 +608,7 @@ __global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__rest
 			sum += godunovSq(neg, m, p);
 		}
 		out[id] = rkUpdate<T, Mode>(f, sum, k6, g.dx, dt, base, id);
+		src.release(w);
 		// slide the window one cell up
 		if (w + 1 < w1) {
 #pragma unroll
@@ -605,6 +620,179 @@ __global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__rest
 			mW = mNext;
 		}
 	}
+}
+
+template <int D, typename T, int Mode>
+__global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__restrict__ in, const T *base, T *out, T dt, int chunk) {
+	const int plane = g.s[0] * (D == 3 ? g.s[1] : 1);
+	const int pidx = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pidx >= plane) return;
+	const int w0 = blockIdx.y * chunk;
+	if (w0 >= g.s[D - 1]) return;
+	GlobalPlanes src;
+	columnWalk<D, T, Mode>(g, in, base, out, dt, pidx, w0, min(w0 + chunk, g.s[D - 1]), src);
+}
+
+// ---- Tiled column form (3D FP32): the in-plane stencils of each z-plane read a tile of
+// the plane that the tensor memory accelerator (TMA) stages into shared memory.  A block
+// is a 32 x 4 patch of columns; the tile holds x0-4 .. x0+35 (the start rounded down to a
+// 16-byte boundary, as TMA requires) and y0-3 .. y0+6 of one plane.  Four planes are in
+// flight in a ring of shared-memory slots, each completed on its own mbarrier; one thread
+// issues the copies, and a slot is refilled once every thread has passed its plane.
+// Blocks whose tile would leave the grid in x or y walk with global loads (the clamped
+// edge); so do grids whose rows are not a multiple of 16 bytes.
+constexpr int kTileX = 32, kTileY = 4, kTileSlots = 4;
+constexpr int kTileRow = kTileX + 8, kTileRows = kTileY + 6;
+constexpr int kTileBytes = kTileRow * kTileRows * 4;
+constexpr int kTileStride = (kTileBytes + 127) / 128 * 128;
+constexpr unsigned long long kTileWaitNs = 1000000000ull;  // a plane not staged within 1 s: error
+
+__device__ int g_tiledError = 0;
+
+__device__ __forceinline__ unsigned smemAddr(const void *p) { return unsigned(__cvta_generic_to_shared(p)); }
+
+struct TmaPlanes {
+	static constexpr bool kStaged = true;
+	const CUtensorMap *map;
+	unsigned char *ring;
+	unsigned long long *bars;
+	int w0, w1, x0, y0, tx, ty;
+	const float *cur = nullptr;
+
+	__device__ void issue(int w) const {
+		const int slot = (w - w0) % kTileSlots;
+		const unsigned bar = smemAddr(bars + slot), dst = smemAddr(ring + slot * kTileStride);
+		asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(kTileBytes) : "memory");
+		asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+		             :: "r"(dst), "l"(reinterpret_cast<unsigned long long>(map)), "r"(x0 - 4), "r"(y0 - 3), "r"(w), "r"(bar) : "memory");
+	}
+	// Barriers initialised and the first planes requested (every thread calls it).
+	__device__ void start() {
+		if (threadIdx.x == 0) {
+			for (int q = 0; q < kTileSlots; q++)
+				asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smemAddr(bars + q)) : "memory");
+			asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+			asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+		}
+		__syncthreads();
+		if (threadIdx.x == 0)
+			for (int w = w0; w < min(w1, w0 + kTileSlots); w++) issue(w);
+	}
+	// Waits (bounded) until plane w is staged; false in every thread if any gave up.
+	__device__ bool ready(int w) {
+		const int slot = (w - w0) % kTileSlots;
+		const unsigned bar = smemAddr(bars + slot), parity = unsigned((w - w0) / kTileSlots) & 1u;
+		unsigned done = 0;
+		unsigned long long start = 0;
+		for (unsigned it = 0;; it++) {
+			asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+			             : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+			if (done) break;
+			if ((it & 255u) == 0) {
+				const unsigned long long now = globalNs();
+				if (start == 0) start = now;
+				else if (now - start > kTileWaitNs) break;
+			}
+		}
+		if (__syncthreads_or(!done)) {
+			if (threadIdx.x == 0) atomicExch(&g_tiledError, 1);
+			return false;
+		}
+		cur = reinterpret_cast<const float *>(ring + slot * kTileStride);
+		return true;
+	}
+	__device__ __forceinline__ float at(int ox, int oy) const { return cur[(ty + 3 + oy) * kTileRow + tx + 4 + ox]; }
+	// Every thread is done with plane w: its slot takes plane w + kTileSlots.
+	__device__ void release(int w) {
+		__syncthreads();
+		if (threadIdx.x == 0 && w + kTileSlots < w1) {
+			asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+			issue(w + kTileSlots);
+		}
+	}
+};
+
+template <int Mode>
+__global__ void __launch_bounds__(kTileX * kTileY) kReinitColumnsTiled(const __grid_constant__ CUtensorMap map, G<3, float> g, const float *__restrict__ in,
+                                                                       const float *base, float *out, float dt, int chunk) {
+	__shared__ __align__(128) unsigned char ring[kTileSlots * kTileStride];
+	__shared__ __align__(8) unsigned long long bars[kTileSlots];
+	const int sx = g.s[0], sy = g.s[1], sz = g.s[2];
+	const int tx = int(threadIdx.x) % kTileX, ty = int(threadIdx.x) / kTileX;
+	const int x0 = int(blockIdx.x) * kTileX, y0 = int(blockIdx.y) * kTileY;
+	const int w0 = int(blockIdx.z) * chunk;
+	if (w0 >= sz) return;
+	const int w1 = min(w0 + chunk, sz);
+	if (!(x0 >= 4 && x0 + kTileX + 4 <= sx && y0 >= 3 && y0 + kTileY + 3 <= sy)) {
+		const int i = x0 + tx, j = y0 + ty;
+		GlobalPlanes src;
+		if (i < sx && j < sy) columnWalk<3, float, Mode>(g, in, base, out, dt, i + j * sx, w0, w1, src);
+		return;
+	}
+	TmaPlanes src{&map, ring, bars, w0, w1, x0, y0, tx, ty};
+	src.start();
+	columnWalk<3, float, Mode>(g, in, base, out, dt, (x0 + tx) + (y0 + ty) * sx, w0, w1, src);
+}
+
+// Tensor maps of the planes the tiled form reads, per (address, shape); encoded on the host
+// (cuTensorMapEncodeTiled through the runtime's driver entry point) on first use.
+namespace {
+struct MapKey {
+	const void *p; int sx, sy, sz;
+	bool operator<(const MapKey &o) const {
+		if (p != o.p) return p < o.p;
+		if (sx != o.sx) return sx < o.sx;
+		if (sy != o.sy) return sy < o.sy;
+		return sz < o.sz;
+	}
+};
+std::mutex g_mapMutex;
+std::map<MapKey, CUtensorMap> g_maps;
+PFN_cuTensorMapEncodeTiled_v12000 encodeTiled() {
+	static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+	static bool tried = false;
+	if (!tried) {
+		tried = true;
+		void *f = nullptr;
+		cudaDriverEntryPointQueryResult q;
+		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess && q == cudaDriverEntryPointSuccess)
+			fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+		else cudaGetLastError();
+	}
+	return fn;
+}
+}  // namespace
+
+// The tensor map of plane `in` of a 3D FP32 grid, or false when the tiled form cannot
+// read it (rows not a multiple of 16 bytes, an unaligned address, no encoder).
+static bool tiledMap(const float *in, const G<3, float> &g, CUtensorMap *out) {
+	const int sx = g.s[0], sy = g.s[1], sz = g.s[2];
+	if (sx % 4 != 0 || (reinterpret_cast<uintptr_t>(in) & 15) != 0) return false;
+	std::lock_guard<std::mutex> lock(g_mapMutex);
+	const MapKey key{in, sx, sy, sz};
+	auto it = g_maps.find(key);
+	if (it != g_maps.end()) { *out = it->second; return true; }
+	PFN_cuTensorMapEncodeTiled_v12000 enc = encodeTiled();
+	if (!enc) return false;
+	CUtensorMap m;
+	const cuuint64_t dims[3] = {cuuint64_t(sx), cuuint64_t(sy), cuuint64_t(sz)};
+	const cuuint64_t strides[2] = {cuuint64_t(sx) * 4, cuuint64_t(sx) * cuuint64_t(sy) * 4};
+	const cuuint32_t box[3] = {cuuint32_t(kTileRow), cuuint32_t(kTileRows), 1};
+	const cuuint32_t elem[3] = {1, 1, 1};
+	if (enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(in), dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+	        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+		return false;
+	g_maps[key] = m;
+	*out = m;
+	return true;
+}
+
+// Error flag of the tiled form (a staged plane that did not arrive in time); synchronises.
+garm_status tiledReinitStatus(cudaStream_t st) {
+	int e = 0;
+	if (cudaMemcpyFromSymbolAsync(&e, g_tiledError, sizeof(int), 0, cudaMemcpyDeviceToHost, st) != cudaSuccess) return GARM_CUDA_ERROR;
+	if (cudaStreamSynchronize(st) != cudaSuccess) return GARM_CUDA_ERROR;
+	return e ? GARM_TIMEOUT : GARM_OK;
 }
 
 // Sweep form: three passes per sub-stage, one per axis (x, then y, then z).
@@ -705,7 +893,7 @@ __global__ void __launch_bounds__(256) kWenoSweep(G<D, T> g, const T *__restrict
 // form, the column form or the sweep form, with `block` threads and `chunk`
 // cells per thread.  Chosen by timing (reinitPlanFor) and cached per device
 // and shape.
-enum ReinitForm { kFormCells = GARM_REINIT_CELLS, kFormColumns = GARM_REINIT_COLUMNS, kFormSweeps = GARM_REINIT_SWEEPS };
+enum ReinitForm { kFormCells = GARM_REINIT_CELLS, kFormColumns = GARM_REINIT_COLUMNS, kFormSweeps = GARM_REINIT_SWEEPS, kFormTiled = GARM_REINIT_TILED };
 struct ReinitPlan { int form = kFormColumns, block = 128, chunk = 8; float ms = 0; };
 
 template <int D, typename T, int A, int Mode>
@@ -729,10 +917,20 @@ static int launchReinit(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g,
 		if (D == 3) launchSweep<D, T, D == 3 ? 2 : 1, Mode>(pl, st, g, in, base, out, dt);
 		return D;
 	}
+	if constexpr (D == 3 && sizeof(T) == 4) {
+		CUtensorMap map;
+		if (pl.form == kFormTiled && tiledMap((const float *)in, g, &map)) {
+			const dim3 grid((g.s[0] + kTileX - 1) / kTileX, (g.s[1] + kTileY - 1) / kTileY, (g.s[2] + pl.chunk - 1) / pl.chunk);
+			kReinitColumnsTiled<Mode><<<grid, kTileX * kTileY, 0, st>>>(map, g, (const float *)in, (const float *)base, (float *)out, float(dt), pl.chunk);
+			return 1;
+		}
+	}
+	// the column form (also the tiled form where it does not apply)
+	const int block = pl.form == kFormTiled ? kTileX * kTileY : pl.block;
 	const int plane = g.s[0] * (D == 3 ? g.s[1] : 1);
 	const int sw = g.s[D - 1];
-	const dim3 grid((plane + pl.block - 1) / pl.block, (sw + pl.chunk - 1) / pl.chunk);
-	kReinitColumns<D, T, Mode><<<grid, pl.block, 0, st>>>(g, in, base, out, dt, pl.chunk);
+	const dim3 grid((plane + block - 1) / block, (sw + pl.chunk - 1) / pl.chunk);
+	kReinitColumns<D, T, Mode><<<grid, block, 0, st>>>(g, in, base, out, dt, pl.chunk);
 	return 1;
 }
 
@@ -772,6 +970,8 @@ static ReinitPlan reinitPlanFor(cudaStream_t st, const G<D, T> &g, const T *phi,
 	cand.push_back({kFormCells, kBlock, 0});
 	for (int b : {64, 128, 256})
 		for (int c : {4, 8, 16, 32}) cand.push_back({kFormColumns, b, c});
+	if (D == 3 && sizeof(T) == 4)
+		for (int c : {4, 8, 16, 32}) cand.push_back({kFormTiled, kTileX * kTileY, c});
 	// sweeps: walks that split the longest axis into 2-8 equal pieces, plus short fixed ones
 	int longest = 0;
 	for (int a = 0; a < D; a++) longest = std::max(longest, g.s[a]);
@@ -819,7 +1019,7 @@ garm_status pinReinitPlan(int dim, int esz, const int *size, int form, int block
 	if (block == 0) { g_plans.erase(key); return GARM_OK; }
 	ReinitPlan pl;
 	pl.form = form;
-	pl.block = form == kFormCells ? kBlock : block;
+	pl.block = form == kFormCells ? kBlock : form == kFormTiled ? kTileX * kTileY : block;
 	pl.chunk = form == kFormCells ? 0 : chunk;
 	g_plans[key] = pl;
 	return GARM_OK;

@@ -20,7 +20,7 @@ STATUS_NAMES = {OK: "ok", INVALID: "invalid", OOM: "oom", NOT_CONVERGED: "not_co
                 CUDA_ERROR: "cuda_error", TIMEOUT: "timeout", UNSUPPORTED: "unsupported"}
 
 PRECISION_FP64, PRECISION_MIXED = 0, 1
-REINIT_FORMS = ["cells", "columns", "sweeps"]  # GARM_REINIT_CELLS, _COLUMNS, _SWEEPS
+REINIT_FORMS = ["cells", "columns", "sweeps", "tiled"]  # GARM_REINIT_CELLS, _COLUMNS, _SWEEPS, _TILED
 
 # garm_field
 (FIELD_VELOCITY, FIELD_LEVEL_SET, FIELD_REF_MAP, FIELD_REF_MAP_GRAD, FIELD_REF_LEVEL_SET, FIELD_REF_LEVEL_SET_GRAD,
@@ -365,7 +365,7 @@ def reinit_host(phi: np.ndarray, spacing: float, iters: int, cfl: float, precisi
 
 def reinit_plan_set(shape_xyz, precision: int, form: str, threads: int, cells_per_thread: int) -> None:
     """Pin the reinitialisation launch plan of one grid shape (cells per axis, x first):
-    form "cells" | "columns" | "sweeps"; threads=0 returns the shape to the autotuner."""
+    form "cells" | "columns" | "sweeps" | "tiled"; threads=0 returns the shape to the autotuner."""
     size = (C.c_int * 3)(*([int(x) for x in shape_xyz] + [1] * (3 - len(shape_xyz))))
     check(load().garm_reinit_plan_set(len(shape_xyz), int(precision), size, REINIT_FORMS.index(form), int(threads),
                                       int(cells_per_thread)), "garm_reinit_plan_set")

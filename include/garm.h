@@ -191,11 +191,14 @@ garm_status garm_batch_advance_auto(garm_sim *const *sims, int count, int steps,
 /* 1 when garm_sim_advance_auto replays captured step graphs (no reference counterpart). */
 garm_status garm_sim_graph_active(const garm_sim *sim, int *active);
 /* Launch forms of the WENO5 reinitialisation sub-stages (no reference counterpart):
- * one thread per cell; threads walking columns along the last axis; or one pass
- * per axis, threads walking lines of that axis. */
+ * one thread per cell; threads walking columns along the last axis; one pass
+ * per axis, threads walking lines of that axis; or (3D FP32) columns whose in-plane
+ * stencils read tiles of each plane staged in shared memory by TMA, 128 threads per
+ * block (other precisions and shapes run the column form). */
 #define GARM_REINIT_CELLS 0
 #define GARM_REINIT_COLUMNS 1
 #define GARM_REINIT_SWEEPS 2
+#define GARM_REINIT_TILED 3
 /* The launch plan the reinitialisation autotuner chose for this simulation's grid:
  * form, threads per block, cells each thread walks and the timed sub-stage in ms.
  * Plans are tuned once per grid shape, precision and device in the process, on
