@@ -45,6 +45,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-batch", action="store_true")
+    p.add_argument("--no-default-build", action="store_true",
+                   help="skip the same workload in the reference's default build (Newton restart + fast marching)")
     p.add_argument("--workload", choices=["dam", "batch", "serve"], default="dam",
                    help="dam: the 128^3 dam break (default line, with mixed and batch sub-objects); "
                         "batch: 48 uneven pool scenes only; serve: the Poisson request stream only")
@@ -335,8 +337,10 @@ def run_garm(args) -> None:
         for prec in (capi.PRECISION_FP64, capi.PRECISION_MIXED):
             capi.reinit_plan_set([scene.grid.resolution[a] for a in range(3)], prec, form, int(threads), int(cells))
 
-    def make(precision):
+    def make(precision, **flags):
         cfg = capi.default_config(precision=precision)
+        for k, v in flags.items():
+            setattr(cfg, k, v)
         sim = capi.Simulation(scene.grid, cfg, stream=stream.cuda_stream)
         sim.upload(capi.FIELD_LEVEL_SET, scene.phi.ravel())
         sim.upload(capi.FIELD_VELOCITY, scene.velocity)
@@ -452,6 +456,27 @@ def run_garm(args) -> None:
             out["mixed"]["roofline"]["traffic"] = profiled_traffic(out["mixed"]["roofline"]["plan"], "mixed", n)
             out["mixed"]["roofline"]["compute"] = profiled_pipe(out["mixed"]["roofline"]["plan"], "mixed", n)
         mix.close()
+
+    # the same workload in the reference's default build: HybridNewton restart and fast
+    # marching in place of WENO5 (restart_newton = fast_marching = 1)
+    if not args.no_default_build and args.precision == "fp64":
+        legs = {}
+        for name, prec in (("fp64", capi.PRECISION_FP64), ("mixed", capi.PRECISION_MIXED)):
+            d = make(prec, restart_newton=1, fast_marching=1)
+            d.set_clock(25, 1.0)
+            d.advance_auto(W)
+            barrier(world)
+            torch.cuda.synchronize()
+            d0, d1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            d0.record(stream)
+            st = d.advance_auto(K)
+            d1.record(stream)
+            torch.cuda.synchronize()
+            dms = reduce_max(d0.elapsed_time(d1), world)
+            legs[name] = {"value": world * interior * K / (dms * 1e-3), "unit": UNIT, "ms_per_step": dms / K,
+                          "restarted_last_step": st["restarted"]}
+            d.close()
+        out["default_build"] = {"config": "restart_newton=1, fast_marching=1 (the reference's default xmake options)", **legs}
 
     # many uneven scenes at once (mixed): the batched form of the same pipeline
     if not args.no_batch:

@@ -121,6 +121,7 @@ garm_status allocState(State &s) {
 		GARM_TRY(dalloc(s, &s.marchTent, N * e));
 		GARM_TRY(dalloc(s, &s.marchTent2, N * e));
 		GARM_TRY(dalloc(s, (void **)&s.marchFixed, N));
+		GARM_TRY(dalloc(s, (void **)&s.marchStamp, N * 4));
 		GARM_TRY(dalloc(s, (void **)&s.marchBar, 64));
 		GARM_TRY(dalloc(s, (void **)&s.marchInts, 64));
 	}

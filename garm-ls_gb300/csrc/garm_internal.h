@@ -51,6 +51,7 @@ struct State {
 	// flags, the relaxation's barrier and control words
 	void *marchTent = nullptr, *marchTent2 = nullptr;
 	uint8_t *marchFixed = nullptr;
+	int *marchStamp = nullptr;         // per cell: the last relaxation sweep it was queued for
 	unsigned *marchBar = nullptr;
 	int *marchInts = nullptr;
 	uint8_t *adv = nullptr;    // _advRegion
