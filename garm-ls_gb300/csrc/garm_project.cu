@@ -182,10 +182,18 @@ __device__ __forceinline__ float ldcg(const float *p) { return *p; }
 template <int NV>
 __device__ __forceinline__ void blockPartials(double (&acc)[NV], double *partials, int maxBlocks, double *sh) {
 	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+	// the NV warp sums level by level, so their shuffles and additions overlap
 #pragma unroll
-	for (int v = 0; v < NV; v++) {
-		double x = warpSum(acc[v]);
-		if (lane == 0) sh[v * 16 + w] = x;
+	for (int o = 16; o > 0; o >>= 1) {
+		double y[NV];
+#pragma unroll
+		for (int v = 0; v < NV; v++) y[v] = __shfl_xor_sync(0xffffffffu, acc[v], o);
+#pragma unroll
+		for (int v = 0; v < NV; v++) acc[v] += y[v];
+	}
+	if (lane == 0) {
+#pragma unroll
+		for (int v = 0; v < NV; v++) sh[v * 16 + w] = acc[v];
 	}
 	__syncthreads();
 	if (threadIdx.x < NV) {
@@ -205,11 +213,23 @@ __device__ __forceinline__ void gridTotals(const double *partials, int maxBlocks
 	const int lane = threadIdx.x & 31;
 	if (threadIdx.x < 32) {
 		double t[NOUT];
+		// the NV partials of one block are loaded together, so their L2 round trips overlap
 #pragma unroll
-		for (int v = 0; v < NV; v++) {
-			double s = 0;
-			for (int b = lane; b < (int)gridDim.x; b += 32) s += ldcg(partials + v * maxBlocks + b);
-			t[v] = warpSum(s);
+		for (int v = 0; v < NV; v++) t[v] = 0;
+		for (int b = lane; b < (int)gridDim.x; b += 32) {
+			double q[NV];
+#pragma unroll
+			for (int v = 0; v < NV; v++) q[v] = ldcg(partials + v * maxBlocks + b);
+#pragma unroll
+			for (int v = 0; v < NV; v++) t[v] += q[v];
+		}
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			double y[NV];
+#pragma unroll
+			for (int v = 0; v < NV; v++) y[v] = __shfl_xor_sync(0xffffffffu, t[v], o);
+#pragma unroll
+			for (int v = 0; v < NV; v++) t[v] += y[v];
 		}
 		if (lane == 0) {
 			fin(t);
@@ -388,11 +408,13 @@ __device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, unsigned &epoch,
 		}
 		double acc[3] = {g, d, rr};
 		blockPartials<3>(acc, a.partials, a.maxBlocks, sh);
+		// β = γ/γ_old and α = γ/(δ - βγ/α_old) with the reciprocals of the known γ_old and
+		// γ_old·α_old formed before the barrier: one division after it
+		const double invG = 1.0 / gamma, invGA = invG / alpha;
 		if (!gridSync(a.bar, a.err, epoch)) { *ok = false; it++; break; }
-		const double gOld = gamma;
-		gridTotals<3, 5>(a.partials, a.maxBlocks, tot, sh, [gOld, alpha](double *t) {
-			t[3] = t[0] / gOld;
-			t[4] = t[0] / (t[1] - t[3] * t[0] / alpha);
+		gridTotals<3, 5>(a.partials, a.maxBlocks, tot, sh, [invG, invGA](double *t) {
+			t[3] = t[0] * invG;
+			t[4] = t[0] / fma(-t[0] * t[0], invGA, t[1]);
 		});
 		it++;
 		*outRR = tot[2];
