@@ -335,6 +335,14 @@ static VelView<D, T> makeVelView(State &s) {
 template <int D, typename T>
 garm_status advectFields(State &s) {
 	const int64_t F0 = s.F[0], F1 = s.F[1];
+	// u (reads the old velocity for every axis: Advection.h:15-22) needs neither ∇u nor ξ,
+	// so it runs beside steps 1-3 on the second stream
+	GARM_TRY(forkAux(s, 0));
+	{
+		const VelView<D, T> vu = makeVelView<D, T>(s);
+		kAdvectVelocity<D, T><<<gridFor(s.Ftot), kBlock, 0, s.aux>>>(s.geom, vu, (T *)s.uNew[0], (T *)s.uNew[1], (T *)s.uNew[2], F0, F1, s.Ftot, s.dtDev); s.launches++;
+		GARM_CHECK_LAUNCH();
+	}
 	// 1. ∇u
 	kVelocityGrad<D, T><<<gridFor(s.Ftot), kBlock, 0, s.stream>>>(s.geom, (const T *)s.u[0], (const T *)s.u[1], (const T *)s.u[2],
 		(T *)s.uGrad[0], (T *)s.uGrad[1], (T *)s.uGrad[2], (T *)s.uGrad[3], (T *)s.uGrad[4], (T *)s.uGrad[5],
@@ -355,9 +363,7 @@ garm_status advectFields(State &s) {
 	for (int q = 0; q < 12; q++) io.mixed[q] = (const T *)s.xiMixed[q];
 	kAdvectRefMap<D, T><<<gridFor(s.N), kBlock, 0, s.stream>>>(s.geom, vv, io, s.dtDev); s.launches++;
 	GARM_CHECK_LAUNCH();
-	// 4. u (reads the old velocity for every axis: Advection.h:15-22)
-	kAdvectVelocity<D, T><<<gridFor(s.Ftot), kBlock, 0, s.stream>>>(s.geom, vv, (T *)s.uNew[0], (T *)s.uNew[1], (T *)s.uNew[2], F0, F1, s.Ftot, s.dtDev); s.launches++;
-	GARM_CHECK_LAUNCH();
+	GARM_TRY(joinAux(s, 0));
 	for (int c = 0; c < D; c++) { void *t = s.xi[c]; s.xi[c] = s.xiNew[c]; s.xiNew[c] = t; }
 	for (int q = 0; q < D * D; q++) { void *t = s.Pi[q]; s.Pi[q] = s.PiNew[q]; s.PiNew[q] = t; }
 	for (int a = 0; a < D; a++) { void *t = s.u[a]; s.u[a] = s.uNew[a]; s.uNew[a] = t; }

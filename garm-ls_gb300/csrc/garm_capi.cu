@@ -75,6 +75,9 @@ void freeAll(State &s) {
 	for (int i = 0; i < s.nAllocs; i++) cudaFree(s.allocs[i]);
 	s.nAllocs = 0;
 	for (auto &e : s.ev) if (e) { cudaEventDestroy(e); e = nullptr; }
+	for (auto &e : s.forkEv) if (e) { cudaEventDestroy(e); e = nullptr; }
+	for (auto &e : s.joinEv) if (e) { cudaEventDestroy(e); e = nullptr; }
+	if (s.aux) { cudaStreamDestroy(s.aux); s.aux = nullptr; }
 	if (s.ownStream && s.stream) { cudaStreamDestroy(s.stream); s.stream = nullptr; }
 }
 
@@ -134,6 +137,10 @@ garm_status allocState(State &s) {
 	GARM_TRY(dalloc(s, (void **)&s.frontList[0], size_t(s.Ftot) * 4));
 	GARM_TRY(dalloc(s, (void **)&s.frontList[1], size_t(s.Ftot) * 4));
 	GARM_TRY(dalloc(s, (void **)&s.frontCount, size_t(kFrontMaxPasses + 2) * 4));
+	GARM_TRY(dalloc(s, (void **)&s.frontBitsB, (size_t(s.Ftot) + 31) / 32 * 4));
+	GARM_TRY(dalloc(s, (void **)&s.frontListB[0], size_t(s.Ftot) * 4));
+	GARM_TRY(dalloc(s, (void **)&s.frontListB[1], size_t(s.Ftot) * 4));
+	GARM_TRY(dalloc(s, (void **)&s.frontCountB, size_t(kFrontMaxPasses + 2) * 4));
 	GARM_TRY(dalloc(s, &s.bcList, size_t(s.Ftot) * 8));
 	GARM_TRY(dalloc(s, &s.bcTmp, size_t(s.Ftot) * e));
 	// projection
@@ -686,6 +693,10 @@ garm_status garm_sim_create(const garm_grid_desc *gd, const garm_config *cfg, vo
 	}
 	for (auto &e : s.ev)
 		if (cudaEventCreate(&e) != cudaSuccess) { freeAll(s); delete sim; return GARM_CUDA_ERROR; }
+	if (cudaStreamCreateWithFlags(&s.aux, cudaStreamNonBlocking) != cudaSuccess) { freeAll(s); delete sim; return GARM_CUDA_ERROR; }
+	for (int k = 0; k < 2; k++)
+		if (cudaEventCreateWithFlags(&s.forkEv[k], cudaEventDisableTiming) != cudaSuccess ||
+		    cudaEventCreateWithFlags(&s.joinEv[k], cudaEventDisableTiming) != cudaSuccess) { freeAll(s); delete sim; return GARM_CUDA_ERROR; }
 	const int D = s.dim;
 	s.N = int64_t(s.geom.n[0]) * s.geom.n[1] * s.geom.n[2];
 	s.NN = int64_t(s.geom.n[0] + 1) * (s.geom.n[1] + 1) * (D == 3 ? s.geom.n[2] + 1 : 1);

@@ -391,7 +391,8 @@ __global__ void __launch_bounds__(kBlock) kFrontPass(FrontArgs<T> a, int pass, c
 static inline int passCount(double r) { int n = 0; while (n < r) n++; return n; }  // `for (iter = 0; iter < maxSteps; ...)`
 
 template <int D, typename T, int Kind>
-static garm_status front(State &s, int passes) {
+static garm_status front(State &s, int passes, bool second = false) {
+	cudaStream_t st = second ? s.aux : s.stream;
 	FrontArgs<T> a{};
 	a.geom = s.geom;
 	if (Kind == kFrontFaces) {
@@ -421,24 +422,24 @@ static garm_status front(State &s, int passes) {
 	a.adv = s.adv;
 	a.cellDist = (const T *)s.cellDist;
 	a.ori = (const T *)s.ori;
-	a.bits = s.frontBits;
-	a.list[0] = s.frontList[0];
-	a.list[1] = s.frontList[1];
-	a.count = s.frontCount;
+	a.bits = second ? s.frontBitsB : s.frontBits;
+	a.list[0] = second ? s.frontListB[0] : s.frontList[0];
+	a.list[1] = second ? s.frontListB[1] : s.frontList[1];
+	a.count = second ? s.frontCountB : s.frontCount;
 	a.passes = passes;
 	if (passes > kFrontMaxPasses) return GARM_INVALID;
 	const int total = a.off[a.nsub];
 	const int *gate = s.gate;
-	kFrontSeed<D, T, Kind><<<gridFor(total), kBlock, 0, s.stream>>>(a, gate); s.launches++;
+	kFrontSeed<D, T, Kind><<<gridFor(total), kBlock, 0, st>>>(a, gate); s.launches++;
 	GARM_CHECK_LAUNCH();
 	if (passes <= 0) return GARM_OK;
-	kFrontFirst<D, T><<<gridFor(total), kBlock, 0, s.stream>>>(a, gate); s.launches++;
+	kFrontFirst<D, T><<<gridFor(total), kBlock, 0, st>>>(a, gate); s.launches++;
 	GARM_CHECK_LAUNCH();
 	// the frontiers are thin shells: a grid in proportion to the grid size, at most 8 blocks
 	// per SM, enough warps to hide the latency of the scattered shell
 	const unsigned blocks = unsigned(std::max<int64_t>(1, std::min<int64_t>((int64_t(total) + kFrontElemsPerBlock - 1) / kFrontElemsPerBlock, 8 * int64_t(s.numSMs))));
 	for (int pass = 1; pass <= passes; pass++) {
-		kFrontPass<D, T, Kind><<<blocks, kBlock, 0, s.stream>>>(a, pass, gate); s.launches++;
+		kFrontPass<D, T, Kind><<<blocks, kBlock, 0, st>>>(a, pass, gate); s.launches++;
 	}
 	GARM_CHECK_LAUNCH();
 	return GARM_OK;
@@ -456,9 +457,13 @@ garm_status extrapolateToCollider(State &s) {
 template <int D, typename T>
 garm_status extrapolateToAir(State &s) {
 	const int R = passCount(s.cfg.air_extrap_radius);
+	// the face march reads ori and the fractions only, so it runs beside the two cell
+	// marches (ξ, then the flags, which ξ's seeds are read from) on the second stream
+	GARM_TRY(forkAux(s, 1));
+	GARM_TRY((front<D, T, kFrontFaces>(s, passCount(s.cfg.air_extrap_radius + 2), true)));
 	GARM_TRY((front<D, T, kFrontRefMap>(s, R)));
 	GARM_TRY((front<D, T, kFrontAdv>(s, R)));
-	return front<D, T, kFrontFaces>(s, passCount(s.cfg.air_extrap_radius + 2));
+	return joinAux(s, 1);
 }
 
 // ---------------------------------------------------------------------------

@@ -22,6 +22,10 @@ struct State {
 	size_t esz = 8;            // bytes per stored field element
 	cudaStream_t stream = nullptr;
 	bool ownStream = false;
+	// a second stream for independent stages: forked from and joined back to `stream` by
+	// events, so a captured step has them as parallel branches
+	cudaStream_t aux = nullptr;
+	cudaEvent_t forkEv[2] = {}, joinEv[2] = {};
 	int numSMs = 0;
 	long long stepIndex = 0;
 	long long launches = 0;    // kernels launched by this simulation (for the bench's gpu_launches)
@@ -57,10 +61,11 @@ struct State {
 	uint8_t *adv = nullptr;    // _advRegion
 	uint8_t *vis0 = nullptr;   // cell extrapolation levels (seed 0, joined in pass p, 255 unreached)
 	uint8_t *fvis0 = nullptr;  // face extrapolation levels (all axes, concatenated)
-	// frontier extrapolation: queued-once bits, the two frontier lists, per-pass sizes
-	unsigned *frontBits = nullptr;
-	int *frontList[2] = {};
-	int *frontCount = nullptr;
+	// frontier extrapolation: queued-once bits, the two frontier lists, per-pass sizes; a
+	// second set for the face march, which runs beside the cell marches
+	unsigned *frontBits = nullptr, *frontBitsB = nullptr;
+	int *frontList[2] = {}, *frontListB[2] = {};
+	int *frontCount = nullptr, *frontCountB = nullptr;
 	// boundary (Boundary<Dim>, Source/Core/Boundary.h:16-24)
 	void *cellDist = nullptr, *nodeDist = nullptr;
 	void *fraction[3] = {}, *bvel[3] = {}, *normal[3] = {};
@@ -184,6 +189,15 @@ template <int D, typename T> garm_status copyField(State &s, void *dst, const vo
 template <int D, typename T> garm_status reinitRaw(cudaStream_t st, const int *size, double dx, T *phi, T *a, T *b, int iters, double cfl);
 
 inline garm_status cudaStatus(cudaError_t e) { return e == cudaSuccess ? GARM_OK : GARM_CUDA_ERROR; }
+// Work after forkAux(k) on s.aux runs beside work on s.stream until joinAux(k).
+inline garm_status forkAux(State &s, int k) {
+	if (cudaEventRecord(s.forkEv[k], s.stream) != cudaSuccess || cudaStreamWaitEvent(s.aux, s.forkEv[k], 0) != cudaSuccess) return GARM_CUDA_ERROR;
+	return GARM_OK;
+}
+inline garm_status joinAux(State &s, int k) {
+	if (cudaEventRecord(s.joinEv[k], s.aux) != cudaSuccess || cudaStreamWaitEvent(s.stream, s.joinEv[k], 0) != cudaSuccess) return GARM_CUDA_ERROR;
+	return GARM_OK;
+}
 #define GARM_CHECK_LAUNCH() do { cudaError_t _e = cudaGetLastError(); if (_e != cudaSuccess) return GARM_CUDA_ERROR; } while (0)
 #define GARM_TRY(x) do { garm_status _s = (x); if (_s != GARM_OK) return _s; } while (0)
 
