@@ -15,9 +15,10 @@
 // sweeps between two buffers, so the result does not depend on the order in which blocks
 // run (an in-place relaxation can settle on different last bits where a neighbour ties
 // with a root), and each visits only the cells whose neighbours changed in the sweep
-// before (about a hundred sweeps cross a 15-cell band at 128^3, each moving a thin shell).  Each cell's update is the reference's quadratic in the same operation
-// order, so the result is the reference's up to the last bits in exact ties, where a
-// neighbour equal to the root enters or drops out of Q.
+// before (about 140 sweeps cross a 15-cell band at 128^3, each moving a thin shell).  Each
+// cell's update is the reference's quadratic in the same operation order, so the result is
+// the reference's up to the last bits in exact ties, where a neighbour equal to the root
+// enters or drops out of Q.
 #include "garm_internal.h"
 #include "garm_sync.cuh"
 

@@ -74,3 +74,27 @@ def test_null_arguments_are_rejected_without_a_gpu(garm_lib):
     bad = capi.grid_desc(3, [3, 3, 3], 0.1, [0, 0, 0])  # smaller than the solid ring
     h = C.c_void_p()
     assert garm_lib.garm_sim_create(C.byref(bad), None, None, C.byref(h)) == capi.INVALID
+
+
+def test_header_constants_match_the_binding():
+    """Field ids and reinitialisation forms of include/garm.h against the ctypes binding."""
+    text = HEADER.read_text()
+    fields = {m.group(1): int(m.group(2)) for m in re.finditer(r"GARM_FIELD_([A-Z_]+)\s*=\s*(\d+)", text)}
+    count = fields.pop("COUNT")
+    assert count == len(fields) == len(capi.FIELD_NAMES)
+    for name, value in fields.items():
+        assert getattr(capi, "FIELD_" + name) == value, name
+    forms = {m.group(1).lower(): int(m.group(2)) for m in re.finditer(r"#define GARM_REINIT_([A-Z]+) (\d+)", text)}
+    assert forms == {f: i for i, f in enumerate(capi.REINIT_FORMS)}
+
+
+def test_new_config_fields_are_validated_without_a_gpu(garm_lib):
+    g = capi.grid_desc(3, [12, 12, 12], 0.1, [0.6, 0.6, 0.6])
+    h = C.c_void_p()
+    for field, bad in (("restart_newton", 2), ("fast_marching", -1), ("record_volume", 3), ("air_extrap_radius", 1000.0),
+                       ("boundary_extrap_radius", float("nan")), ("cg_cells_per_block", -5)):
+        cfg = host_default_config(**{field: bad})
+        assert garm_lib.garm_sim_create(C.byref(g), C.byref(cfg), None, C.byref(h)) == capi.INVALID, field
+    size = (C.c_int * 3)(20, 20, 20)
+    assert garm_lib.garm_reinit_plan_set(3, capi.PRECISION_MIXED, size, 7, 128, 8) == capi.INVALID
+    assert garm_lib.garm_reinit_plan_set(3, capi.PRECISION_MIXED, size, 3, 100, 8) == capi.INVALID
