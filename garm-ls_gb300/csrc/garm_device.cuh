@@ -35,6 +35,12 @@ __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, 
 
 template <typename T> __device__ __forceinline__ T ldg(const T *p) { return __ldg(p); }
 
+// Programmatic dependent launch (sm_90 and later): a kernel launched with launchPdl may be
+// scheduled while the kernel before it on the stream is still finishing.  It calls pdlWait()
+// before its first global memory access; that returns once the previous kernel has completed
+// and its writes are visible, so every dependency, write-after-read included, still holds.
+__device__ __forceinline__ void pdlWait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // A regular sub-grid (node, cell or one face grid): Grid<Dim> (Source/Core/Grid.h:10-61).
 template <int D, typename T>
 struct G {

@@ -297,6 +297,7 @@ __device__ __forceinline__ bool liquidFace(const FrontArgs<T> &a, const FrontPos
 // concurrent scenes' graphs).
 template <int D, typename T, int Kind>
 __global__ void __launch_bounds__(kBlock) kFrontSeed(FrontArgs<T> a, const int *gate) {
+	pdlWait();
 	if (gate && !*gate) return;
 	const int gid = int(blockIdx.x) * blockDim.x + threadIdx.x;
 	if (gid < (a.off[a.nsub] + 31) / 32) a.bits[gid] = 0u;
@@ -325,6 +326,7 @@ __global__ void __launch_bounds__(kBlock) kFrontSeed(FrontArgs<T> a, const int *
 // Phase B: the first frontier, the unvisited neighbours of seeds.
 template <int D, typename T>
 __global__ void __launch_bounds__(kBlock) kFrontFirst(FrontArgs<T> a, const int *gate) {
+	pdlWait();
 	if (gate && !*gate) return;
 	const int total = a.off[a.nsub];
 	const int gid = int(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -347,6 +349,7 @@ __global__ void __launch_bounds__(kBlock) kFrontFirst(FrontArgs<T> a, const int 
 // frontier.  A small grid strides over the frontier, whose size is on the device.
 template <int D, typename T, int Kind>
 __global__ void __launch_bounds__(kBlock) kFrontPass(FrontArgs<T> a, int pass, const int *gate) {
+	pdlWait();
 	if (gate && !*gate) return;
 	const int stride = int(gridDim.x) * blockDim.x;
 	const int n = a.count[pass];
@@ -430,16 +433,16 @@ static garm_status front(State &s, int passes, bool second = false) {
 	if (passes > kFrontMaxPasses) return GARM_INVALID;
 	const int total = a.off[a.nsub];
 	const int *gate = s.gate;
-	kFrontSeed<D, T, Kind><<<gridFor(total), kBlock, 0, st>>>(a, gate); s.launches++;
+	launchPdl(kFrontSeed<D, T, Kind>, dim3(gridFor(total)), dim3(kBlock), st, a, gate); s.launches++;
 	GARM_CHECK_LAUNCH();
 	if (passes <= 0) return GARM_OK;
-	kFrontFirst<D, T><<<gridFor(total), kBlock, 0, st>>>(a, gate); s.launches++;
+	launchPdl(kFrontFirst<D, T>, dim3(gridFor(total)), dim3(kBlock), st, a, gate); s.launches++;
 	GARM_CHECK_LAUNCH();
 	// the frontiers are thin shells: a grid in proportion to the grid size, at most 8 blocks
 	// per SM, enough warps to hide the latency of the scattered shell
 	const unsigned blocks = unsigned(std::max<int64_t>(1, std::min<int64_t>((int64_t(total) + kFrontElemsPerBlock - 1) / kFrontElemsPerBlock, 8 * int64_t(s.numSMs))));
 	for (int pass = 1; pass <= passes; pass++) {
-		kFrontPass<D, T, Kind><<<blocks, kBlock, 0, st>>>(a, pass, gate); s.launches++;
+		launchPdl(kFrontPass<D, T, Kind>, dim3(blocks), dim3(kBlock), st, a, pass, gate); s.launches++;
 	}
 	GARM_CHECK_LAUNCH();
 	return GARM_OK;

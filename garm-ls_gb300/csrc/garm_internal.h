@@ -7,6 +7,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <utility>
 #include <cuda_runtime.h>
 
 namespace garm {
@@ -202,5 +203,22 @@ inline garm_status joinAux(State &s, int k) {
 #define GARM_TRY(x) do { garm_status _s = (x); if (_s != GARM_OK) return _s; } while (0)
 
 inline unsigned gridFor(int64_t n, int block = kBlock) { return unsigned((n + block - 1) / block); }
+
+// Launch with programmatic stream serialisation: the kernel (which calls pdlWait() before
+// touching global memory) is scheduled during the previous kernel's tail instead of after it.
+template <typename... K, typename... A>
+inline cudaError_t launchPdl(void (*kernel)(K...), dim3 grid, dim3 block, cudaStream_t st, A &&...args) {
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = grid;
+	cfg.blockDim = block;
+	cfg.dynamicSmemBytes = 0;
+	cfg.stream = st;
+	cudaLaunchAttribute at[1];
+	at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	at[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = at;
+	cfg.numAttrs = 1;
+	return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
 
 }  // namespace garm

@@ -469,6 +469,7 @@ __device__ __forceinline__ float godunovSq2(bool neg, const Ratio2 &m, const Rat
 // GridBasedData.h:47).  Used where columns give too little parallelism.
 template <int D, typename T, int Mode>
 __global__ void __launch_bounds__(kBlock) kReinitCells(G<D, T> g, const T *__restrict__ in, const T *base, T *out, T dt) {
+	pdlWait();
 	const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
 	if (id >= g.count()) return;
 	int i, j, k;
@@ -624,6 +625,7 @@ __device__ __forceinline__ void columnWalk(const G<D, T> &g, const T *__restrict
 
 template <int D, typename T, int Mode>
 __global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__restrict__ in, const T *base, T *out, T dt, int chunk) {
+	pdlWait();
 	const int plane = g.s[0] * (D == 3 ? g.s[1] : 1);
 	const int pidx = blockIdx.x * blockDim.x + threadIdx.x;
 	if (pidx >= plane) return;
@@ -715,6 +717,7 @@ struct TmaPlanes {
 template <int Mode>
 __global__ void __launch_bounds__(kTileX * kTileY) kReinitColumnsTiled(const __grid_constant__ CUtensorMap map, G<3, float> g, const float *__restrict__ in,
                                                                        const float *base, float *out, float dt, int chunk) {
+	pdlWait();
 	__shared__ __align__(128) unsigned char ring[kTileSlots * kTileStride];
 	__shared__ __align__(8) unsigned long long bars[kTileSlots];
 	const int sx = g.s[0], sy = g.s[1], sz = g.s[2];
@@ -818,6 +821,7 @@ template <typename T> __device__ __forceinline__ T g13(T x, T y) { const T d = x
 
 template <int D, typename T, int A, int Mode>
 __global__ void __launch_bounds__(256) kWenoSweep(G<D, T> g, const T *__restrict__ in, const T *base, T *out, T dt, int chunk) {
+	pdlWait();
 	constexpr int Stage = A == 0 ? 0 : (A == D - 1 ? 2 : 1);
 	const int sx = g.s[0], sy = g.s[1], sz = D == 3 ? g.s[2] : 1;
 	const int len = g.s[A];
@@ -901,14 +905,14 @@ static void launchSweep(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g,
 	const int sx = g.s[0], sy = g.s[1], sz = D == 3 ? g.s[2] : 1;
 	const int nLines = A == 0 ? sy * sz : (A == 1 ? sx * sz : sx * sy);
 	const dim3 grid((nLines + pl.block - 1) / pl.block, (g.s[A] + pl.chunk - 1) / pl.chunk);
-	kWenoSweep<D, T, A, Mode><<<grid, pl.block, 0, st>>>(g, in, base, out, dt, pl.chunk);
+	launchPdl(kWenoSweep<D, T, A, Mode>, grid, dim3(pl.block), st, g, in, base, out, dt, pl.chunk);
 }
 
 // One sub-stage; returns the number of kernels launched.
 template <int D, typename T, int Mode>
 static int launchReinit(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g, const T *in, const T *base, T *out, T dt) {
 	if (pl.form == kFormCells) {
-		kReinitCells<D, T, Mode><<<gridFor(g.count()), kBlock, 0, st>>>(g, in, base, out, dt);
+		launchPdl(kReinitCells<D, T, Mode>, dim3(gridFor(g.count())), dim3(kBlock), st, g, in, base, out, dt);
 		return 1;
 	}
 	if (pl.form == kFormSweeps) {
@@ -921,7 +925,7 @@ static int launchReinit(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g,
 		CUtensorMap map;
 		if (pl.form == kFormTiled && tiledMap((const float *)in, g, &map)) {
 			const dim3 grid((g.s[0] + kTileX - 1) / kTileX, (g.s[1] + kTileY - 1) / kTileY, (g.s[2] + pl.chunk - 1) / pl.chunk);
-			kReinitColumnsTiled<Mode><<<grid, kTileX * kTileY, 0, st>>>(map, g, (const float *)in, (const float *)base, (float *)out, float(dt), pl.chunk);
+			launchPdl(kReinitColumnsTiled<Mode>, grid, dim3(kTileX * kTileY), st, map, g, (const float *)in, (const float *)base, (float *)out, float(dt), pl.chunk);
 			return 1;
 		}
 	}
@@ -930,7 +934,7 @@ static int launchReinit(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g,
 	const int plane = g.s[0] * (D == 3 ? g.s[1] : 1);
 	const int sw = g.s[D - 1];
 	const dim3 grid((plane + block - 1) / block, (sw + pl.chunk - 1) / pl.chunk);
-	kReinitColumns<D, T, Mode><<<grid, block, 0, st>>>(g, in, base, out, dt, pl.chunk);
+	launchPdl(kReinitColumns<D, T, Mode>, grid, dim3(block), st, g, in, base, out, dt, pl.chunk);
 	return 1;
 }
 
