@@ -188,6 +188,25 @@ __device__ __forceinline__ void hermiteBasis(T x, T dx, T b[2][2], T d[2][2]) {
 	d[1][1] = x * (T(3) * x - T(2)) * dx;
 }
 
+// Appends this lane's `n` entries (ids[0..n)) to a work list (list/count) with one atomic per
+// warp: a warp prefix sum of the lane counts, one atomicAdd by the last lane.
+// Every lane of the warp must call it.
+__device__ __forceinline__ void warpAppend(int *list, int *count, const int *ids, int n) {
+	const unsigned lane = threadIdx.x & 31;
+	int incl = n;
+#pragma unroll
+	for (int o = 1; o < 32; o <<= 1) {
+		const int v = __shfl_up_sync(0xffffffffu, incl, o);
+		if (lane >= unsigned(o)) incl += v;
+	}
+	const int total = __shfl_sync(0xffffffffu, incl, 31);
+	int base = 0;
+	if (lane == 31 && total > 0) base = atomicAdd(count, total);
+	base = __shfl_sync(0xffffffffu, base, 31);
+	const int start = base + incl - n;
+	for (int q = 0; q < n; q++) list[start + q] = ids[q];
+}
+
 // Block-wide reductions (warp shuffles, then one warp).
 template <typename T>
 __device__ __forceinline__ T warpSum(T v) {

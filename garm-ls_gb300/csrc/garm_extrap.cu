@@ -256,24 +256,6 @@ __device__ __forceinline__ int frontNeighbour(const FrontArgs<T> &a, const Front
 
 __device__ __forceinline__ uint8_t ldLevel(const uint8_t *p) { return *(const volatile uint8_t *)p; }
 
-// Appends this lane's `n` entries (ids[0..n)) to list/count with one atomic per warp.
-// Every lane of the warp must call it.
-__device__ __forceinline__ void warpAppend(int *list, int *count, const int *ids, int n) {
-	const unsigned lane = threadIdx.x & 31;
-	int incl = n;
-#pragma unroll
-	for (int o = 1; o < 32; o <<= 1) {
-		const int v = __shfl_up_sync(0xffffffffu, incl, o);
-		if (lane >= unsigned(o)) incl += v;
-	}
-	const int total = __shfl_sync(0xffffffffu, incl, 31);
-	int base = 0;
-	if (lane == 31 && total > 0) base = atomicAdd(count, total);
-	base = __shfl_sync(0xffffffffu, base, 31);
-	const int start = base + incl - n;
-	for (int q = 0; q < n; q++) list[start + q] = ids[q];
-}
-
 // Claims element `nb` for the next frontier; true when this thread set its bit.
 __device__ __forceinline__ bool claim(unsigned *bits, int nb) {
 	const unsigned m = 1u << (nb & 31);

@@ -117,24 +117,6 @@ struct MarchCtl {
 	const unsigned long long *counter;
 };
 
-// Appends this lane's `n` cells (ids[0..n)) to list/count with one atomic per warp.
-// Every lane of the warp must call it.
-__device__ __forceinline__ void marchAppend(int *list, int *count, const int *ids, int n) {
-	const unsigned lane = threadIdx.x & 31;
-	int incl = n;
-#pragma unroll
-	for (int o = 1; o < 32; o <<= 1) {
-		const int v = __shfl_up_sync(0xffffffffu, incl, o);
-		if (lane >= unsigned(o)) incl += v;
-	}
-	const int total = __shfl_sync(0xffffffffu, incl, 31);
-	int base = 0;
-	if (lane == 31 && total > 0) base = atomicAdd(count, total);
-	base = __shfl_sync(0xffffffffu, base, 31);
-	const int start = base + incl - n;
-	for (int q = 0; q < n; q++) list[start + q] = ids[q];
-}
-
 // The relaxation as Jacobi sweeps over an active list.  Sweep s reads buffer s%2 and writes
 // min(u, Q(neighbours)) into the other for the cells of its list; a cell that changes queues
 // itself and its unseeded neighbours for sweep s+1 (once each: a per-cell stamp raised with
@@ -177,7 +159,7 @@ __global__ void __launch_bounds__(kMarchBlock) kMarch(Geom geom, T *tentA, T *te
 			}
 			if (touch) { ctl.stamp[id] = 1; ids[m++] = id; }
 		}
-		marchAppend(ctl.list[1], ctl.ints + 1, ids, m);
+		warpAppend(ctl.list[1], ctl.ints + 1, ids, m);
 	}
 	if (!gridSync(ctl.bar, err, epoch)) return;
 	int sweep = 1;
@@ -223,7 +205,7 @@ __global__ void __launch_bounds__(kMarchBlock) kMarch(Geom geom, T *tentA, T *te
 						if (nbs[q] >= 0 && !fixed[nbs[q]] && atomicMax(ctl.stamp + nbs[q], sweep + 1) < sweep + 1) ids[m++] = nbs[q];
 				}
 			}
-			marchAppend(next, nextCount, ids, m);
+			warpAppend(next, nextCount, ids, m);
 		}
 		if (!gridSync(ctl.bar, err, epoch)) break;
 	}
