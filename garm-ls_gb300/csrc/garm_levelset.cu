@@ -972,8 +972,14 @@ static ReinitPlan reinitPlanFor(cudaStream_t st, const G<D, T> &g, const T *phi,
 	if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) { cudaGetLastError(); return best; }
 	std::vector<ReinitPlan> cand;
 	cand.push_back({kFormCells, kBlock, 0});
+	// walks of the column form: fixed lengths, plus ones that split the walked axis into 4-16
+	// equal pieces, so that some block count fits the resident waves well
+	std::vector<int> colWalks = {4, 8, 16, 32};
+	for (int pieces : {4, 6, 8, 12, 16}) colWalks.push_back((g.s[D - 1] + pieces - 1) / pieces);
+	std::sort(colWalks.begin(), colWalks.end());
+	colWalks.erase(std::unique(colWalks.begin(), colWalks.end()), colWalks.end());
 	for (int b : {64, 128, 256})
-		for (int c : {4, 8, 16, 32}) cand.push_back({kFormColumns, b, c});
+		for (int c : colWalks) cand.push_back({kFormColumns, b, c});
 	if (D == 3 && sizeof(T) == 4)
 		for (int c : {4, 8, 16, 32}) cand.push_back({kFormTiled, kTileX * kTileY, c});
 	// sweeps: walks that split the longest axis into 2-8 equal pieces, plus short fixed ones
