@@ -618,11 +618,37 @@ garm_status garm_config_default(garm_config *c) {
 	return GARM_OK;
 }
 
+// The checks a grid and a configuration pass before anything is allocated, shared by
+// garm_sim_create and garm_sim_estimate_bytes (no CUDA call).
+static garm_status validateRequest(const garm_grid_desc *gd, const garm_config &c) {
+	if (gd->dim != 2 && gd->dim != 3) return GARM_INVALID;
+	if (!(gd->spacing > 0) || gd->boundary_width < 0) return GARM_INVALID;
+	for (int a = 0; a < gd->dim; a++)
+		if (gd->resolution[a] < 2 * gd->boundary_width + 1 || gd->resolution[a] > (1 << 14)) return GARM_INVALID;
+	// every grid (the node grid is the largest) holds fewer than 2^31 points: 32-bit indices
+	int64_t nodes = 1, faces = 0;
+	for (int a = 0; a < gd->dim; a++) nodes *= int64_t(gd->resolution[a]) + 1;
+	for (int a = 0; a < gd->dim; a++) {
+		int64_t f = 1;
+		for (int b = 0; b < gd->dim; b++) f *= int64_t(gd->resolution[b]) + (b == a ? 1 : 0);
+		faces += f;
+	}
+	if (nodes >= (int64_t(1) << 31) || faces >= (int64_t(1) << 31)) return GARM_INVALID;
+	if (c.precision != GARM_PRECISION_FP64 && c.precision != GARM_PRECISION_MIXED) return GARM_INVALID;
+	if (c.reinit_iters < 0 || c.cg_max_iters < 0 || !(c.cg_tolerance > 0) || c.cg_cells_per_block < 0) return GARM_INVALID;
+	if (c.record_volume != 0 && c.record_volume != 1) return GARM_INVALID;
+	if (c.restart_newton != 0 && c.restart_newton != 1) return GARM_INVALID;
+	if (c.fast_marching != 0 && c.fast_marching != 1) return GARM_INVALID;
+	// extrapolation passes are counted in a level byte
+	if (!(c.boundary_extrap_radius <= 240.0) || !(c.air_extrap_radius <= 240.0)) return GARM_INVALID;
+	return GARM_OK;
+}
+
 garm_status garm_sim_estimate_bytes(const garm_grid_desc *gd, const garm_config *cfg, size_t *bytes) {
 	if (!gd || !bytes) return GARM_INVALID;
-	if (gd->dim != 2 && gd->dim != 3) return GARM_INVALID;
 	garm_config c;
 	if (cfg) c = *cfg; else garm_config_default(&c);
+	GARM_TRY(validateRequest(gd, c));
 	State s;
 	s.dryRun = true;
 	s.cfg = c;
@@ -650,19 +676,9 @@ garm_status garm_sim_estimate_bytes(const garm_grid_desc *gd, const garm_config 
 garm_status garm_sim_create(const garm_grid_desc *gd, const garm_config *cfg, void *stream, garm_sim **out) {
 	if (!gd || !out) return GARM_INVALID;
 	*out = nullptr;
-	if (gd->dim != 2 && gd->dim != 3) return GARM_INVALID;
-	if (!(gd->spacing > 0) || gd->boundary_width < 0) return GARM_INVALID;
-	for (int a = 0; a < gd->dim; a++)
-		if (gd->resolution[a] < 2 * gd->boundary_width + 1 || gd->resolution[a] > (1 << 14)) return GARM_INVALID;
 	garm_config c;
 	if (cfg) c = *cfg; else garm_config_default(&c);
-	if (c.precision != GARM_PRECISION_FP64 && c.precision != GARM_PRECISION_MIXED) return GARM_INVALID;
-	if (c.reinit_iters < 0 || c.cg_max_iters < 0 || !(c.cg_tolerance > 0) || c.cg_cells_per_block < 0) return GARM_INVALID;
-	if (c.record_volume != 0 && c.record_volume != 1) return GARM_INVALID;
-	if (c.restart_newton != 0 && c.restart_newton != 1) return GARM_INVALID;
-	if (c.fast_marching != 0 && c.fast_marching != 1) return GARM_INVALID;
-	// extrapolation passes are counted in a level byte
-	if (!(c.boundary_extrap_radius <= 240.0) || !(c.air_extrap_radius <= 240.0)) return GARM_INVALID;
+	GARM_TRY(validateRequest(gd, c));
 
 	garm_sim *sim = new (std::nothrow) garm_sim();
 	if (!sim) return GARM_OOM;
@@ -709,8 +725,6 @@ garm_status garm_sim_create(const garm_grid_desc *gd, const garm_config *cfg, vo
 		} else s.F[a] = 0;
 		s.Ftot += s.F[a];
 	}
-	// every grid (cells, nodes, faces) must index with 32-bit integers
-	if (s.NN >= (int64_t(1) << 31) || s.Ftot >= (int64_t(1) << 31)) { freeAll(s); delete sim; return GARM_INVALID; }
 	garm_status r = allocState(s);
 	if (r == GARM_OK && D == 3 && s.cfg.record_volume) r = loadVolumeTables();  // before any step capture
 	if (r == GARM_OK) r = GARM_DISPATCH(s, initBoundary, s);           // Boundary ctor → reset()

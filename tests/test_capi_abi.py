@@ -98,3 +98,24 @@ def test_new_config_fields_are_validated_without_a_gpu(garm_lib):
     size = (C.c_int * 3)(20, 20, 20)
     assert garm_lib.garm_reinit_plan_set(3, capi.PRECISION_MIXED, size, 7, 128, 8) == capi.INVALID
     assert garm_lib.garm_reinit_plan_set(3, capi.PRECISION_MIXED, size, 3, 100, 8) == capi.INVALID
+
+
+def test_estimate_bytes_validates_like_create(garm_lib):
+    """garm_sim_estimate_bytes applies the grid and configuration checks of garm_sim_create
+    before sizing anything, and sizes a valid request without a GPU."""
+    n = C.c_size_t()
+    est = garm_lib.garm_sim_estimate_bytes
+    ok = capi.grid_desc(3, [32, 32, 32], 1 / 32, [1.0, 1.0, 1.0])
+    assert est(C.byref(ok), None, C.byref(n)) == capi.OK and n.value > 0
+    small = n.value
+    big = capi.grid_desc(3, [64, 64, 64], 1 / 64, [1.0, 1.0, 1.0])
+    assert est(C.byref(big), None, C.byref(n)) == capi.OK and 6 * small < n.value < 10 * small
+    for grid in (capi.grid_desc(3, [0, 8, 8], 0.1, [0, 0, 0]), capi.grid_desc(3, [-4, 8, 8], 0.1, [0, 0, 0]),
+                 capi.grid_desc(3, [3, 3, 3], 0.1, [0, 0, 0]), capi.grid_desc(3, [1300, 1300, 1300], 1e-3, [0, 0, 0]),
+                 capi.grid_desc(3, [20000, 8, 8], 0.1, [0, 0, 0]), capi.grid_desc(3, [8, 8, 8], 0.0, [0, 0, 0]),
+                 capi.grid_desc(4, [8, 8, 8], 0.1, [0, 0, 0])):
+        assert est(C.byref(grid), None, C.byref(n)) == capi.INVALID, list(grid.resolution)
+    for field, bad in (("precision", 7), ("fast_marching", 2), ("cg_tolerance", 0.0), ("air_extrap_radius", 300.0)):
+        cfg = host_default_config(**{field: bad})
+        assert est(C.byref(ok), C.byref(cfg), C.byref(n)) == capi.INVALID, field
+    assert est(None, None, C.byref(n)) == capi.INVALID and est(C.byref(ok), None, None) == capi.INVALID
