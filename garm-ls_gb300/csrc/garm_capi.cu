@@ -176,6 +176,7 @@ garm_status allocState(State &s) {
 	GARM_TRY(dalloc(s, &s.dtDev, 64));
 	GARM_TRY(dalloc(s, &s.clockDev, 64));
 	GARM_TRY(dalloc(s, &s.restartFlag, 64));
+	GARM_TRY(dalloc(s, &s.reinitErr, 64));
 	GARM_TRY(dalloc(s, &s.stepCounter, 64));
 	GARM_TRY(dalloc(s, &s.statsDev, size_t(kStatsCap) * kStatsSlots * 8));
 	if (s.dryRun) return GARM_OK;
@@ -324,7 +325,7 @@ garm_status download(State &s, int field, void *host, size_t bytes) {
 // Outside a step the fast-marching relaxation reports its status on the host.
 garm_status reinitChecked(State &s) {
 	GARM_TRY(GARM_DISPATCH(s, reinitialize, s));
-	return s.cfg.fast_marching ? marchStatus(s, nullptr) : GARM_OK;
+	return s.cfg.fast_marching ? marchStatus(s, nullptr) : tiledReinitStatus(s.stream, s.reinitErr);
 }
 garm_status restartChecked(State &s) {
 	GARM_TRY(GARM_DISPATCH(s, restart, s));
@@ -420,7 +421,7 @@ garm_status enqueueAutoDt(State &s) {
 garm_status readRecords(State &s, int k, garm_step_stats *S) {
 	if (cudaMemcpyAsync(s.statsHost, s.statsDev, size_t(kStatsCap) * kStatsSlots * 8, cudaMemcpyDeviceToHost, s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
 	if (cudaStreamSynchronize(s.stream) != cudaSuccess) return GARM_CUDA_ERROR;
-	GARM_TRY(tiledReinitStatus(s.stream));
+	GARM_TRY(tiledReinitStatus(s.stream, s.reinitErr));
 	garm_status worst = GARM_OK;
 	for (int q = 0; q < k; q++) {
 		const double *rec = s.statsHost + ((s.hostSteps - 1 - q + kStatsCap) % kStatsCap) * kStatsSlots;
@@ -924,29 +925,36 @@ garm_status garm_stage_enforce_boundary_level_set(garm_sim *sim, double tol) { S
 
 garm_status garm_reinit_host(int dim, const int *size, double spacing, double *phi, int iters, double cfl, int precision) {
 	if ((dim != 2 && dim != 3) || !size || !phi || !(spacing > 0) || iters < 0) return GARM_INVALID;
+	if (precision != GARM_PRECISION_FP64 && precision != GARM_PRECISION_MIXED) return GARM_INVALID;
 	int64_t n = 1;
-	for (int a = 0; a < dim; a++) { if (size[a] <= 0) return GARM_INVALID; n *= size[a]; }
+	for (int a = 0; a < dim; a++) { if (size[a] <= 0 || size[a] > (1 << 14)) return GARM_INVALID; n *= size[a]; }
+	if (n >= (int64_t(1) << 31)) return GARM_INVALID;  // 32-bit cell indices
 	const bool f32 = precision == GARM_PRECISION_MIXED;
 	const size_t e = f32 ? 4 : 8;
+	// three planes, then the error flag of the tiled form on its own 16-byte line
+	const size_t planes = (size_t(n) * e * 3 + 15) / 16 * 16;
 	void *buf = nullptr, *stage = nullptr;
-	if (cudaMalloc(&buf, size_t(n) * e * 3) != cudaSuccess) { cudaGetLastError(); return GARM_OOM; }
+	if (cudaMalloc(&buf, planes + 16) != cudaSuccess) { cudaGetLastError(); return GARM_OOM; }
 	if (cudaMalloc(&stage, size_t(n) * 8) != cudaSuccess) { cudaGetLastError(); cudaFree(buf); return GARM_OOM; }
+	int *err = reinterpret_cast<int *>(static_cast<char *>(buf) + planes);
 	garm_status r = GARM_OK;
 	cudaStream_t st = nullptr;
-	if (cudaMemcpy(stage, phi, size_t(n) * 8, cudaMemcpyHostToDevice) != cudaSuccess) r = GARM_CUDA_ERROR;
+	if (cudaMemset(err, 0, sizeof(int)) != cudaSuccess) r = GARM_CUDA_ERROR;
+	if (r == GARM_OK && cudaMemcpy(stage, phi, size_t(n) * 8, cudaMemcpyHostToDevice) != cudaSuccess) r = GARM_CUDA_ERROR;
 	if (r == GARM_OK) {
 		if (f32) {
 			float *p = (float *)buf;
 			kDeinterleave<float><<<gridFor(n), kBlock>>>((const double *)stage, 1, n, p, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
-			r = dim == 2 ? reinitRaw<2, float>(st, size, spacing, p, p + n, p + 2 * n, iters, cfl) : reinitRaw<3, float>(st, size, spacing, p, p + n, p + 2 * n, iters, cfl);
+			r = dim == 2 ? reinitRaw<2, float>(st, size, spacing, p, p + n, p + 2 * n, iters, cfl, err) : reinitRaw<3, float>(st, size, spacing, p, p + n, p + 2 * n, iters, cfl, err);
 			if (r == GARM_OK) kInterleave<float><<<gridFor(n), kBlock>>>((double *)stage, 1, n, p, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
 		} else {
 			double *p = (double *)buf;
 			cudaMemcpy(p, stage, size_t(n) * 8, cudaMemcpyDeviceToDevice);
-			r = dim == 2 ? reinitRaw<2, double>(st, size, spacing, p, p + n, p + 2 * n, iters, cfl) : reinitRaw<3, double>(st, size, spacing, p, p + n, p + 2 * n, iters, cfl);
+			r = dim == 2 ? reinitRaw<2, double>(st, size, spacing, p, p + n, p + 2 * n, iters, cfl, err) : reinitRaw<3, double>(st, size, spacing, p, p + n, p + 2 * n, iters, cfl, err);
 			if (r == GARM_OK) cudaMemcpy(stage, p, size_t(n) * 8, cudaMemcpyDeviceToDevice);
 		}
 	}
+	if (r == GARM_OK) r = tiledReinitStatus(st, err);
 	if (r == GARM_OK && cudaMemcpy(phi, stage, size_t(n) * 8, cudaMemcpyDeviceToHost) != cudaSuccess) r = GARM_CUDA_ERROR;
 	cudaFree(buf);
 	cudaFree(stage);

@@ -111,6 +111,7 @@ struct State {
 	double *clockDev = nullptr;
 	int *restartFlag = nullptr;
 	const int *gate = nullptr;
+	int *reinitErr = nullptr;          // set by a tiled reinitialisation whose staged plane did not arrive
 	bool inStep = false;               // enqueueing a step: stage errors go to its device record
 	double *statsDev = nullptr;        // kStatsSlots doubles per recorded step
 	unsigned long long *stepCounter = nullptr;  // device count of started steps
@@ -153,7 +154,7 @@ template <int D, typename T> garm_status reinitPlanInfo(State &s, int *form, int
 garm_status pinReinitPlan(int dim, int esz, const int *size, int form, int block, int chunk);
 // GARM_TIMEOUT once a TMA-staged plane of the tiled reinitialisation form did not arrive
 // within its bounded wait (sticky); synchronises the stream.
-garm_status tiledReinitStatus(cudaStream_t st);
+garm_status tiledReinitStatus(cudaStream_t st, const int *err);
 template <int D, typename T> garm_status extrapolateToCollider(State &s);
 template <int D, typename T> garm_status checkReferenceMap(State &s, int *keep, int *tot, int *bad);
 template <int D, typename T> garm_status checkReferenceMapAsync(State &s, bool record);
@@ -187,7 +188,7 @@ __global__ void kStepDt(const unsigned long long *maxBits, double dx, double *cl
 template <int D, typename T> garm_status copyField(State &s, void *dst, const void *src, int64_t n);
 
 // Standalone WENO5 reinitialisation on raw device planes.
-template <int D, typename T> garm_status reinitRaw(cudaStream_t st, const int *size, double dx, T *phi, T *a, T *b, int iters, double cfl);
+template <int D, typename T> garm_status reinitRaw(cudaStream_t st, const int *size, double dx, T *phi, T *a, T *b, int iters, double cfl, int *err);
 
 inline garm_status cudaStatus(cudaError_t e) { return e == cudaSuccess ? GARM_OK : GARM_CUDA_ERROR; }
 // Work after forkAux(k) on s.aux runs beside work on s.stream until joinAux(k).

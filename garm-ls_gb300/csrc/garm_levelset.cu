@@ -649,8 +649,6 @@ constexpr int kTileBytes = kTileRow * kTileRows * 4;
 constexpr int kTileStride = (kTileBytes + 127) / 128 * 128;
 constexpr unsigned long long kTileWaitNs = 1000000000ull;  // a plane not staged within 1 s: error
 
-__device__ int g_tiledError = 0;
-
 __device__ __forceinline__ unsigned smemAddr(const void *p) { return unsigned(__cvta_generic_to_shared(p)); }
 
 struct TmaPlanes {
@@ -659,6 +657,7 @@ struct TmaPlanes {
 	unsigned char *ring;
 	unsigned long long *bars;
 	int w0, w1, x0, y0, tx, ty;
+	int *err;  // the owner's error flag, set when a plane did not arrive in time
 	const float *cur = nullptr;
 
 	__device__ void issue(int w) const {
@@ -697,7 +696,7 @@ struct TmaPlanes {
 			}
 		}
 		if (__syncthreads_or(!done)) {
-			if (threadIdx.x == 0) atomicExch(&g_tiledError, 1);
+			if (threadIdx.x == 0) atomicExch(err, 1);
 			return false;
 		}
 		cur = reinterpret_cast<const float *>(ring + slot * kTileStride);
@@ -716,7 +715,7 @@ struct TmaPlanes {
 
 template <int Mode>
 __global__ void __launch_bounds__(kTileX * kTileY) kReinitColumnsTiled(const __grid_constant__ CUtensorMap map, G<3, float> g, const float *__restrict__ in,
-                                                                       const float *base, float *out, float dt, int chunk) {
+                                                                       const float *base, float *out, float dt, int chunk, int *err) {
 	pdlWait();
 	__shared__ __align__(128) unsigned char ring[kTileSlots * kTileStride];
 	__shared__ __align__(8) unsigned long long bars[kTileSlots];
@@ -732,7 +731,7 @@ __global__ void __launch_bounds__(kTileX * kTileY) kReinitColumnsTiled(const __g
 		if (i < sx && j < sy) columnWalk<3, float, Mode>(g, in, base, out, dt, i + j * sx, w0, w1, src);
 		return;
 	}
-	TmaPlanes src{&map, ring, bars, w0, w1, x0, y0, tx, ty};
+	TmaPlanes src{&map, ring, bars, w0, w1, x0, y0, tx, ty, err};
 	src.start();
 	columnWalk<3, float, Mode>(g, in, base, out, dt, (x0 + tx) + (y0 + ty) * sx, w0, w1, src);
 }
@@ -790,10 +789,12 @@ static bool tiledMap(const float *in, const G<3, float> &g, CUtensorMap *out) {
 	return true;
 }
 
-// Error flag of the tiled form (a staged plane that did not arrive in time); synchronises.
-garm_status tiledReinitStatus(cudaStream_t st) {
+// The error flag of the tiled form (a staged plane that did not arrive in time) that the
+// launches on `st` write to `err`; synchronises.  The flag stays set: the level set of a
+// reinitialisation that gave up is not usable.
+garm_status tiledReinitStatus(cudaStream_t st, const int *err) {
 	int e = 0;
-	if (cudaMemcpyFromSymbolAsync(&e, g_tiledError, sizeof(int), 0, cudaMemcpyDeviceToHost, st) != cudaSuccess) return GARM_CUDA_ERROR;
+	if (cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return GARM_CUDA_ERROR;
 	if (cudaStreamSynchronize(st) != cudaSuccess) return GARM_CUDA_ERROR;
 	return e ? GARM_TIMEOUT : GARM_OK;
 }
@@ -910,7 +911,7 @@ static void launchSweep(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g,
 
 // One sub-stage; returns the number of kernels launched.
 template <int D, typename T, int Mode>
-static int launchReinit(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g, const T *in, const T *base, T *out, T dt) {
+static int launchReinit(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g, const T *in, const T *base, T *out, T dt, int *err) {
 	if (pl.form == kFormCells) {
 		launchPdl(kReinitCells<D, T, Mode>, dim3(gridFor(g.count())), dim3(kBlock), st, g, in, base, out, dt);
 		return 1;
@@ -925,7 +926,7 @@ static int launchReinit(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g,
 		CUtensorMap map;
 		if (pl.form == kFormTiled && tiledMap((const float *)in, g, &map)) {
 			const dim3 grid((g.s[0] + kTileX - 1) / kTileX, (g.s[1] + kTileY - 1) / kTileY, (g.s[2] + pl.chunk - 1) / pl.chunk);
-			launchPdl(kReinitColumnsTiled<Mode>, grid, dim3(kTileX * kTileY), st, map, g, (const float *)in, (const float *)base, (float *)out, float(dt), pl.chunk);
+			launchPdl(kReinitColumnsTiled<Mode>, grid, dim3(kTileX * kTileY), st, map, g, (const float *)in, (const float *)base, (float *)out, float(dt), pl.chunk, err);
 			return 1;
 		}
 	}
@@ -958,7 +959,7 @@ std::map<PlanKey, ReinitPlan> g_plans;
 // that stream once per candidate.  Under capture, or when a timing
 // call fails, the plan is the default column form and nothing is cached.
 template <int D, typename T>
-static ReinitPlan reinitPlanFor(cudaStream_t st, const G<D, T> &g, const T *phi, T *scratch, T dt) {
+static ReinitPlan reinitPlanFor(cudaStream_t st, const G<D, T> &g, const T *phi, T *scratch, T dt, int *err) {
 	int dev = 0;
 	cudaGetDevice(&dev);
 	const PlanKey key{dev, D, int(sizeof(T)), g.s[0], g.s[1], D == 3 ? g.s[2] : 1};
@@ -997,11 +998,11 @@ static ReinitPlan reinitPlanFor(cudaStream_t st, const G<D, T> &g, const T *phi,
 	bool ok = true;
 	float bestMs = 1e30f;
 	for (ReinitPlan &c : cand) {
-		launchReinit<D, T, 0>(c, st, g, phi, nullptr, scratch, dt);  // warm
+		launchReinit<D, T, 0>(c, st, g, phi, nullptr, scratch, dt, err);  // warm
 		float shortest = 1e30f;
 		for (int rep = 0; rep < 3 && ok; rep++) {
 			cudaEventRecord(e0, st);
-			launchReinit<D, T, 0>(c, st, g, phi, nullptr, scratch, dt);
+			launchReinit<D, T, 0>(c, st, g, phi, nullptr, scratch, dt, err);
 			cudaEventRecord(e1, st);
 			if (cudaEventSynchronize(e1) != cudaSuccess) { ok = false; break; }
 			float ms = 0;
@@ -1040,17 +1041,17 @@ garm_status pinReinitPlan(int dim, int esz, const int *size, int form, int block
 // no sub-stage writes a plane it reads; after a multiple of three iterations the
 // result is back in phi, otherwise one copy puts it there.
 template <int D, typename T>
-static garm_status reinitLoop(cudaStream_t st, const G<D, T> &g, T *phi, T *A, T *B, int iters, double cfl, long long *launches) {
+static garm_status reinitLoop(cudaStream_t st, const G<D, T> &g, T *phi, T *A, T *B, int iters, double cfl, long long *launches, int *err) {
 	const T dt = T(double(g.dx) * cfl);
 	if (iters <= 0) return GARM_OK;
-	const ReinitPlan pl = reinitPlanFor<D, T>(st, g, phi, A, dt);
+	const ReinitPlan pl = reinitPlanFor<D, T>(st, g, phi, A, dt, err);
 	T *buf[3] = {phi, A, B};
 	int cur = 0, n = 0;
 	for (int it = 0; it < iters; it++) {
 		T *u0 = buf[cur], *X = buf[(cur + 1) % 3], *Y = buf[(cur + 2) % 3];
-		n += launchReinit<D, T, 0>(pl, st, g, u0, nullptr, X, dt);
-		n += launchReinit<D, T, 1>(pl, st, g, X, u0, Y, dt);
-		n += launchReinit<D, T, 2>(pl, st, g, Y, u0, X, dt);
+		n += launchReinit<D, T, 0>(pl, st, g, u0, nullptr, X, dt, err);
+		n += launchReinit<D, T, 1>(pl, st, g, X, u0, Y, dt, err);
+		n += launchReinit<D, T, 2>(pl, st, g, Y, u0, X, dt, err);
 		cur = (cur + 1) % 3;
 	}
 	if (cur != 0 && cudaMemcpyAsync(phi, buf[cur], size_t(g.count()) * sizeof(T), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
@@ -1065,25 +1066,25 @@ garm_status reinitialize(State &s) {
 	// fast-marching configuration: FastMarching over a band of 15 cells (LevelSetLiquid.cpp:1151-1152)
 	if (s.cfg.fast_marching) return fastMarch<D, T>(s, s.phi, nullptr, 15, s.inStep);
 	const G<D, T> g = cellGrid<D, T>(s.geom);
-	return reinitLoop<D, T>(s.stream, g, (T *)s.phi, (T *)s.rA, (T *)s.rB, s.cfg.reinit_iters, s.cfg.reinit_cfl, &s.launches);
+	return reinitLoop<D, T>(s.stream, g, (T *)s.phi, (T *)s.rA, (T *)s.rB, s.cfg.reinit_iters, s.cfg.reinit_cfl, &s.launches, s.reinitErr);
 }
 
 // The cached (or freshly tuned) plan of this simulation's grid, for reporting.
 template <int D, typename T>
 garm_status reinitPlanInfo(State &s, int *form, int *block, int *chunk, float *ms) {
 	const G<D, T> g = cellGrid<D, T>(s.geom);
-	const ReinitPlan pl = reinitPlanFor<D, T>(s.stream, g, (const T *)s.phi, (T *)s.rA, T(double(g.dx) * s.cfg.reinit_cfl));
+	const ReinitPlan pl = reinitPlanFor<D, T>(s.stream, g, (const T *)s.phi, (T *)s.rA, T(double(g.dx) * s.cfg.reinit_cfl), s.reinitErr);
 	*form = pl.form; *block = pl.block; *chunk = pl.chunk; *ms = pl.ms;
 	return GARM_OK;
 }
 
 template <int D, typename T>
-garm_status reinitRaw(cudaStream_t st, const int *size, double dx, T *phi, T *a, T *b, int iters, double cfl) {
+garm_status reinitRaw(cudaStream_t st, const int *size, double dx, T *phi, T *a, T *b, int iters, double cfl, int *err) {
 	G<D, T> g;
 	g.s[0] = size[0]; g.s[1] = size[1]; g.s[2] = D == 3 ? size[2] : 1;
 	for (int q = 0; q < 3; q++) g.org[q] = T(0);
 	g.dx = T(dx); g.inv = T(1.0 / dx);
-	return reinitLoop<D, T>(st, g, phi, a, b, iters, cfl, nullptr);
+	return reinitLoop<D, T>(st, g, phi, a, b, iters, cfl, nullptr, err);
 }
 
 // ---------------------------------------------------------------------------
@@ -1632,7 +1633,7 @@ garm_status enforceBoundaryLevelSet(State &s, void *field, double tol) {
 	template garm_status generateCurrentFields<D, T>(State &); \
 	template garm_status reinitialize<D, T>(State &); \
 	template garm_status reinitPlanInfo<D, T>(State &, int *, int *, int *, float *); \
-	template garm_status reinitRaw<D, T>(cudaStream_t, const int *, double, T *, T *, T *, int, double); \
+	template garm_status reinitRaw<D, T>(cudaStream_t, const int *, double, T *, T *, T *, int, double, int *); \
 	template garm_status checkReferenceMap<D, T>(State &, int *, int *, int *); \
 	template garm_status checkReferenceMapAsync<D, T>(State &, bool); \
 	template garm_status restart<D, T>(State &); \

@@ -58,6 +58,7 @@ extern "C" garm_status garm_reinit_device_noalloc(int dim, const int *size, doub
 	double *scratch = nullptr;
 	GARM_TRY(scratchOnCurrentDevice(&scratch));
 	const cudaStream_t st = static_cast<cudaStream_t>(stream);
-	if (dim == 2) return garm::reinitRaw<2, double>(st, size, spacing, phi, scratch, scratch + n, iters, cfl);
-	return garm::reinitRaw<3, double>(st, size, spacing, phi, scratch, scratch + n, iters, cfl);
+	// FP64 never takes the tiled form, the only one with an error flag
+	if (dim == 2) return garm::reinitRaw<2, double>(st, size, spacing, phi, scratch, scratch + n, iters, cfl, nullptr);
+	return garm::reinitRaw<3, double>(st, size, spacing, phi, scratch, scratch + n, iters, cfl, nullptr);
 }
