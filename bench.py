@@ -39,7 +39,7 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["garm", "reference"], default="garm")
-    p.add_argument("--n", type=int, default=128, help="interior cells per axis")
+    p.add_argument("--n", type=int, default=None, help="interior cells per axis (128; 256 for the drop workload)")
     p.add_argument("--precision", choices=["fp64", "mixed"], default="fp64", help="form timed as `value`")
     p.add_argument("--no-mixed", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -47,14 +47,19 @@ def parse():
     p.add_argument("--no-batch", action="store_true")
     p.add_argument("--no-default-build", action="store_true",
                    help="skip the same workload in the reference's default build (Newton restart + fast marching)")
-    p.add_argument("--workload", choices=["dam", "batch", "serve"], default="dam",
+    p.add_argument("--seed", type=int, default=0, help="drop: seed of the sphere's centre")
+    p.add_argument("--workload", choices=["dam", "batch", "serve", "drop"], default="dam",
                    help="dam: the 128^3 dam break (default line, with mixed and batch sub-objects); "
-                        "batch: 48 uneven pool scenes only; serve: the Poisson request stream only")
+                        "batch: 48 uneven pool scenes only; serve: the Poisson request stream only; "
+                        "drop: the 256^3 drop into a pool, mixed against FP64 over K steps with per-field errors")
     p.add_argument("--batch-scenes", type=int, default=48)
     p.add_argument("--reinit-plan", default=None, metavar="FORM,THREADS,CELLS",
                    help="pin the reinitialisation launch plan of the dam-break grid instead of autotuning it")
     p.add_argument("--requests", type=int, default=48, help="serve: number of requests")
-    return p.parse_args()
+    args = p.parse_args()
+    if args.n is None:
+        args.n = 256 if args.workload == "drop" else 128
+    return args
 
 
 def dist_env():
@@ -214,6 +219,33 @@ def reinit_roofline(sim, torch, stream, n_cells: int, esz: int, iters: int, peak
             "traffic": None, "ms_per_launch": round(ms_per_launch, 4), "algorithmic_bytes_per_launch": int(bytes_per_launch)}
 
 
+def field_errors(test, ref, dx: float) -> dict:
+    """Per-field L∞ and RMS of simulation `test` against simulation `ref` on the same grid:
+    φ and ξ in units of dx (φ also over the band |φ| <= 3 dx), u relative to max|u| over
+    the faces of the fluid domain (fraction < 1; solid-ring faces hold the wall
+    condition's sign ties)."""
+    import numpy as np
+    from garm import capi
+
+    def linf_rms(d):
+        return (float(np.max(d)) if d.size else 0.0), (float(np.sqrt(np.mean(d * d))) if d.size else 0.0)
+
+    pr = ref.download(capi.FIELD_LEVEL_SET)
+    d = np.abs(test.download(capi.FIELD_LEVEL_SET) - pr)
+    band = np.abs(pr) <= 3 * dx
+    out = {"phi_linf_band3dx_dx": float(np.max(d[band], initial=0.0)) / dx}
+    a, b = linf_rms(d)
+    out.update({"phi_linf_dx": a / dx, "phi_rms_dx": b / dx})
+    ur = ref.download(capi.FIELD_VELOCITY)
+    scale = max(float(np.max(np.abs(ur))), 1e-300)
+    fluid = ref.download(capi.FIELD_FRACTION) < 1
+    a, b = linf_rms(np.abs(test.download(capi.FIELD_VELOCITY) - ur)[fluid])
+    out.update({"u_linf_rel_fluid_faces": a / scale, "u_rms_rel_fluid_faces": b / scale})
+    a, b = linf_rms(np.abs(test.download(capi.FIELD_REF_MAP) - ref.download(capi.FIELD_REF_MAP)))
+    out.update({"xi_linf_dx": a / dx, "xi_rms_dx": b / dx})
+    return out
+
+
 BATCH_CG_CELLS_PER_BLOCK = 262144  # measured best for the 48-scene batch (4096: 177M, 262144: 194-198M cell-steps/s)
 
 
@@ -295,6 +327,72 @@ def run_serve(args, world: int) -> dict:
     return out
 
 
+def run_drop(args, torch, stream, world: int, W: int, K: int) -> dict:
+    """The 3D drop into a pool, mixed against FP64: a pool of depth 0.3 and a sphere of
+    radius 0.12 at a seeded centre in [0.3,0.7]^2 x [0.6,0.8], every face at u_y = -1.
+    Both forms take the same dt sequence (the Simulator's CFL-1 policy on the FP64
+    form's velocity) from the same scene, one host-driven step at a time.  The mixed
+    form's per-field errors against the FP64 form are taken at steps 1, 10, 50 and K;
+    each step is timed with CUDA events, and steps after the first W make the figures."""
+    import numpy as np
+    from garm import capi, scenes
+    n = args.n
+    sc = scenes.drop(n, seed=args.seed)
+    dx = sc.grid.spacing
+    sims = {}
+    for name, prec in (("fp64", capi.PRECISION_FP64), ("mixed", capi.PRECISION_MIXED)):
+        s = capi.Simulation(sc.grid, capi.default_config(precision=prec), stream=stream.cuda_stream)
+        s.upload(capi.FIELD_LEVEL_SET, sc.phi.ravel())
+        s.upload(capi.FIELD_VELOCITY, sc.velocity)
+        s.initialize()
+        s.stage("restart")
+        sims[name] = s
+    marks = {m for m in (1, 10, 50, K) if 1 <= m <= K}
+    times = {k: [] for k in sims}
+    cg = {k: [] for k in sims}
+    launches = {k: 0 for k in sims}
+    restarts = {k: 0 for k in sims}
+    errors = {}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    for step, dt in enumerate(scenes.frame_time_steps(sims["fp64"].max_speed, K, 25, 1.0, dx), 1):
+        for name, s in sims.items():
+            l0 = s.launch_count()
+            e0.record(stream)
+            st = s.advance(dt)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            restarts[name] += st["restarted"]
+            if step > W:
+                times[name].append(e0.elapsed_time(e1))
+                cg[name].append(st["cg_iterations"])
+                launches[name] += s.launch_count() - l0
+        if step in marks:
+            errors[str(step)] = field_errors(sims["mixed"], sims["fp64"], dx)
+    clk = clocks.stop()
+    timed = max(K - W, 1)
+    legs = {}
+    for name in sims:
+        total = reduce_max(sum(times[name]), world)
+        legs[name] = {"value": world * n ** 3 * len(times[name]) / max(total * 1e-3, 1e-30), "unit": UNIT,
+                      "ms_per_step": total / timed, "p50_step_ms": statistics.median(times[name]) if times[name] else None,
+                      "p99_step_ms": float(np.percentile(times[name], 99)) if times[name] else None,
+                      "cg_iterations_mean": statistics.mean(cg[name]) if cg[name] else None,
+                      "restarts": restarts[name], "resident_bytes": sims[name].device_bytes()}
+        sims[name].close()
+    legs["mixed"]["dtype"] = "f32 storage+math, f64 dots/residual/refinement/RM test"
+    return {"value": legs["mixed"]["value"], "ms_per_step": legs["mixed"]["ms_per_step"], "clocks": clk,
+            "gpu_launches": launches["mixed"],
+            "workload": f"3D drop into a pool {n}^3 (seed {args.seed}), mixed and FP64 on one dt sequence, "
+                        f"{K} steps, the first {W} untimed",
+            "drop": {"fp64": legs["fp64"], "mixed": legs["mixed"],
+                     "speedup_vs_fp64": legs["mixed"]["value"] / legs["fp64"]["value"],
+                     "sphere": {"center": [float(c) for c in sc.meta["center"]], "radius": sc.meta["radius"]},
+                     "errors_mixed_vs_fp64": errors}}
+
+
 def run_garm(args) -> None:
     import numpy as np
     import torch
@@ -309,6 +407,20 @@ def run_garm(args) -> None:
     stream = torch.cuda.current_stream()
     capi.load()
     n, K, W = args.n, args.steps, args.warmup
+    if args.workload == "drop":
+        sub = run_drop(args, torch, stream, world, W, K)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": sub["value"], "unit": UNIT, "n_gpus": world, "steps": K,
+                              "warmup": W, "ms_per_step": sub["ms_per_step"], "higher_is_better": True,
+                              "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+                              "config": {"workload": sub["workload"], "n": n, "replicas": world,
+                                         "l2": "no flush: device state larger than L2"},
+                              "clocks": sub["clocks"], "gpu_launches": sub["gpu_launches"], "drop": sub["drop"]}),
+                  flush=True)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
     if args.workload in ("batch", "serve"):
         clocks = Clocks(local)
         clocks.start()
@@ -484,11 +596,12 @@ def run_garm(args) -> None:
         out["batch"]["speedup_vs_fp64"] = out["batch"]["value"] / value if args.precision == "fp64" else None
 
     # CPU baseline: the oracle (a CPU port of the reference's FP64 path) on this host,
-    # one step of the same 128^3 workload started from the GPU's state
+    # one step of the same 128^3 workload started from the GPU's state.  The GPU then
+    # takes the same step from the same state, and the two are compared field by field.
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as O
         o = O.OracleSim(scene.grid, sim.cfg)
-        for f in state_fields() + [capi.FIELD_LEVEL_SET, capi.FIELD_ORI_LEVEL_SET, capi.FIELD_FRACTION]:
+        for f in state_fields() + [capi.FIELD_LEVEL_SET, capi.FIELD_ORI_LEVEL_SET, capi.FIELD_TMP_LEVEL_SET, capi.FIELD_FRACTION]:
             o.upload(f, sim.download(f))
         dt = next(scenes.frame_time_steps(o.max_speed, 1, 25, 1.0, dx))
         t0 = time.perf_counter()
@@ -496,6 +609,8 @@ def run_garm(args) -> None:
         secs = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": interior / secs, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
                                "sample": f"1 oracle advance of the {n}^3 dam break from the GPU state ({secs:.1f} s)"}
+        sim.advance(dt)
+        out["parity_vs_oracle_1_step"] = {"form": args.precision, **field_errors(sim, o, dx)}
         o.close()
     sim.close()
     if rank == 0:
