@@ -172,9 +172,9 @@ struct CgArgs {
 	int *ints;     // [0] matvecs, [1] refinements
 };
 
-// Vectors written by other blocks in the previous phase.  gridSync() ends with
-// fences of GPU scope, which order these plain (L1-cacheable) loads after the
-// other blocks' stores; the read-only texture path (__ldg) is never used for them.
+// Vectors written by other blocks in the previous phase.  gridSync()'s acquire
+// load and the block barrier after it order these plain (L1-cacheable) loads after
+// the other blocks' stores; the read-only texture path (__ldg) is never used for them.
 __device__ __forceinline__ double ldcg(const double *p) { return *p; }
 __device__ __forceinline__ float ldcg(const float *p) { return *p; }
 
@@ -204,25 +204,29 @@ __device__ __forceinline__ void blockPartials(double (&acc)[NV], double *partial
 	__syncthreads();
 }
 
-// Sum of the gridDim partials of slot v, identical in every block (fixed lane
-// partition and shuffle tree: deterministic).  Lane 0 then runs `fin` on the
-// totals (scalar work done once per block) and the results are broadcast.
+// Sum of the gridDim partials of slot v, identical in every block (a fixed
+// partition of the blocks over lanes and warps and fixed shuffle trees:
+// deterministic).  Thread t loads the partials of blocks t, t + blockDim, ..., all
+// NV values of a block together, so the whole grid's partials arrive in one L2
+// round trip; warp 0 sums the warp sums from shared memory, its lane 0 runs `fin`
+// on the totals (scalar work done once per block) and the results are broadcast.
+// Shared memory: sh[0, NOUT) holds the results, sh[8 + 32 v + w] the warp sums.
 template <int NV, int NOUT, typename Fin>
 __device__ __forceinline__ void gridTotals(const double *partials, int maxBlocks, double (&out)[NOUT], double *sh, Fin fin) {
-	static_assert(NOUT >= NV, "outputs include the sums");
-	const int lane = threadIdx.x & 31;
-	if (threadIdx.x < 32) {
-		double t[NOUT];
-		// the NV partials of one block are loaded together, so their L2 round trips overlap
+	static_assert(NOUT >= NV && NOUT <= 8, "outputs include the sums");
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	const int nb = gridDim.x;
+	double t[NOUT];
 #pragma unroll
-		for (int v = 0; v < NV; v++) t[v] = 0;
-		for (int b = lane; b < (int)gridDim.x; b += 32) {
-			double q[NV];
+	for (int v = 0; v < NV; v++) t[v] = 0;
+	for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+		double q[NV];
 #pragma unroll
-			for (int v = 0; v < NV; v++) q[v] = ldcg(partials + v * maxBlocks + b);
+		for (int v = 0; v < NV; v++) q[v] = ldcg(partials + v * maxBlocks + b);
 #pragma unroll
-			for (int v = 0; v < NV; v++) t[v] += q[v];
-		}
+		for (int v = 0; v < NV; v++) t[v] += q[v];
+	}
+	auto warpTree = [&]() {
 #pragma unroll
 		for (int o = 16; o > 0; o >>= 1) {
 			double y[NV];
@@ -231,6 +235,20 @@ __device__ __forceinline__ void gridTotals(const double *partials, int maxBlocks
 #pragma unroll
 			for (int v = 0; v < NV; v++) t[v] += y[v];
 		}
+	};
+	if (w * 32 < nb) {
+		warpTree();
+		if (lane == 0) {
+#pragma unroll
+			for (int v = 0; v < NV; v++) sh[8 + v * 32 + w] = t[v];
+		}
+	}
+	__syncthreads();
+	if (w == 0) {
+		const int nl = min(nw, (nb + 31) >> 5);
+#pragma unroll
+		for (int v = 0; v < NV; v++) t[v] = lane < nl ? sh[8 + v * 32 + lane] : 0.0;
+		warpTree();
 		if (lane == 0) {
 			fin(t);
 #pragma unroll
@@ -432,7 +450,7 @@ __device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, unsigned &epoch,
 // FP64 form: one PCG on the FP64 operator.
 template <int NB>
 __global__ void __launch_bounds__(kCgBlock) kPcgFp64(CgArgs a) {
-	__shared__ double sh[3 * 16];
+	__shared__ double sh[8 + 3 * 32];  // block partials, then the grid totals' warp sums
 	const int n = *a.nDev;
 	double rr = 0, b2 = 0;
 	bool ok = true;
@@ -521,27 +539,44 @@ __device__ __forceinline__ void blockPartialsDF(DF (&acc)[NV], double *partials,
 	}
 	__syncthreads();
 }
-// Grid totals of NV double-float partials, widened to FP64 by lane 0, which then
-// runs `fin` on them; the NOUT results are broadcast to the block.
+// Grid totals of NV double-float partials in the arrangement of gridTotals (one L2
+// round trip for all partials, warp sums in shared memory at sh + 8 as float pairs,
+// a fixed order), widened to FP64 by lane 0 of warp 0, which then runs `fin` on
+// them; the NOUT results are broadcast to the block.
 template <int NV, int NOUT, typename Fin>
 __device__ __forceinline__ void gridTotalsDF(const double *partials, int maxBlocks, double (&out)[NOUT], double *sh, Fin fin) {
-	const int lane = threadIdx.x & 31;
-	if (threadIdx.x < 32) {
-		const float2 *p2 = reinterpret_cast<const float2 *>(partials);
-		double t[NOUT];
-		// the NV partials of one block are loaded together, so the L2 round trips of the
-		// values overlap
-		DF x[NV];
+	static_assert(NOUT >= NV && NOUT <= 8, "outputs include the sums");
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	const int nb = gridDim.x;
+	const float2 *p2 = reinterpret_cast<const float2 *>(partials);
+	float2 *ws = reinterpret_cast<float2 *>(sh + 8);  // [32 v + w]
+	DF x[NV];
 #pragma unroll
-		for (int v = 0; v < NV; v++) x[v] = DF{0.f, 0.f};
-		for (int b = lane; b < (int)gridDim.x; b += 32) {
-			float2 q[NV];
+	for (int v = 0; v < NV; v++) x[v] = DF{0.f, 0.f};
+	for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+		float2 q[NV];
 #pragma unroll
-			for (int v = 0; v < NV; v++) q[v] = p2[v * maxBlocks + b];  // ordered by gridSync, as ldcg
+		for (int v = 0; v < NV; v++) q[v] = p2[v * maxBlocks + b];  // ordered by gridSync, as ldcg
 #pragma unroll
-			for (int v = 0; v < NV; v++) x[v] = dfMerge(x[v], DF{q[v].x, q[v].y});
+		for (int v = 0; v < NV; v++) x[v] = dfMerge(x[v], DF{q[v].x, q[v].y});
+	}
+	if (w * 32 < nb) {
+		dfWarpSumN<NV>(x);
+		if (lane == 0) {
+#pragma unroll
+			for (int v = 0; v < NV; v++) ws[v * 32 + w] = make_float2(x[v].hi, x[v].lo);
+		}
+	}
+	__syncthreads();
+	if (w == 0) {
+		const int nl = min(nw, (nb + 31) >> 5);
+#pragma unroll
+		for (int v = 0; v < NV; v++) {
+			x[v] = DF{0.f, 0.f};
+			if (lane < nl) { const float2 q = ws[v * 32 + lane]; x[v] = DF{q.x, q.y}; }
 		}
 		dfWarpSumN<NV>(x);
+		double t[NOUT];
 #pragma unroll
 		for (int v = 0; v < NV; v++) t[v] = double(x[v].hi) + double(x[v].lo);
 		if (lane == 0) {
@@ -814,7 +849,7 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 }
 template <int NB>
 __global__ void __launch_bounds__(kCgBlock) kPcgMixed(CgArgs a) {
-	__shared__ double sh[3 * 32];
+	__shared__ double sh[8 + 3 * 32];  // block partials, then the grid totals' warp sums
 	const int n = *a.nDev;
 	unsigned epoch = 0;
 	int it = 0, repl = 0;

@@ -27,26 +27,34 @@ __device__ __forceinline__ void addRelease(unsigned *ptr, unsigned v) {
 // Grid-wide barrier with a bounded wait.  Each block adds 1 to a counter with
 // release semantics once its threads have passed __syncthreads; a block waits
 // (acquire loads) until the counter reaches gridDim.x times the number of
-// barriers passed so far.  The wait is bounded in time (checked every 1024
-// polls against the global nanosecond timer): past the limit the block sets the
-// error flag and every block leaves at its next barrier.  Returns false then.
+// barriers passed so far.  Every poll also loads the error flag, issued first so
+// that the two loads are in flight together; the flag seen with the last poll is
+// handed to the block through shared memory, so leaving the barrier costs no
+// further L2 round trip.  The wait is bounded in time (checked every 1024 polls
+// against the global nanosecond timer): past the limit the block sets the error
+// flag and returns false; every other block sees the flag while it waits at this
+// barrier or the next one and returns false too.
 __device__ inline bool gridSync(unsigned *bar, int *err, unsigned &epoch) {
+	__shared__ int blockErr;
 	__syncthreads();
 	if (threadIdx.x == 0) {
 		epoch += gridDim.x;
 		addRelease(bar, 1u);
 		unsigned long long spins = 0, start = 0;
-		while (ldAcquire(bar) < epoch) {
+		int e;
+		for (;;) {
+			e = *(volatile int *)err;
+			if (ldAcquire(bar) >= epoch || e) break;
 			if ((++spins & 1023ull) == 0) {
-				if (*(volatile int *)err) break;
 				const unsigned long long now = globalNs();
 				if (start == 0) start = now;
-				if (now - start > kBarrierWaitNs || spins > kBarrierSpinLimit) { atomicExch(err, 1); break; }
+				if (now - start > kBarrierWaitNs || spins > kBarrierSpinLimit) { atomicExch(err, 1); e = 1; break; }
 			}
 		}
+		blockErr = e;
 	}
 	__syncthreads();
-	return *(volatile int *)err == 0;
+	return blockErr == 0;
 }
 
 }  // namespace garm

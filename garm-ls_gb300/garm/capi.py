@@ -112,6 +112,7 @@ _SIGS = {
     "garm_stage_enforce_boundary_level_set": (C.c_int, [C.c_void_p, C.c_double]),
     "garm_reinit_host": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int, C.c_double, C.c_int]),
     "garm_reinit_device_noalloc": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.c_double, C.c_void_p, C.c_int, C.c_double, C.c_void_p]),
+    "garm_barrier_selftest": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]),
 }
 
 NOALLOC_MAX_CELLS = 1 << 19
@@ -344,6 +345,13 @@ class Simulation:
         else:
             raise ValueError(name)
         return None
+
+
+def barrier_selftest(blocks: int, rounds: int, never_complete: bool = False) -> tuple[int, float]:
+    """garm_barrier_selftest: (status, ms per barrier passed) of one cooperative launch."""
+    ms = C.c_double()
+    st = load().garm_barrier_selftest(int(blocks), int(rounds), int(bool(never_complete)), C.byref(ms))
+    return st, ms.value
 
 
 def estimate_bytes(grid: GridDesc, cfg: Config) -> int:

@@ -264,6 +264,14 @@ garm_status garm_reinit_host(int dim, const int *size, double spacing, double *p
 #define GARM_NOALLOC_MAX_CELLS (1 << 19)
 garm_status garm_reinit_device_noalloc(int dim, const int *size, double spacing, double *phi, int iters, double cfl, void *stream);
 
+/* Self-test of the grid barrier that the persistent pressure solve and the fast-marching
+ * relaxation use (no counterpart in the reference).  One cooperative launch of `blocks`
+ * blocks passes `rounds` barriers in a row; *ms_per_barrier is the launch's device time
+ * per barrier passed.  With never_complete = 1 the blocks wait for a count that is never
+ * reached: every wait is bounded (about 2 s), and the call returns GARM_TIMEOUT with the
+ * context still usable.  `blocks` above the co-resident limit returns GARM_INVALID. */
+garm_status garm_barrier_selftest(int blocks, int rounds, int never_complete, double *ms_per_barrier);
+
 #ifdef __cplusplus
 }
 #endif

@@ -119,3 +119,9 @@ def test_estimate_bytes_validates_like_create(garm_lib):
         cfg = host_default_config(**{field: bad})
         assert est(C.byref(ok), C.byref(cfg), C.byref(n)) == capi.INVALID, field
     assert est(None, None, C.byref(n)) == capi.INVALID and est(C.byref(ok), None, None) == capi.INVALID
+
+
+def test_barrier_selftest_validates_without_a_gpu(garm_lib):
+    ms = C.c_double()
+    for blocks, rounds, never in ((0, 10, 0), (4, 0, 0), (4, 10, 2), (-1, 10, 1)):
+        assert garm_lib.garm_barrier_selftest(blocks, rounds, never, C.byref(ms)) == capi.INVALID
