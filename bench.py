@@ -246,6 +246,14 @@ def field_errors(test, ref, dx: float) -> dict:
     return out
 
 
+def stage_ms(sim, dx: float, steps: int = 3) -> dict:
+    """Median device time of each stage of LevelSetLiquid::advance over `steps`
+    host-driven steps (CUDA events between the stages; garm_step_stats.ms_stage)."""
+    from garm import capi, scenes
+    rows = [sim.advance(dt)["ms_stage"] for dt in scenes.frame_time_steps(sim.max_speed, steps, 25, 1.0, dx)]
+    return {name: round(statistics.median(r[i] for r in rows), 4) for i, name in enumerate(capi.STAGE_NAMES)}
+
+
 BATCH_CG_CELLS_PER_BLOCK = 262144  # measured best for the 48-scene batch (4096: 177M, 262144: 194-198M cell-steps/s)
 
 
@@ -484,6 +492,7 @@ def run_garm(args) -> None:
         step_ms.append(st["ms_total"])
         cg_it.append(st["cg_iterations"])
         restarts += st["restarted"]
+    stages = stage_ms(sim, dx)
     barrier(world)
     value = replica_value(world, interior, K, elapsed_ms)
     peaks = measured_peaks()
@@ -497,6 +506,7 @@ def run_garm(args) -> None:
                    "l2": "no flush: device state > 1 GB, larger than L2"},
         "p50_step_ms": statistics.median(step_ms), "p99_step_ms": float(np.percentile(step_ms, 99)),
         "cg_iterations_mean": statistics.mean(cg_it), "restarts": restarts, "graph_replay": sim.graph_active(),
+        "stage_ms": stages,
         "clocks": clk, "gpu_launches": launches,
     }
     if rank == 0:
@@ -559,9 +569,10 @@ def run_garm(args) -> None:
             mms.append(st["ms_total"])
             mcg.append(st["cg_iterations"])
         mval = world * interior * K / (mix_ms * 1e-3)
+        mstages = stage_ms(mix, dx)
         out["mixed"] = {"value": mval, "unit": UNIT, "ms_per_step": mix_ms / K, "p50_step_ms": statistics.median(mms),
                         "p99_step_ms": float(np.percentile(mms, 99)), "phi_err_dx_band3dx_after_1_step_vs_fp64": phi_err_band, "phi_err_dx_all_cells_after_1_step_vs_fp64": phi_err,
-                        "speedup_vs_fp64": mval / value, "cg_iterations_mean": statistics.mean(mcg),
+                        "speedup_vs_fp64": mval / value, "cg_iterations_mean": statistics.mean(mcg), "stage_ms": mstages,
                         "dtype": "f32 storage+math, f64 dots/residual/refinement/RM test"}
         if rank == 0:
             out["mixed"]["roofline"] = reinit_roofline(mix, torch, stream, int(scene.phi.size), 4, 30, peaks)

@@ -263,6 +263,19 @@ __device__ __forceinline__ void gridTotals(const double *partials, int maxBlocks
 
 struct NoFin { __device__ void operator()(double *) const {} };
 
+// Scalar work of an iteration is done once, by the lane that finishes the grid totals,
+// and handed to the block through the broadcast totals: a decision as 0.0 / 1.0 and
+// the FP32 β, α packed into the bits of one double.  The other threads read both with
+// integer operations.  GB300 issues FP64 (and FP64 to FP32 conversions) at 1/64 of the
+// FP32 rate, so the same scalar work in all 16 warps of a block costs microseconds per
+// iteration.
+__device__ __forceinline__ double packFloats(double hi, double lo) {
+	return __hiloint2double(__float_as_int(float(hi)), __float_as_int(float(lo)));
+}
+__device__ __forceinline__ float packedHi(double p) { return __int_as_float(__double2hiint(p)); }
+__device__ __forceinline__ float packedLo(double p) { return __int_as_float(__double2loint(p)); }
+__device__ __forceinline__ bool flagSet(double f) { return __double_as_longlong(f) != 0; }
+
 __device__ __forceinline__ double mulRn(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float mulRn(float a, float b) { return __fmul_rn(a, b); }
 
@@ -325,8 +338,8 @@ __device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, unsigned &epoch,
 		blockPartials<3>(acc, a.partials, a.maxBlocks, sh);
 	}
 	if (!gridSync(a.bar, a.err, epoch)) { *ok = false; return 0; }
-	double tot[5];
-	gridTotals<3, 5>(a.partials, a.maxBlocks, tot, sh, [](double *t) { t[3] = 0; t[4] = t[0] / t[1]; });
+	double tot[6];
+	gridTotals<3, 6>(a.partials, a.maxBlocks, tot, sh, [](double *t) { t[3] = 0; t[4] = t[0] / t[1]; t[5] = 0; });
 	double gamma = tot[0];
 	const double rhsNorm2 = tot[2];
 	*outB2 = rhsNorm2;
@@ -428,15 +441,18 @@ __device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, unsigned &epoch,
 		blockPartials<3>(acc, a.partials, a.maxBlocks, sh);
 		// β = γ/γ_old and α = γ/(δ - βγ/α_old) with the reciprocals of the known γ_old and
 		// γ_old·α_old formed before the barrier: one division after it
-		const double invG = 1.0 / gamma, invGA = invG / alpha;
+		// (warp 0 alone, whose lane 0 finishes the totals)
+		double invG = 0, invGA = 0;
+		if (threadIdx.x < 32) { invG = 1.0 / gamma; invGA = invG / alpha; }
 		if (!gridSync(a.bar, a.err, epoch)) { *ok = false; it++; break; }
-		gridTotals<3, 5>(a.partials, a.maxBlocks, tot, sh, [invG, invGA](double *t) {
+		gridTotals<3, 6>(a.partials, a.maxBlocks, tot, sh, [invG, invGA, threshold](double *t) {
 			t[3] = t[0] * invG;
 			t[4] = t[0] / fma(-t[0] * t[0], invGA, t[1]);
+			t[5] = t[2] < threshold ? 1.0 : 0.0;  // converged
 		});
 		it++;
 		*outRR = tot[2];
-		if (tot[2] < threshold) break;
+		if (flagSet(tot[5])) break;
 		gamma = tot[0];
 	}
 	if constexpr (Reg) {
@@ -667,9 +683,13 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 		blockPartialsDF<2>(acc, a.partials, a.maxBlocks, sh);
 	}
 	if (!gridSync(a.bar, a.err, epoch)) return;
-	double tot[5];
-	gridTotalsDF<2, 5>(a.partials, a.maxBlocks, tot, sh, [](double *t) { t[2] = 0; t[3] = 0; t[4] = t[0] / t[1]; });
+	// tot: γ, δ, |r|^2, β, α, the replacement decision, FP32 β and α packed
+	double tot[7];
+	gridTotalsDF<2, 7>(a.partials, a.maxBlocks, tot, sh, [](double *t) {
+		t[2] = 0; t[3] = 0; t[4] = t[0] / t[1]; t[5] = 0; t[6] = packFloats(t[3], t[4]);
+	});
 	const double drop2 = a.drop * a.drop;
+	const int maxIter = a.maxIter, replaceEvery = a.replaceEvery;
 	double gamma = tot[0], lastTrue = b2;
 	int cur = 0, it = 0, lastReplace = 0;
 	// register-resident copies (used when every thread owns at most kRegUnknowns unknowns)
@@ -699,7 +719,7 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 	while (it < a.maxIter) {
 		// ---- one fused C-G iteration ----
 		const double alpha = tot[4];
-		const V bV = V(tot[3]), aV = V(alpha);
+		const V bV = packedHi(tot[6]), aV = packedLo(tot[6]);
 		{
 			const Pack<V> *__restrict__ sc = stb[cur];
 			Pack<V> *__restrict__ sn = stb[cur ^ 1];
@@ -747,19 +767,25 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 			blockPartialsDF<3>(acc, a.partials, a.maxBlocks, sh);
 		}
 		// β = γ/γ_old and α = γ/(δ - βγ/α_old) with the reciprocals of the known
-		// γ_old and γ_old·α_old formed before the barrier: one division after it
+		// γ_old and γ_old·α_old formed before the barrier (by warp 0 alone, whose lane 0
+		// finishes the totals): one division after it.  The same lane decides whether
+		// the residual is replaced after this iteration.
 		const double gOld = gamma;
-		const double invG = 1.0 / gOld, invGA = invG / alpha;
+		double invG = 0, invGA = 0;
+		if (threadIdx.x < 32) { invG = 1.0 / gOld; invGA = invG / alpha; }
 		if (!gridSync(a.bar, a.err, epoch)) break;
-		gridTotalsDF<3, 5>(a.partials, a.maxBlocks, tot, sh, [invG, invGA](double *t) {
+		const int itNext = it + 1;
+		gridTotalsDF<3, 7>(a.partials, a.maxBlocks, tot, sh, [=](double *t) {
 			t[3] = t[0] * invG;
 			t[4] = t[0] / fma(-t[0] * t[0], invGA, t[1]);
+			const double s2 = scale * scale;
+			const bool due = replaceEvery > 0 && itNext - lastReplace >= replaceEvery;
+			t[5] = (t[2] < drop2 * lastTrue * s2 || t[2] < threshold * s2 || itNext >= maxIter || due) ? 1.0 : 0.0;
+			t[6] = packFloats(t[3], t[4]);
 		});
-		it++;
+		it = itNext;
 		gamma = tot[0];
-		const double s2 = scale * scale;
-		const bool due = a.replaceEvery > 0 && it - lastReplace >= a.replaceEvery;
-		if (!(tot[2] < drop2 * lastTrue * s2 || tot[2] < threshold * s2 || it >= a.maxIter || due)) continue;
+		if (!flagSet(tot[5])) continue;
 		lastReplace = it;
 
 		// ---- residual replacement ----
@@ -837,11 +863,12 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 			blockPartialsDF<2>(acc, a.partials, a.maxBlocks, sh);
 		}
 		if (!gridSync(a.bar, a.err, epoch)) break;
-		const double gOldScaled = gOld * ratio2;
-		gridTotalsDF<2, 5>(a.partials, a.maxBlocks, tot, sh, [gOldScaled, alpha](double *t) {
+		gridTotalsDF<2, 7>(a.partials, a.maxBlocks, tot, sh, [gOld, ratio2, alpha](double *t) {
 			t[2] = 0;
-			t[3] = t[0] / gOldScaled;
+			t[3] = t[0] / (gOld * ratio2);
 			t[4] = t[0] / (t[1] - t[3] * t[0] / alpha);
+			t[5] = 0;
+			t[6] = packFloats(t[3], t[4]);
 		});
 		gamma = tot[0];
 	}
