@@ -234,35 +234,6 @@ __device__ __forceinline__ float maxNonNeg(float a, float b) {
 __device__ __forceinline__ bool signBit(double a) { return __double2hiint(a) < 0; }
 __device__ __forceinline__ bool signBit(float a) { return __float_as_int(a) < 0; }
 
-// 1/x for x in [2^-125, 2^125], by Newton–Raphson iteration for the reciprocal
-// (y ← y(1 + e + e²), e = 1 − x·y, the second-order form of y ← y(2 − x·y);
-// Muller et al., Handbook of Floating-Point Arithmetic, ch. 4) from the single-
-// precision hardware approximation rcp.approx.ftz.f32 (at most 1 ulp of float).
-// The FP64 seed is built with integer operations: x's exponent re-biased and the
-// top 23 bits of its mantissa make a float within 2^-23 of x, and the float
-// result widens back exactly the same way.  The seed is then within 2^-21 of
-// 1/x, one refinement leaves e³ < 2^-63, and the result is within 2 ulp of
-// the correctly rounded reciprocal.  The WENO weight sums below always lie in
-// [1, 2^106]: each scaled q lies in [1, 2^27].
-__device__ __forceinline__ double recipPos(double x) {
-	const int hi = __double2hiint(x), lo = __double2loint(x);
-	const int ex = ((hi >> 20) & 0x7ff) - 1023;
-	const unsigned man = (unsigned(hi & 0xfffff) << 3) | (unsigned(lo) >> 29);
-	const float xf = __int_as_float(((ex + 127) << 23) | int(man));
-	float yf;
-	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(xf));
-	const int yb = __float_as_int(yf);
-	const int ey = ((yb >> 23) & 0xff) - 127;
-	const double y = __hiloint2double(((ey + 1023) << 20) | ((yb & 0x7fffff) >> 3), (yb & 7) << 29);
-	const double e = fma(-x, y, 1.0);
-	return fma(y, fma(e, e, e), y);
-}
-__device__ __forceinline__ float recipPos(float x) {
-	float y;
-	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-	return fmaf(y, fmaf(-x, y, 1.0f), y);
-}
-
 // 1/sqrt(x) for x in [2^-120, 2^120]: the FP32 hardware approximation
 // rsqrt.approx.ftz.f32 of x (x's mantissa truncated to float; the seed is then within
 // about 2^-21 of 1/sqrt(x)) refined by one second-order Newton–Raphson step for the

@@ -683,10 +683,13 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 		blockPartialsDF<2>(acc, a.partials, a.maxBlocks, sh);
 	}
 	if (!gridSync(a.bar, a.err, epoch)) return;
-	// tot: γ, δ, |r|^2, β, α, the replacement decision, FP32 β and α packed
+	// tot: γ, δ, |r|^2, β, α, the replacement decision, FP32 β and α packed.  The lane
+	// that finishes the totals also keeps 1/γ and 1/(γα) for the next iteration's β and α
+	// in sh[96], sh[97], which no reduction touches.
 	double tot[7];
-	gridTotalsDF<2, 7>(a.partials, a.maxBlocks, tot, sh, [](double *t) {
+	gridTotalsDF<2, 7>(a.partials, a.maxBlocks, tot, sh, [sh](double *t) {
 		t[2] = 0; t[3] = 0; t[4] = t[0] / t[1]; t[5] = 0; t[6] = packFloats(t[3], t[4]);
+		sh[96] = 1.0 / t[0]; sh[97] = sh[96] / t[4];
 	});
 	const double drop2 = a.drop * a.drop;
 	const int maxIter = a.maxIter, replaceEvery = a.replaceEvery;
@@ -766,18 +769,24 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 			cur ^= 1;
 			blockPartialsDF<3>(acc, a.partials, a.maxBlocks, sh);
 		}
-		// β = γ/γ_old and α = γ/(δ - βγ/α_old) with the reciprocals of the known
-		// γ_old and γ_old·α_old formed before the barrier (by warp 0 alone, whose lane 0
-		// finishes the totals): one division after it.  The same lane decides whether
-		// the residual is replaced after this iteration.
+		// β = γ/γ_old and α = γ/den, den = δ - βγ/α_old = δ - γ²/(γ_old α_old), from the
+		// kept 1/γ_old and 1/(γ_old α_old).  One reciprocal, of q = γ·den, gives α = γ²/q
+		// and the next pair: 1/γ = den/q and 1/(γα) = den/γ².  It is the Newton–Raphson
+		// reciprocal from an FP32 seed (2 ulp), a plain division outside its range.  The same
+		// lane decides whether the residual is replaced after this iteration.
 		const double gOld = gamma;
-		double invG = 0, invGA = 0;
-		if (threadIdx.x < 32) { invG = 1.0 / gOld; invGA = invG / alpha; }
 		if (!gridSync(a.bar, a.err, epoch)) break;
 		const int itNext = it + 1;
 		gridTotalsDF<3, 7>(a.partials, a.maxBlocks, tot, sh, [=](double *t) {
-			t[3] = t[0] * invG;
-			t[4] = t[0] / fma(-t[0] * t[0], invGA, t[1]);
+			const double g = t[0];
+			t[3] = g * sh[96];
+			const double den = fma(-g * g, sh[97], t[1]);
+			const double q = g * den;
+			const double rq = recipRange(q) ? recipPos(q) : 1.0 / q;
+			t[4] = (g * g) * rq;
+			const double invG = den * rq;
+			sh[96] = invG;
+			sh[97] = (invG * invG) * den;
 			const double s2 = scale * scale;
 			const bool due = replaceEvery > 0 && itNext - lastReplace >= replaceEvery;
 			t[5] = (t[2] < drop2 * lastTrue * s2 || t[2] < threshold * s2 || itNext >= maxIter || due) ? 1.0 : 0.0;
@@ -863,12 +872,13 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 			blockPartialsDF<2>(acc, a.partials, a.maxBlocks, sh);
 		}
 		if (!gridSync(a.bar, a.err, epoch)) break;
-		gridTotalsDF<2, 7>(a.partials, a.maxBlocks, tot, sh, [gOld, ratio2, alpha](double *t) {
+		gridTotalsDF<2, 7>(a.partials, a.maxBlocks, tot, sh, [gOld, ratio2, alpha, sh](double *t) {
 			t[2] = 0;
 			t[3] = t[0] / (gOld * ratio2);
 			t[4] = t[0] / (t[1] - t[3] * t[0] / alpha);
 			t[5] = 0;
 			t[6] = packFloats(t[3], t[4]);
+			sh[96] = 1.0 / t[0]; sh[97] = sh[96] / t[4];
 		});
 		gamma = tot[0];
 	}

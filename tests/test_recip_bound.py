@@ -50,6 +50,20 @@ def test_reciprocal_within_two_ulp():
     assert worst <= 2.0 ** -52, worst  # two ulp of the correctly rounded value
 
 
+def test_reciprocal_over_the_pressure_solve_range():
+    """The same reciprocal forms the mixed pressure solve's step sizes from γ·(p·Ap), which
+    it accepts anywhere in [2^-124, 2^125) and otherwise divides."""
+    rng = random.Random(9)
+    worst = 0.0
+    for n in range(2000):
+        x = 2.0 ** rng.uniform(-124.0, 125.0)
+        for ulps in (-1, 0, 1):
+            r = refine(x, seed(x, ulps))
+            exact = 1 / Fraction(x)
+            worst = max(worst, float(abs(Fraction(r) - exact) / exact))
+    assert worst <= 2.0 ** -52, worst
+
+
 def test_reciprocal_edges():
     for x in (1.0, 2.0 ** 106, 1.5, 3.0, 7.0, 2.0 ** 53 - 1):
         r = refine(x, seed(x, 1))
