@@ -209,16 +209,15 @@ garm_status generateCurrentFields(State &s) {
 // once to the squared sum), so results agree with the FP64 oracle to rounding
 // (~1e-13·dx after a full reinitialisation), not bitwise.
 
-// 2^-e for the binary exponent e of x > 0 (x normal): an exact power-of-two
-// scale built from the exponent bits, used to keep the WENO weights in range.
+// 2^-e for the binary exponent e of x > 0 (x normal, e > -bias): an exact power-of-two
+// scale built from the exponent bits, used to keep the WENO weights in range.  With E the
+// biased exponent field, the result's field is 2·bias - E: one mask and one subtraction
+// in place.
 __device__ __forceinline__ double pow2NegExp(double x) {
-	const int hi = __double2hiint(x);
-	const int e = ((hi >> 20) & 0x7ff) - 1023;
-	return __hiloint2double((1023 - e) << 20, 0);
+	return __hiloint2double((2046 << 20) - (__double2hiint(x) & 0x7ff00000), 0);
 }
 __device__ __forceinline__ float pow2NegExp(float x) {
-	const int e = ((__float_as_int(x) >> 23) & 0xff) - 127;
-	return __int_as_float((127 - e) << 23);
+	return __int_as_float((254 << 23) - (__float_as_int(x) & 0x7f800000));
 }
 
 // max of two non-negative, non-NaN values.  For such values the IEEE bit
