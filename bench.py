@@ -236,6 +236,12 @@ def field_errors(test, ref, dx: float) -> dict:
     out = {"phi_linf_band3dx_dx": float(np.max(d[band], initial=0.0)) / dx}
     a, b = linf_rms(d)
     out.update({"phi_linf_dx": a / dx, "phi_rms_dx": b / dx})
+    # where the largest φ difference sits: storage cell (x, y, z), φ there, distance from the
+    # nearest face of the storage grid in cells
+    shape = tuple(reversed([int(ref.grid.resolution[q]) for q in range(ref.grid.dim)]))
+    at = np.unravel_index(int(np.argmax(d)), shape)[::-1]
+    out["phi_linf_at"] = {"cell": [int(q) for q in at], "phi_ref_dx": float(pr[int(np.argmax(d))]) / dx,
+                          "cells_from_grid_face": int(min(min(q, s - 1 - q) for q, s in zip(at, reversed(shape))))}
     ur = ref.download(capi.FIELD_VELOCITY)
     scale = max(float(np.max(np.abs(ur))), 1e-300)
     fluid = ref.download(capi.FIELD_FRACTION) < 1
@@ -621,8 +627,23 @@ def run_garm(args) -> None:
         out["cpu_baseline"] = {"value": interior / secs, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
                                "sample": f"1 oracle advance of the {n}^3 dam break from the GPU state ({secs:.1f} s)"}
         sim.advance(dt)
-        out["parity_vs_oracle_1_step"] = {"form": args.precision, **field_errors(sim, o, dx)}
+        out["parity_vs_oracle_1_step"] = {"form": args.precision, "from": f"the GPU state after {2 * K + W + 3} steps",
+                                          **field_errors(sim, o, dx)}
         o.close()
+        # the gate as the path states it: initialize, restart and one step of the scene
+        g0 = make(main_prec)
+        o0 = O.OracleSim(scene.grid, g0.cfg)
+        o0.upload(capi.FIELD_LEVEL_SET, scene.phi.ravel())
+        o0.upload(capi.FIELD_VELOCITY, scene.velocity)
+        o0.initialize()
+        o0.stage("restart")
+        dt0 = next(scenes.frame_time_steps(o0.max_speed, 1, 25, 1.0, dx))
+        o0.advance(dt0)
+        g0.advance(dt0)
+        out["parity_vs_oracle_first_step"] = {"form": args.precision, "from": "the scene (initialize, restart, one step)",
+                                              **field_errors(g0, o0, dx)}
+        o0.close()
+        g0.close()
     sim.close()
     if rank == 0:
         print(json.dumps(out), flush=True)
