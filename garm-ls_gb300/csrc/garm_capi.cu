@@ -727,6 +727,7 @@ garm_status garm_sim_create(const garm_grid_desc *gd, const garm_config *cfg, vo
 		s.Ftot += s.F[a];
 	}
 	garm_status r = allocState(s);
+	if (r == GARM_OK) r = pcgPrepare();                                     // before any step capture
 	if (r == GARM_OK && D == 3 && s.cfg.record_volume) r = loadVolumeTables();  // before any step capture
 	if (r == GARM_OK) r = GARM_DISPATCH(s, initBoundary, s);           // Boundary ctor → reset()
 	if (r == GARM_OK) {

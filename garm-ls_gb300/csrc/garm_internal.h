@@ -163,6 +163,7 @@ template <int D, typename T> garm_status bodyForce(State &s);
 template <int D, typename T> garm_status project(State &s, garm_step_stats *st);
 template <int D, typename T> garm_status projectAsync(State &s, bool record);
 garm_status projectStats(State &s, garm_step_stats *st);
+garm_status pcgPrepare();
 template <int D, typename T> garm_status extrapolateToAir(State &s);
 constexpr int kFrontMaxPasses = 250;  // extrapolation passes fit a level byte (255 = unreached)
 template <int D, typename T> garm_status enforceBoundaryConditions(State &s);

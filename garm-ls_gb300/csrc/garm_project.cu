@@ -303,7 +303,7 @@ template <> struct __align__(32) Pack<double> { double r, w, s, d; };
 // packed {r, w, s} to save the first barrier; in FP64 that recompute, two fma and a
 // product per neighbour entry, costs more FP64-pipe time than the barrier.)
 template <int NB, bool Reg>
-__device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, unsigned &epoch, double *outRR, double *outB2, bool *ok) {
+__device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, NbW64 *enS, unsigned &epoch, double *outRR, double *outB2, bool *ok) {
 	using V = double;
 	using E = NbW64;
 	const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x, nthr = int64_t(gridDim.x) * blockDim.x;
@@ -349,7 +349,8 @@ __device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, unsigned &epoch,
 	const double threshold = fmax(tol * tol * rhsNorm2, DBL_MIN);
 	if (rhsNorm2 < threshold) return 0;
 
-	E en[kRegUnknowns][NB];
+	// the register form's matrix rows, in shared memory [slot][entry][thread]
+	auto en = [&](int c, int k) -> E & { return enS[(c * NB + k) * kCgBlock + threadIdx.x]; };
 	V dgi[kRegUnknowns], pp[kRegUnknowns], xx[kRegUnknowns], un[kRegUnknowns];
 	Pack<V> me[kRegUnknowns];
 	bool own[kRegUnknowns];
@@ -363,12 +364,12 @@ __device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, unsigned &epoch,
 				dgi[c] = dg[i];
 				me[c] = st[i];
 #pragma unroll
-				for (int k = 0; k < NB; k++) en[c][k] = ent[k * S + i];
+				for (int k = 0; k < NB; k++) en(c, k) = ent[k * S + i];
 			} else {
 				dgi[c] = V(0);
 				me[c] = Pack<V>{V(0), V(0), V(0), V(0)};
 #pragma unroll
-				for (int k = 0; k < NB; k++) { en[c][k] = E{}; en[c][k].nb = -1; }
+				for (int k = 0; k < NB; k++) { en(c, k) = E{}; en(c, k).nb = -1; }
 			}
 		}
 	}
@@ -415,7 +416,7 @@ __device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, unsigned &epoch,
 				V wni = dgi[c] * un[c];
 #pragma unroll
 				for (int k = 0; k < NB; k++)
-					if (en[c][k].nb >= 0) wni = fma(-en[c][k].w, uG[en[c][k].nb], wni);
+					{ const E e = en(c, k); if (e.nb >= 0) wni = fma(-e.w, uG[e.nb], wni); }
 				me[c].w = wni;
 				g = fma(me[c].r, un[c], g);
 				d = fma(wni, un[c], d);
@@ -472,8 +473,10 @@ __global__ void __launch_bounds__(kCgBlock) kPcgFp64(CgArgs a) {
 	bool ok = true;
 	unsigned epoch = 0;
 	const int64_t nthr = int64_t(gridDim.x) * blockDim.x;
-	const int mv = n <= kRegUnknowns * nthr ? pcgFp64Split<NB, true>(a, n, sh, epoch, &rr, &b2, &ok)
-	                                        : pcgFp64Split<NB, false>(a, n, sh, epoch, &rr, &b2, &ok);
+	extern __shared__ __align__(16) unsigned char pcgRows[];
+	NbW64 *enS = reinterpret_cast<NbW64 *>(pcgRows);
+	const int mv = n <= kRegUnknowns * nthr ? pcgFp64Split<NB, true>(a, n, sh, enS, epoch, &rr, &b2, &ok)
+	                                        : pcgFp64Split<NB, false>(a, n, sh, enS, epoch, &rr, &b2, &ok);
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		a.ints[0] = mv;
 		a.ints[1] = 1;
@@ -634,7 +637,7 @@ __device__ __forceinline__ double unitScale(double sumSq, int n) {
 // information is discarded, so the iteration count stays close to the FP64
 // solver's, while the residual the solve reports is FP64-exact.
 template <int NB, bool Reg>
-__device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &epoch, int &itOut, int &replOut, double &relOut, double &tolOut) {
+__device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, unsigned &epoch, int &itOut, int &replOut, double &relOut, double &tolOut) {
 	using V = float;
 	using E = NbW32;
 	const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x, nthr = int64_t(gridDim.x) * blockDim.x;
@@ -696,7 +699,8 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 	double gamma = tot[0], lastTrue = b2;
 	int cur = 0, it = 0, lastReplace = 0;
 	// register-resident copies (used when every thread owns at most kRegUnknowns unknowns)
-	E en[kRegUnknowns][NB];
+	// the register form's matrix rows, in shared memory [slot][entry][thread]
+	auto en = [&](int c, int k) -> E & { return enS[(c * NB + k) * kCgBlock + threadIdx.x]; };
 	V dgi[kRegUnknowns], pp[kRegUnknowns], xx[kRegUnknowns];
 	Pack<V> me[kRegUnknowns];
 	bool own[kRegUnknowns];
@@ -710,12 +714,12 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 				dgi[c] = dg[i];
 				me[c] = stb[0][i];
 #pragma unroll
-				for (int k = 0; k < NB; k++) en[c][k] = ent[k * S + i];
+				for (int k = 0; k < NB; k++) en(c, k) = ent[k * S + i];
 			} else {
 				dgi[c] = V(0);
 				me[c] = Pack<V>{V(0), V(0), V(0), V(0)};
 #pragma unroll
-				for (int k = 0; k < NB; k++) { en[c][k] = E{}; en[c][k].nb = -1; }
+				for (int k = 0; k < NB; k++) { en(c, k) = E{}; en(c, k).nb = -1; }
 			}
 		}
 	}
@@ -755,7 +759,7 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 #pragma unroll
 				for (int c = 0; c < kRegUnknowns; c++) {
 					if (!own[c]) continue;
-					update(me[c], dgi[c], pp[c], xx[c], [&](int k) { return en[c][k]; }, me[c], pp[c], xx[c]);
+					update(me[c], dgi[c], pp[c], xx[c], [&](int k) { return en(c, k); }, me[c], pp[c], xx[c]);
 					sn[tid + c * nthr] = me[c];
 				}
 			} else {
@@ -858,7 +862,7 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, unsigned &ep
 				for (int c = 0; c < kRegUnknowns; c++)
 					if (own[c]) {
 						const int64_t i = tid + c * nthr;
-						me[c] = rebuild(i, me[c], dgi[c], [&](int k) { return en[c][k]; });
+						me[c] = rebuild(i, me[c], dgi[c], [&](int k) { return en(c, k); });
 						pp[c] *= ratio;
 						sn[i] = me[c];
 					}
@@ -892,8 +896,10 @@ __global__ void __launch_bounds__(kCgBlock) kPcgMixed(CgArgs a) {
 	int it = 0, repl = 0;
 	double rel = 0, tolUsed = a.tol;
 	const int64_t nthr = int64_t(gridDim.x) * blockDim.x;
-	if (n <= kRegUnknowns * nthr) pcgMixedReplace<NB, true>(a, n, sh, epoch, it, repl, rel, tolUsed);
-	else pcgMixedReplace<NB, false>(a, n, sh, epoch, it, repl, rel, tolUsed);
+	extern __shared__ __align__(16) unsigned char pcgRows[];
+	NbW32 *enS = reinterpret_cast<NbW32 *>(pcgRows);
+	if (n <= kRegUnknowns * nthr) pcgMixedReplace<NB, true>(a, n, sh, enS, epoch, it, repl, rel, tolUsed);
+	else pcgMixedReplace<NB, false>(a, n, sh, enS, epoch, it, repl, rel, tolUsed);
 	if (blockIdx.x == 0 && threadIdx.x == 0) {
 		a.ints[0] = it;
 		a.ints[1] = repl;
@@ -942,6 +948,26 @@ __global__ void kRecordCg(const int *ints, const double *scal, const int *n, dou
 	rec[kStCgErr] = ints[4];
 }
 
+// Dynamic shared memory of a solve: the register form's matrix rows, kRegUnknowns slots of
+// 2·dim entries per thread (98 KB mixed / 192 KB FP64 in 3D).
+static size_t pcgRowBytes(bool mixed, int dim) {
+	return size_t(kRegUnknowns) * size_t(2 * dim) * kCgBlock * (mixed ? sizeof(NbW32) : sizeof(NbW64));
+}
+
+// Lets the four solve kernels take their shared memory on the current device (above the
+// 48 KB default); called before any capture.
+garm_status pcgPrepare() {
+	const struct { const void *fn; bool mixed; int dim; } k[4] = {
+		{(const void *)kPcgMixed<4>, true, 2}, {(const void *)kPcgMixed<6>, true, 3},
+		{(const void *)kPcgFp64<4>, false, 2}, {(const void *)kPcgFp64<6>, false, 3}};
+	for (const auto &q : k)
+		if (cudaFuncSetAttribute(q.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(pcgRowBytes(q.mixed, q.dim))) != cudaSuccess) {
+			cudaGetLastError();
+			return GARM_CUDA_ERROR;
+		}
+	return GARM_OK;
+}
+
 template <int D, typename T>
 garm_status projectAsync(State &s, bool record) {
 	const unsigned nbC = gridFor(s.N);
@@ -986,8 +1012,9 @@ garm_status projectAsync(State &s, bool record) {
 	void *kfn;
 	if (s.mixed) kfn = (D == 2) ? (void *)kPcgMixed<4> : (void *)kPcgMixed<6>;
 	else kfn = (D == 2) ? (void *)kPcgFp64<4> : (void *)kPcgFp64<6>;
+	const size_t rowBytes = pcgRowBytes(s.mixed, D);
 	int perSM = 0;
-	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kfn, kCgBlock, 0);
+	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kfn, kCgBlock, rowBytes);
 	if (e != cudaSuccess || perSM <= 0) return GARM_CUDA_ERROR;
 	// one resident 512-thread block per SM for large scenes; small scenes take one
 	// block per cg_cells_per_block (default 4096) interior cells so that several
@@ -999,7 +1026,7 @@ garm_status projectAsync(State &s, bool record) {
 	if (blocks < 1) blocks = 1;
 	if (blocks > s.maxBlocks) blocks = s.maxBlocks;
 	void *args[] = {&a};
-	e = cudaLaunchCooperativeKernel(kfn, dim3(blocks), dim3(kCgBlock), args, 0, s.stream);
+	e = cudaLaunchCooperativeKernel(kfn, dim3(blocks), dim3(kCgBlock), args, rowBytes, s.stream);
 	if (e != cudaSuccess) return GARM_CUDA_ERROR;
 	s.launches++;
 
