@@ -292,3 +292,35 @@ def test_ga_advection_rotation_matches_oracle(oracle_mod, garm_lib):
     assert linf(pg, po) <= 1e-9 * dx
     for f in (capi.FIELD_REF_MAP, capi.FIELD_REF_MAP_GRAD):
         assert rel(g.download(f), o.download(f)) <= 1e-11, f
+
+
+@pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_MIXED])
+def test_pressure_solve_block_layouts(oracle_mod, garm_lib, precision):
+    """The persistent solve laid out three ways on the same system: one block (more than
+    four unknowns per thread: the streamed form), 41 blocks (the grid totals gather more than
+    one warp of block partials), one block per SM.  Each converges on the oracle's unknowns
+    and matches its pressure within the solve's tolerance."""
+    sc = scenes.dam_break(3, 32)
+    o = advanced_state(oracle_mod, sc, 2)
+    snapshot = {f: o.download(f) for f in STATE_FIELDS}
+    dt = 0.01
+    o.stage("body_force", dt)
+    so = o.stage("project")
+    po = o.download(capi.FIELD_PRESSURE)
+    assert so["unknowns"] > 4 * 512
+    tol = 1e-5 if precision == capi.PRECISION_FP64 else 1e-4
+    pressures = []
+    for per_block in (10 ** 9, 800, 1):
+        g = capi.Simulation(sc.grid, host_default_config(precision=precision, cg_cells_per_block=per_block))
+        load_scene(g, sc)
+        g.initialize()  # boundary fractions
+        for f, v in snapshot.items():
+            g.upload(f, v)
+        g.stage("body_force", dt)
+        sg = g.stage("project")
+        assert sg["status"] == capi.OK and sg["unknowns"] == so["unknowns"]
+        assert sg["cg_residual"] <= 1e-8
+        pg = g.download(capi.FIELD_PRESSURE)
+        assert rel(pg, po) <= tol, f"{per_block}: pressure rel err {rel(pg, po):.3e}"
+        pressures.append(pg)
+    assert rel(pressures[0], pressures[2]) <= tol
