@@ -53,6 +53,8 @@ def parse():
                         "batch: 48 uneven pool scenes only; serve: the Poisson request stream only; "
                         "drop: the 256^3 drop into a pool, mixed against FP64 over K steps with per-field errors")
     p.add_argument("--batch-scenes", type=int, default=48)
+    p.add_argument("--batch-cg-cells", type=int, default=None,
+                   help="batch: interior cells per pressure-solve block (default: the measured best)")
     p.add_argument("--reinit-plan", default=None, metavar="FORM,THREADS,CELLS",
                    help="pin the reinitialisation launch plan of the dam-break grid instead of autotuning it")
     p.add_argument("--requests", type=int, default=48, help="serve: number of requests")
@@ -260,7 +262,7 @@ def stage_ms(sim, dx: float, steps: int = 3) -> dict:
     return {name: round(statistics.median(r[i] for r in rows), 4) for i, name in enumerate(capi.STAGE_NAMES)}
 
 
-BATCH_CG_CELLS_PER_BLOCK = 262144  # measured best for the 48-scene batch (4096: 177M, 262144: 194-198M cell-steps/s)
+BATCH_CG_CELLS_PER_BLOCK = 131072  # measured best for the 48-scene batch (32768: 212M, 65536: 219M, 131072: 226M, 262144: 211M cell-steps/s)
 
 
 def batch_scenes(count: int, seed: int = 0):
@@ -280,9 +282,9 @@ def run_batch(args, torch, world: int, W: int, K: int) -> dict:
     from garm import capi
     scs = batch_scenes(args.batch_scenes)
     cfg = capi.default_config(precision=capi.PRECISION_MIXED)
-    # each scene's pressure solve takes one SM per 262144 interior cells (1-16 SMs here), so the
+    # each scene's pressure solve takes one SM per 131072 interior cells (2-32 SMs here), so the
     # solves of different scenes run side by side instead of each taking the whole GPU
-    cfg.cg_cells_per_block = BATCH_CG_CELLS_PER_BLOCK
+    cfg.cg_cells_per_block = args.batch_cg_cells or BATCH_CG_CELLS_PER_BLOCK
     streams = [torch.cuda.Stream() for _ in scs]
     sims = []
     for sc, st in zip(scs, streams):
@@ -321,7 +323,7 @@ def run_batch(args, torch, world: int, W: int, K: int) -> dict:
     return {"value": world * cells * K / (ms * 1e-3), "unit": UNIT, "ms_per_batch_step": ms / K, "scenes": len(scs),
             "interior_cells": cells, "sizes": sorted({int(round(sc.interior_cells ** (1 / 3))) for sc in scs}),
             "resident_bytes": resident, "graph_replay": graphs, "gpu_launches": launches,
-            "cg_cells_per_block": BATCH_CG_CELLS_PER_BLOCK,
+            "cg_cells_per_block": cfg.cg_cells_per_block,
             "p50_scene_step_ms": float(np.percentile(per_step, 50)), "p99_scene_step_ms": float(np.percentile(per_step, 99)),
             "dtype": "f32 storage+math, f64 dots/residual/refinement/RM test",
             "workload": f"{len(scs)} pool scenes, n uniform in {{64,96,128,160}}, 1-3 spheres, mixed, "

@@ -77,14 +77,14 @@ def build_scene(req: Request) -> scenes.Scene:
 
 class Server:
     def __init__(self, budget_bytes: float = 150e9, precision: int = capi.PRECISION_MIXED, frame_rate: int = 25,
-                 cfl: float = 1.0, chunk: int = 1, keep_phi: bool = False, cg_cells_per_block: int = 262144):
+                 cfl: float = 1.0, chunk: int = 1, keep_phi: bool = False, cg_cells_per_block: int = 131072):
         self.budget = float(budget_bytes)
         self.precision = precision
         self.frame_rate = frame_rate
         self.cfl = cfl
         self.chunk = chunk
         self.keep_phi = keep_phi
-        # one SM per 262144 interior cells for each pressure solve: resident scenes' solves run
+        # one SM per 131072 interior cells for each pressure solve: resident scenes' solves run
         # side by side instead of each taking the whole GPU
         self.cfg = capi.default_config(precision=precision, cg_cells_per_block=cg_cells_per_block)
 
