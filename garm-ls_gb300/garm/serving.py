@@ -77,15 +77,16 @@ def build_scene(req: Request) -> scenes.Scene:
 
 class Server:
     def __init__(self, budget_bytes: float = 150e9, precision: int = capi.PRECISION_MIXED, frame_rate: int = 25,
-                 cfl: float = 1.0, chunk: int = 1, keep_phi: bool = False, cg_cells_per_block: int = 131072):
+                 cfl: float = 1.0, chunk: int = 1, keep_phi: bool = False, cg_cells_per_block: int = 65536):
         self.budget = float(budget_bytes)
         self.precision = precision
         self.frame_rate = frame_rate
         self.cfl = cfl
         self.chunk = chunk
         self.keep_phi = keep_phi
-        # one SM per 131072 interior cells for each pressure solve: resident scenes' solves run
-        # side by side instead of each taking the whole GPU
+        # one SM per 65536 interior cells for each pressure solve: resident scenes' solves run
+        # side by side instead of each taking the whole GPU (measured on the default stream:
+        # 262144 cells per block 133M, 131072 189M, 65536 206M cell-steps/s)
         self.cfg = capi.default_config(precision=precision, cg_cells_per_block=cg_cells_per_block)
 
     def _admit(self, req: Request, t0: float):
