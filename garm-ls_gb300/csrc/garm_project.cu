@@ -18,7 +18,7 @@
 namespace garm {
 
 constexpr int kCgBlock = 512;
-constexpr int kRegUnknowns = 4;  // unknowns per thread held in registers by the PCG
+constexpr int kRegUnknowns = 4;  // unknowns per thread the PCG holds on chip (state in registers, rows in shared memory)
 
 // ---------------------------------------------------------------------------
 // unknown set and numbering
@@ -698,7 +698,7 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 	const int maxIter = a.maxIter, replaceEvery = a.replaceEvery;
 	double gamma = tot[0], lastTrue = b2;
 	int cur = 0, it = 0, lastReplace = 0;
-	// register-resident copies (used when every thread owns at most kRegUnknowns unknowns)
+	// on-chip copies (used when every thread owns at most kRegUnknowns unknowns)
 	// the register form's matrix rows, in shared memory [slot][entry][thread]
 	auto en = [&](int c, int k) -> E & { return enS[(c * NB + k) * kCgBlock + threadIdx.x]; };
 	V dgi[kRegUnknowns], pp[kRegUnknowns], xx[kRegUnknowns];
