@@ -38,7 +38,7 @@ def _worker(rank, world, port, out):
 def test_max_over_ranks_and_weak_scaling_value():
     world = 2
     port = _free_port()
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()  # no fork of this (threaded) process
     out = mgr.dict()
     mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
     for r in range(world):
