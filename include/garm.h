@@ -141,7 +141,8 @@ garm_status garm_config_default(garm_config *cfg);
 garm_status garm_sim_create(const garm_grid_desc *grid, const garm_config *cfg, void *stream, garm_sim **out);
 garm_status garm_sim_destroy(garm_sim *sim);
 /* Device bytes garm_sim_create would allocate for this grid and configuration,
- * without allocating (admission control; no reference counterpart). */
+ * without allocating (admission control; no reference counterpart).  A grid or a
+ * configuration that garm_sim_create would refuse returns GARM_INVALID here too. */
 garm_status garm_sim_estimate_bytes(const garm_grid_desc *grid, const garm_config *cfg, size_t *bytes);
 garm_status garm_sim_device_bytes(const garm_sim *sim, size_t *bytes);
 /* Kernels launched by this simulation since creation (no reference counterpart: instrumentation). */
