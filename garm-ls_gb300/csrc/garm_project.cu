@@ -763,7 +763,21 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 					sn[tid + c * nthr] = me[c];
 				}
 			} else {
-				for (int64_t i = tid; i < n; i += nthr) {
+				int64_t i = tid;
+				for (; i + nthr < n; i += 2 * nthr) {
+					const int64_t j = i + nthr;
+					Pack<V> m0 = sc[i], m1 = sc[j];
+					V p0 = p32[i], x0 = x32[i], p1 = p32[j], x1 = x32[j];
+					const V d0 = dg[i], d1 = dg[j];
+					E e0[NB], e1[NB];
+#pragma unroll
+					for (int k = 0; k < NB; k++) { e0[k] = ent[k * S + i]; e1[k] = ent[k * S + j]; }
+					update(m0, d0, p0, x0, [&](int k) { return e0[k]; }, m0, p0, x0);
+					update(m1, d1, p1, x1, [&](int k) { return e1[k]; }, m1, p1, x1);
+					sn[i] = m0; p32[i] = p0; x32[i] = x0;
+					sn[j] = m1; p32[j] = p1; x32[j] = x1;
+				}
+				if (i < n) {
 					Pack<V> m = sc[i];
 					V pv = p32[i], xv = x32[i];
 					update(m, dg[i], pv, xv, [&](int k) { return ent[k * S + i]; }, m, pv, xv);
