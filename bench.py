@@ -9,6 +9,12 @@ per second of the plain FP64 form measured with CUDA events over exactly K
 steps; the state (> 1 GB) is larger than L2, so no flush is needed.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl garm|reference]
+                  [--workload dam|batch|serve|drop]
+
+The default line also carries the mixed form, the reference's default build, the 48-scene
+batch, the end-to-end figure through the C ABI, per-stage times, the roofline of the
+reinitialisation sub-stage, and the CPU oracle: its speed and, at full size, the per-field
+differences between the FP64 form and it after one step.
 
 Under torchrun each rank advances its own replica of the scene (replicas
 only: the path does not shard), `value` = all ranks' cell-steps / max time.
