@@ -188,8 +188,10 @@ __global__ void kClearWords(unsigned *a, int na, unsigned *b, int nb);
 __global__ void kStepDt(const unsigned long long *maxBits, double dx, double *clock, double *dt, double *stats, const unsigned long long *counter);
 template <int D, typename T> garm_status copyField(State &s, void *dst, const void *src, int64_t n);
 
-// Standalone WENO5 reinitialisation on raw device planes.
-template <int D, typename T> garm_status reinitRaw(cudaStream_t st, const int *size, double dx, T *phi, T *a, T *b, int iters, double cfl, int *err);
+// Standalone WENO5 reinitialisation on raw device planes.  With tune = false a shape
+// that has no cached or pinned launch plan runs the default column plan instead of
+// timing the candidates (no event creation, no stream synchronisation).
+template <int D, typename T> garm_status reinitRaw(cudaStream_t st, const int *size, double dx, T *phi, T *a, T *b, int iters, double cfl, int *err, bool tune = true);
 
 inline garm_status cudaStatus(cudaError_t e) { return e == cudaSuccess ? GARM_OK : GARM_CUDA_ERROR; }
 // Work after forkAux(k) on s.aux runs beside work on s.stream until joinAux(k).

@@ -649,8 +649,8 @@ struct TmaPlanes {
 		if (threadIdx.x == 0)
 			for (int w = w0; w < min(w1, w0 + kTileSlots); w++) issue(w);
 	}
-	// Waits (bounded) until plane w is staged; false in every thread if any gave up.
-	__device__ bool ready(int w) {
+	// Bounded wait of the calling thread for plane w's slot; true once the plane is staged.
+	__device__ bool waitPlane(int w) const {
 		const int slot = (w - w0) % kTileSlots;
 		const unsigned bar = smemAddr(bars + slot), parity = unsigned((w - w0) / kTileSlots) & 1u;
 		unsigned done = 0;
@@ -658,18 +658,29 @@ struct TmaPlanes {
 		for (unsigned it = 0;; it++) {
 			asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
 			             : "=r"(done) : "r"(bar), "r"(parity) : "memory");
-			if (done) break;
+			if (done) return true;
 			if ((it & 255u) == 0) {
 				const unsigned long long now = globalNs();
 				if (start == 0) start = now;
-				else if (now - start > kTileWaitNs) break;
+				else if (now - start > kTileWaitNs) return false;
 			}
 		}
+	}
+	// Waits (bounded) until plane w is staged; false in every thread if any gave up.
+	// Before a block gives up, thread 0 waits (again bounded) for the other planes still in
+	// flight into its ring, so that no issued copy is left writing into the shared memory
+	// of a block that has exited.
+	__device__ bool ready(int w) {
+		const bool done = waitPlane(w);
 		if (__syncthreads_or(!done)) {
-			if (threadIdx.x == 0) atomicExch(err, 1);
+			if (threadIdx.x == 0) {
+				atomicExch(err, 1);
+				for (int q = w; q < min(w1, w + kTileSlots); q++) waitPlane(q);
+			}
+			__syncthreads();
 			return false;
 		}
-		cur = reinterpret_cast<const float *>(ring + slot * kTileStride);
+		cur = reinterpret_cast<const float *>(ring + ((w - w0) % kTileSlots) * kTileStride);
 		return true;
 	}
 	__device__ __forceinline__ float at(int ox, int oy) const { return cur[(ty + 3 + oy) * kTileRow + tx + 4 + ox]; }
@@ -926,10 +937,11 @@ std::map<PlanKey, ReinitPlan> g_plans;
 // (outside stream capture) every candidate runs sub-stage 0 (in → out only, so
 // the field is untouched) once to warm up and three times timed on the caller's
 // stream; the candidate with the smallest time is kept.  The tuning synchronises
-// that stream once per candidate.  Under capture, or when a timing
-// call fails, the plan is the default column form and nothing is cached.
+// that stream once per candidate.  Under capture, when a timing call fails, or
+// when the caller asks for no tuning, the plan is the default column form and
+// nothing is cached.
 template <int D, typename T>
-static ReinitPlan reinitPlanFor(cudaStream_t st, const G<D, T> &g, const T *phi, T *scratch, T dt, int *err) {
+static ReinitPlan reinitPlanFor(cudaStream_t st, const G<D, T> &g, const T *phi, T *scratch, T dt, int *err, bool tune = true) {
 	int dev = 0;
 	cudaGetDevice(&dev);
 	const PlanKey key{dev, D, int(sizeof(T)), g.s[0], g.s[1], D == 3 ? g.s[2] : 1};
@@ -939,6 +951,7 @@ static ReinitPlan reinitPlanFor(cudaStream_t st, const G<D, T> &g, const T *phi,
 		if (it != g_plans.end()) return it->second;
 	}
 	ReinitPlan best;
+	if (!tune) return best;
 	cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
 	if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) { cudaGetLastError(); return best; }
 	std::vector<ReinitPlan> cand;
@@ -1011,10 +1024,10 @@ garm_status pinReinitPlan(int dim, int esz, const int *size, int form, int block
 // no sub-stage writes a plane it reads; after a multiple of three iterations the
 // result is back in phi, otherwise one copy puts it there.
 template <int D, typename T>
-static garm_status reinitLoop(cudaStream_t st, const G<D, T> &g, T *phi, T *A, T *B, int iters, double cfl, long long *launches, int *err) {
+static garm_status reinitLoop(cudaStream_t st, const G<D, T> &g, T *phi, T *A, T *B, int iters, double cfl, long long *launches, int *err, bool tune = true) {
 	const T dt = T(double(g.dx) * cfl);
 	if (iters <= 0) return GARM_OK;
-	const ReinitPlan pl = reinitPlanFor<D, T>(st, g, phi, A, dt, err);
+	const ReinitPlan pl = reinitPlanFor<D, T>(st, g, phi, A, dt, err, tune);
 	T *buf[3] = {phi, A, B};
 	int cur = 0, n = 0;
 	for (int it = 0; it < iters; it++) {
@@ -1049,12 +1062,12 @@ garm_status reinitPlanInfo(State &s, int *form, int *block, int *chunk, float *m
 }
 
 template <int D, typename T>
-garm_status reinitRaw(cudaStream_t st, const int *size, double dx, T *phi, T *a, T *b, int iters, double cfl, int *err) {
+garm_status reinitRaw(cudaStream_t st, const int *size, double dx, T *phi, T *a, T *b, int iters, double cfl, int *err, bool tune) {
 	G<D, T> g;
 	g.s[0] = size[0]; g.s[1] = size[1]; g.s[2] = D == 3 ? size[2] : 1;
 	for (int q = 0; q < 3; q++) g.org[q] = T(0);
 	g.dx = T(dx); g.inv = T(1.0 / dx);
-	return reinitLoop<D, T>(st, g, phi, a, b, iters, cfl, nullptr, err);
+	return reinitLoop<D, T>(st, g, phi, a, b, iters, cfl, nullptr, err, tune);
 }
 
 // ---------------------------------------------------------------------------
@@ -1603,7 +1616,7 @@ garm_status enforceBoundaryLevelSet(State &s, void *field, double tol) {
 	template garm_status generateCurrentFields<D, T>(State &); \
 	template garm_status reinitialize<D, T>(State &); \
 	template garm_status reinitPlanInfo<D, T>(State &, int *, int *, int *, float *); \
-	template garm_status reinitRaw<D, T>(cudaStream_t, const int *, double, T *, T *, T *, int, double, int *); \
+	template garm_status reinitRaw<D, T>(cudaStream_t, const int *, double, T *, T *, T *, int, double, int *, bool); \
 	template garm_status checkReferenceMap<D, T>(State &, int *, int *, int *); \
 	template garm_status checkReferenceMapAsync<D, T>(State &, bool); \
 	template garm_status restart<D, T>(State &); \

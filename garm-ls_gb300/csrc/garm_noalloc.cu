@@ -13,6 +13,11 @@
 // Host code cannot use the array's name as a device address (in host code it is
 // only a stand-in symbol), so the address is fetched with cudaGetSymbolAddress,
 // once per device, with that device current, on the first call made there.
+//
+// Nothing here blocks the host either: the launch plan is the one already cached
+// or pinned for the grid shape (garm_reinit_plan_set, or an earlier tuned call
+// through another entry point), else the default column plan.  This entry point
+// never runs the autotuner, whose candidate timings synchronise the stream.
 #include "garm_internal.h"
 
 #include <mutex>
@@ -55,10 +60,18 @@ extern "C" garm_status garm_reinit_device_noalloc(int dim, const int *size, doub
 		n *= size[a];
 		if (n > kMaxCells) return GARM_INVALID;  // larger than the fixed scratch
 	}
+	// phi must be memory of the current device (or managed memory): a host pointer
+	// handed over by mistake would be dereferenced by the stencil kernels
+	cudaPointerAttributes attr{};
+	if (cudaPointerGetAttributes(&attr, phi) != cudaSuccess) { cudaGetLastError(); return GARM_INVALID; }
+	int dev = -1;
+	if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return GARM_CUDA_ERROR; }
+	if (attr.type == cudaMemoryTypeDevice ? attr.device != dev : attr.type != cudaMemoryTypeManaged) return GARM_INVALID;
 	double *scratch = nullptr;
 	GARM_TRY(scratchOnCurrentDevice(&scratch));
 	const cudaStream_t st = static_cast<cudaStream_t>(stream);
-	// FP64 never takes the tiled form, the only one with an error flag
-	if (dim == 2) return garm::reinitRaw<2, double>(st, size, spacing, phi, scratch, scratch + n, iters, cfl, nullptr);
-	return garm::reinitRaw<3, double>(st, size, spacing, phi, scratch, scratch + n, iters, cfl, nullptr);
+	// FP64 never takes the tiled form, the only one with an error flag; tune = false keeps
+	// the autotuner (and its stream synchronisations) off this path
+	if (dim == 2) return garm::reinitRaw<2, double>(st, size, spacing, phi, scratch, scratch + n, iters, cfl, nullptr, false);
+	return garm::reinitRaw<3, double>(st, size, spacing, phi, scratch, scratch + n, iters, cfl, nullptr, false);
 }

@@ -113,6 +113,7 @@ _SIGS = {
     "garm_reinit_host": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int, C.c_double, C.c_int]),
     "garm_reinit_device_noalloc": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.c_double, C.c_void_p, C.c_int, C.c_double, C.c_void_p]),
     "garm_barrier_selftest": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    "garm_fp64_peak_selftest": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
 }
 
 NOALLOC_MAX_CELLS = 1 << 19
@@ -345,6 +346,13 @@ class Simulation:
         else:
             raise ValueError(name)
         return None
+
+
+def fp64_peak_tflops(blocks_per_sm: int = 4, iters: int = 4096) -> float:
+    """garm_fp64_peak_selftest: measured FP64 FMA throughput of the current device (TFLOP/s)."""
+    out = C.c_double(0)
+    check(load().garm_fp64_peak_selftest(int(blocks_per_sm), int(iters), C.byref(out)), "garm_fp64_peak_selftest")
+    return out.value
 
 
 def barrier_selftest(blocks: int, rounds: int, never_complete: bool = False) -> tuple[int, float]:

@@ -34,7 +34,9 @@ typedef enum garm_status {
     GARM_NOT_CONVERGED = 3,  /* pressure PCG hit its iteration cap (reference: LinearSystem.h:33-36 exits) */
     GARM_NUMERIC = 4,        /* NaN/Inf found in an input or in the state */
     GARM_CUDA_ERROR = 5,     /* a CUDA runtime call failed */
-    GARM_TIMEOUT = 6,        /* a bounded device-side wait gave up (grid barrier) */
+    GARM_TIMEOUT = 6,        /* a bounded device-side wait gave up (grid barrier, or a TMA-staged
+                                plane of the tiled reinitialisation form); the fields the call was
+                                writing are not usable: reload or recreate the simulation */
     GARM_UNSUPPORTED = 7     /* feature not built into this library */
 } garm_status;
 
@@ -257,11 +259,17 @@ garm_status garm_reinit_host(int dim, const int *size, double spacing, double *p
  * It calls no cudaMalloc, cudaFree or allocating library routine: its two stage
  * planes live in one fixed device array of 2*GARM_NOALLOC_MAX_CELLS doubles
  * (8 MiB), held by every GPU that loads the library until the process exits.
- * Grids of more than GARM_NOALLOC_MAX_CELLS cells return GARM_INVALID.
+ * Grids of more than GARM_NOALLOC_MAX_CELLS cells return GARM_INVALID, and so does
+ * a `phi` that is not memory of the current device or managed memory (a host
+ * pointer, for instance).
  * The first call on a device looks up that array's device address
  * (cudaGetSymbolAddress, with that device current); make that first call before
- * any stream capture.  All calls share the one array, so calls whose work
- * overlaps on the GPU race; the array needs no clearing between calls. */
+ * any stream capture.  No call runs the reinitialisation autotuner or waits for
+ * the stream: the launch plan is the one cached or pinned for the grid shape on
+ * this device (garm_reinit_plan_set, or an earlier garm_reinit_host call of the
+ * same shape), else the default column plan.  All calls share the one array, so
+ * calls whose work overlaps on the GPU race; the array needs no clearing between
+ * calls. */
 #define GARM_NOALLOC_MAX_CELLS (1 << 19)
 garm_status garm_reinit_device_noalloc(int dim, const int *size, double spacing, double *phi, int iters, double cfl, void *stream);
 
@@ -272,6 +280,13 @@ garm_status garm_reinit_device_noalloc(int dim, const int *size, double spacing,
  * reached: every wait is bounded (about 2 s), and the call returns GARM_TIMEOUT with the
  * context still usable.  `blocks` above the co-resident limit returns GARM_INVALID. */
 garm_status garm_barrier_selftest(int blocks, int rounds, int never_complete, double *ms_per_barrier);
+
+/* FP64 FMA throughput of the current device (no counterpart in the reference): one launch
+ * of blocks_per_sm × SMs blocks of 256 threads, each thread `iters` rounds of 8 independent
+ * FMA chains, timed with CUDA events (shortest of three after one untimed launch).
+ * *tflops counts an FMA as two operations.  It reads no clocks and changes none.  This is
+ * the compute peak the plain FP64 form's stencil kernels are measured against. */
+garm_status garm_fp64_peak_selftest(int blocks_per_sm, int iters, double *tflops);
 
 #ifdef __cplusplus
 }

@@ -125,3 +125,10 @@ def test_barrier_selftest_validates_without_a_gpu(garm_lib):
     ms = C.c_double()
     for blocks, rounds, never in ((0, 10, 0), (4, 0, 0), (4, 10, 2), (-1, 10, 1)):
         assert garm_lib.garm_barrier_selftest(blocks, rounds, never, C.byref(ms)) == capi.INVALID
+
+
+def test_fp64_peak_selftest_validates_without_a_gpu(garm_lib):
+    out = C.c_double()
+    for per_sm, iters in ((0, 100), (17, 100), (4, 0), (4, (1 << 22) + 1)):
+        assert garm_lib.garm_fp64_peak_selftest(per_sm, iters, C.byref(out)) == capi.INVALID
+    assert garm_lib.garm_fp64_peak_selftest(4, 100, None) == capi.INVALID

@@ -43,3 +43,12 @@ def test_barrier_wait_is_bounded_and_the_context_survives(garm_lib):
     assert g.advance(0.005)["status"] == capi.OK
     assert np.all(np.isfinite(g.download(capi.FIELD_LEVEL_SET)))
     assert capi.barrier_selftest(sms, 100)[0] == capi.OK
+
+
+def test_fp64_peak_selftest(garm_lib, capsys):
+    """The FP64 FMA throughput the plain form's stencils are measured against: positive and
+    below the nominal 1.25 TFLOP/s of a GB300 by no more than a timing margin."""
+    tf = capi.fp64_peak_tflops()
+    with capsys.disabled():
+        print(f"\n[FP64 FMA peak] {tf:.3f} TFLOP/s")
+    assert 0.1 < tf < 5.0
