@@ -54,16 +54,19 @@ def parse():
     p.add_argument("--no-default-build", action="store_true",
                    help="skip the same workload in the reference's default build (Newton restart + fast marching)")
     p.add_argument("--seed", type=int, default=0, help="drop: seed of the sphere's centre")
-    p.add_argument("--workload", choices=["dam", "batch", "serve", "drop"], default="dam",
+    p.add_argument("--workload", choices=["dam", "batch", "serve", "drop", "reinit"], default="dam",
                    help="dam: the 128^3 dam break (default line, with mixed and batch sub-objects); "
                         "batch: 48 uneven pool scenes only; serve: the Poisson request stream only; "
-                        "drop: the 256^3 drop into a pool, mixed against FP64 over K steps with per-field errors")
+                        "drop: the 256^3 drop into a pool, mixed against FP64 over K steps with per-field errors; "
+                        "reinit: the dam break's reinitialisation stage alone, K times after W (for profiling one kernel)")
     p.add_argument("--batch-scenes", type=int, default=48)
     p.add_argument("--batch-cg-cells", type=int, default=None,
                    help="batch: interior cells per pressure-solve block (default: the measured best)")
     p.add_argument("--reinit-plan", default=None, metavar="FORM,THREADS,CELLS",
                    help="pin the reinitialisation launch plan of the dam-break grid instead of autotuning it")
     p.add_argument("--requests", type=int, default=48, help="serve: number of requests")
+    p.add_argument("--serve-requests", type=int, default=12, help="requests of the serving leg of the default line")
+    p.add_argument("--no-serve", action="store_true")
     args = p.parse_args()
     if args.n is None:
         args.n = 256 if args.workload == "drop" else 128
@@ -123,6 +126,14 @@ class Clocks:
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dam_config(n: int, precision: str, world: int) -> dict:
+    """The workload description both arms print (the repo arm and --impl reference)."""
+    return {"workload": f"3D dam break {n}^3 MAC grid, {'plain FP64' if precision == 'fp64' else 'mixed FP32/FP64'} form",
+            "n": n, "interior_cells": n ** 3, "storage_cells": (n + 4) ** 3, "cfl": 1.0, "frame_rate": 25,
+            "reinit": "WENO5 x30 every step", "pcg_tol": 1e-8, "replicas": world,
+            "l2": "no flush: device state > 1 GB, larger than L2"}
 
 
 def reduce_max(x: float, world: int) -> float:
@@ -199,9 +210,25 @@ def profiled_traffic(plan: dict, precision: str, n: int):
     return None
 
 
+def profiled_fp64_ops(plan: dict):
+    """FP64 operations per storage cell and sub-stage (2·DFMA + DADD + DMUL executed, from
+    the ncu capture summarised under profiles/) of the FP64 plan the autotuner picked."""
+    name = PROFILED_PLANS.get((plan["form"], "fp64"))
+    p = REPO / "profiles" / name if name else None
+    if p is None or not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        if ln.startswith("fp64_ops_per_cell_substage:"):
+            return float(ln.split(":")[1])
+    return None
+
+
 def reinit_roofline(sim, torch, stream, n_cells: int, esz: int, iters: int, peaks: dict) -> dict:
     """Time the WENO5 reinitialisation stage alone with CUDA events on the sim's stream
-    and express its algorithmic bytes per launch against the measured HBM peak."""
+    and express its algorithmic bytes per launch against the measured HBM peak.  In the
+    FP64 form the sub-stage is bound by the FP64 pipe, not by HBM: there the line's
+    roofline is its FP64 operations per second against the FP64 FMA peak measured on
+    this device (garm_fp64_peak_selftest), and the HBM figures ride along."""
     launches = 3 * iters
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     sim.stage("reinit")  # warm
@@ -222,16 +249,42 @@ def reinit_roofline(sim, torch, stream, n_cells: int, esz: int, iters: int, peak
     plan = sim.reinit_plan()
     name = {"cells": "kReinitCells", "columns": "kReinitColumns", "sweeps": "kWenoSweep x3",
             "tiled": "kReinitColumnsTiled (TMA-staged plane tiles)"}[plan["form"]]
-    return {"kernel": f"{name} (WENO5 TVD-RK3 sub-stage)", "plan": plan, "bound": "hbm", "achieved": round(achieved, 1),
-            "peak": peak, "peak_source": src, "unit": "GB/s", "frac": round(achieved / peak, 4),
-            "traffic": None, "ms_per_launch": round(ms_per_launch, 4), "algorithmic_bytes_per_launch": int(bytes_per_launch)}
+    hbm = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "peak_source": src, "unit": "GB/s",
+           "frac": round(achieved / peak, 4), "traffic": None, "algorithmic_bytes_per_launch": int(bytes_per_launch)}
+    out = {"kernel": f"{name} (WENO5 TVD-RK3 sub-stage)", "plan": plan, **hbm, "ms_per_launch": round(ms_per_launch, 4)}
+    ops = profiled_fp64_ops(plan) if esz == 8 else None
+    if ops:
+        from garm import capi
+        fp64_peak = capi.fp64_peak_tflops()
+        tflops = ops * n_cells / (ms_per_launch * 1e-3) / 1e12
+        out.update({"bound": "fp64", "achieved": round(tflops, 4), "peak": round(fp64_peak, 4),
+                    "peak_source": "measured: garm_fp64_peak_selftest (FP64 FMA chains, CUDA events) on this device",
+                    "unit": "TFLOP/s", "frac": round(tflops / fp64_peak, 4),
+                    "fp64_ops_per_launch": int(ops * n_cells), "fp64_ops_per_cell": ops, "hbm": hbm})
+    return out
+
+
+# The level-set band φ is gated on: |φ| <= 15·dx, the reference's air extrapolation radius
+# (_airExtrapolationRadius, LevelSetLiquid.h:93).  Beyond it the reinitialisation amplifies
+# rounding along 3D diagonals, so forms that round differently differ there by more, and
+# those cells do not feed back into the band (tests/test_oracle_kat.py, test_gpu_far_field.py).
+LEVEL_SET_BAND = 15.0
+PHI_BINS = ((0, 3), (3, 10), (10, 15), (15, 20), (20, 30), (30, 1e9))
+
+
+def phi_profile(d, pr, dx: float) -> dict:
+    """L∞ of |Δφ| (in dx) by |φ_ref|/dx bin."""
+    import numpy as np
+    a = np.abs(pr) / dx
+    return {f"[{lo},{hi if hi < 1e9 else 'inf'})": float(np.max(d[(a >= lo) & (a < hi)], initial=0.0)) / dx
+            for lo, hi in PHI_BINS}
 
 
 def field_errors(test, ref, dx: float) -> dict:
     """Per-field L∞ and RMS of simulation `test` against simulation `ref` on the same grid:
-    φ and ξ in units of dx (φ also over the band |φ| <= 3 dx), u relative to max|u| over
-    the faces of the fluid domain (fraction < 1; solid-ring faces hold the wall
-    condition's sign ties)."""
+    φ and ξ in units of dx (φ also over the level-set band |φ| <= 15 dx, which the gates
+    use, over |φ| <= 3 dx, and by |φ| bin), u relative to max|u| over the faces of the
+    fluid domain (fraction < 1; solid-ring faces hold the wall condition's sign ties)."""
     import numpy as np
     from garm import capi
 
@@ -241,7 +294,9 @@ def field_errors(test, ref, dx: float) -> dict:
     pr = ref.download(capi.FIELD_LEVEL_SET)
     d = np.abs(test.download(capi.FIELD_LEVEL_SET) - pr)
     band = np.abs(pr) <= 3 * dx
-    out = {"phi_linf_band3dx_dx": float(np.max(d[band], initial=0.0)) / dx}
+    out = {"phi_linf_band15dx_dx": float(np.max(d[np.abs(pr) <= LEVEL_SET_BAND * dx], initial=0.0)) / dx,
+           "phi_linf_band3dx_dx": float(np.max(d[band], initial=0.0)) / dx,
+           "phi_linf_by_abs_phi_dx": phi_profile(d, pr, dx)}
     a, b = linf_rms(d)
     out.update({"phi_linf_dx": a / dx, "phi_rms_dx": b / dx})
     # where the largest φ difference sits: storage cell (x, y, z), φ there, distance from the
@@ -336,10 +391,10 @@ def run_batch(args, torch, world: int, W: int, K: int) -> dict:
                         f"one stream and one step graph per scene, {K} steps each"}
 
 
-def run_serve(args, world: int) -> dict:
+def run_serve(args, world: int, count: int | None = None) -> dict:
     """The Poisson request stream served with HBM-budget admission and continuous batching."""
     from garm import serving
-    reqs = serving.make_requests(args.requests, rate=20.0, seed=11)
+    reqs = serving.make_requests(count or args.requests, rate=20.0, seed=11)
     out = serving.Server(budget_bytes=150e9).run(reqs)
     res = out.pop("results")
     out.update({"unit": UNIT, "value": world * out["cell_steps_per_s"],
@@ -466,6 +521,8 @@ def run_garm(args) -> None:
     scene = scenes.dam_break(3, n)
     dx = scene.grid.spacing
     interior = n ** 3
+    if args.workload == "reinit" and not args.reinit_plan:
+        args.reinit_plan = "sweeps,32,44" if args.precision == "fp64" else "columns,128,8"
     if args.reinit_plan:
         form, threads, cells = args.reinit_plan.split(",")
         for prec in (capi.PRECISION_FP64, capi.PRECISION_MIXED):
@@ -484,6 +541,28 @@ def run_garm(args) -> None:
 
     main_prec = capi.PRECISION_MIXED if args.precision == "mixed" else capi.PRECISION_FP64
     sim = make(main_prec)
+    if args.workload == "reinit":
+        # the reinitialisation stage alone on the scene's level set, with a pinned plan, so that
+        # an ncu capture sees only the sub-stage kernels after the scene's set-up
+        for _ in range(W):
+            sim.stage("reinit")
+        torch.cuda.synchronize()
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = sim.launch_count()
+        r0.record(stream)
+        for _ in range(K):
+            sim.stage("reinit")
+        r1.record(stream)
+        torch.cuda.synchronize()
+        ms = r0.elapsed_time(r1)
+        if rank == 0:
+            print(json.dumps({"metric": "reinitialisation stages/s", "value": K / (ms * 1e-3), "unit": "stages/s", "n_gpus": world,
+                              "steps": K, "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+                              "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32", "data": "synthetic",
+                              "config": {"workload": f"WENO5 x30 reinitialisation of the {n}^3 dam break, plan {args.reinit_plan}",
+                                         "n": n}, "gpu_launches": sim.launch_count() - l0, "plan": sim.reinit_plan()}), flush=True)
+        sim.close()
+        return
     sim.set_clock(25, 1.0)  # Simulator dt policy on the device: CFL 1, 25 frames/s
     sim.advance_auto(W)     # warm-up (also captures the step graphs)
     barrier(world)
@@ -514,10 +593,7 @@ def run_garm(args) -> None:
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": elapsed_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
-        "config": {"workload": f"3D dam break {n}^3 MAC grid, {'plain FP64' if args.precision == 'fp64' else 'mixed FP32/FP64'} form", "n": n,
-                   "interior_cells": interior, "storage_cells": (n + 4) ** 3, "cfl": 1.0, "frame_rate": 25,
-                   "reinit": "WENO5 x30 every step", "pcg_tol": 1e-8, "replicas": world,
-                   "l2": "no flush: device state > 1 GB, larger than L2"},
+        "config": dam_config(n, args.precision, world),
         "p50_step_ms": statistics.median(step_ms), "p99_step_ms": float(np.percentile(step_ms, 99)),
         "cg_iterations_mean": statistics.mean(cg_it), "restarts": restarts, "graph_replay": sim.graph_active(),
         "stage_ms": stages,
@@ -526,6 +602,8 @@ def run_garm(args) -> None:
     if rank == 0:
         out["roofline"] = reinit_roofline(sim, torch, stream, int(scene.phi.size), 8 if args.precision == "fp64" else 4, 30, peaks)
         out["roofline"]["traffic"] = profiled_traffic(out["roofline"]["plan"], args.precision, n)
+        if "hbm" in out["roofline"]:
+            out["roofline"]["hbm"]["traffic"] = out["roofline"]["traffic"]
         out["roofline"]["compute"] = profiled_pipe(out["roofline"]["plan"], args.precision, n)
 
     # end to end through the C ABI with host buffers: upload the step's input state
@@ -563,9 +641,11 @@ def run_garm(args) -> None:
         ref.advance(dt0)
         mix.advance(dt0)
         pr, pm = ref.download(capi.FIELD_LEVEL_SET), mix.download(capi.FIELD_LEVEL_SET)
-        phi_err = float(np.max(np.abs(pr - pm))) / dx
-        band = np.abs(pr) <= 3 * dx
-        phi_err_band = float(np.max(np.abs(pr - pm)[band])) / dx
+        dphi = np.abs(pr - pm)
+        phi_err = float(np.max(dphi)) / dx
+        phi_err_band = float(np.max(dphi[np.abs(pr) <= 3 * dx])) / dx
+        phi_err_band15 = float(np.max(dphi[np.abs(pr) <= LEVEL_SET_BAND * dx])) / dx
+        phi_prof = phi_profile(dphi, pr, dx)
         ref.close()
         mix.set_clock(25, 1.0)
         mix.advance_auto(W)
@@ -585,7 +665,12 @@ def run_garm(args) -> None:
         mval = world * interior * K / (mix_ms * 1e-3)
         mstages = stage_ms(mix, dx)
         out["mixed"] = {"value": mval, "unit": UNIT, "ms_per_step": mix_ms / K, "p50_step_ms": statistics.median(mms),
-                        "p99_step_ms": float(np.percentile(mms, 99)), "phi_err_dx_band3dx_after_1_step_vs_fp64": phi_err_band, "phi_err_dx_all_cells_after_1_step_vs_fp64": phi_err,
+                        "p99_step_ms": float(np.percentile(mms, 99)),
+                        "phi_gate": {"metric": "φ L∞ after 1 step vs the FP64 form over |φ_fp64| <= 15·dx", "limit_dx": 1e-3,
+                                     "value_dx": phi_err_band15, "pass": bool(phi_err_band15 <= 1e-3)},
+                        "phi_err_dx_band15dx_after_1_step_vs_fp64": phi_err_band15,
+                        "phi_err_dx_band3dx_after_1_step_vs_fp64": phi_err_band, "phi_err_dx_all_cells_after_1_step_vs_fp64": phi_err,
+                        "phi_err_dx_by_abs_phi_after_1_step_vs_fp64": phi_prof,
                         "speedup_vs_fp64": mval / value, "cg_iterations_mean": statistics.mean(mcg), "stage_ms": mstages,
                         "dtype": "f32 storage+math, f64 dots/residual/refinement/RM test"}
         if rank == 0:
@@ -620,6 +705,11 @@ def run_garm(args) -> None:
         out["batch"] = run_batch(args, torch, world, W, K)
         out["batch"]["speedup_vs_fp64"] = out["batch"]["value"] / value if args.precision == "fp64" else None
 
+    # the Poisson request stream (a short one) with HBM-budget admission, so that the line
+    # carries serving throughput and p50/p99 step and end-to-end latency
+    if not args.no_serve:
+        out["serve"] = run_serve(args, world, args.serve_requests)
+
     # CPU baseline: the oracle (a CPU port of the reference's FP64 path) on this host,
     # one step of the same 128^3 workload started from the GPU's state.  The GPU then
     # takes the same step from the same state, and the two are compared field by field.
@@ -633,10 +723,24 @@ def run_garm(args) -> None:
         o.advance(dt)
         secs = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": interior / secs, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
-                               "sample": f"1 oracle advance of the {n}^3 dam break from the GPU state ({secs:.1f} s)"}
+                               "sample": f"1 oracle advance of the {n}^3 dam break from the GPU state ({secs:.1f} s)",
+                               "build": O.BUILD_FLAGS,
+                               "solver": "Jacobi-PCG to |r| <= 1e-8 |b| (the workload's tolerance; the reference's "
+                                         "Eigen IC-PCG stops at 1e-5)"}
         sim.advance(dt)
         out["parity_vs_oracle_1_step"] = {"form": args.precision, "from": f"the GPU state after {2 * K + W + 3} steps",
                                           **field_errors(sim, o, dx)}
+        # the reference's own thread policy, omp_set_num_threads(nprocs / 3) (Source/Demo/Demo.cpp:27)
+        all_threads = O.max_threads()
+        third = max(1, (os.cpu_count() or 3) // 3)
+        O.set_threads(third)
+        dt = next(scenes.frame_time_steps(o.max_speed, 1, 25, 1.0, dx))
+        t0 = time.perf_counter()
+        o.advance(dt)
+        secs3 = time.perf_counter() - t0
+        O.set_threads(all_threads)
+        out["cpu_baseline"]["nprocs_div_3"] = {"value": interior / secs3, "threads": third,
+                                               "sample": f"the next oracle step at nprocs/3 threads ({secs3:.1f} s)"}
         o.close()
         # the gate as the path states it: initialize, restart and one step of the scene
         g0 = make(main_prec)
@@ -694,7 +798,7 @@ def run_reference(args) -> None:
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": 1e3 * total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": f"3D dam break {n}^3 MAC grid, plain FP64 form", "n": n},
+        "config": dam_config(n, "fp64", world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
                          "sample": f"{K} full oracle steps of the {n}^3 dam break; warm-up capped at 1 step"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -19,6 +19,8 @@ from garm.capi import (Config, GridDesc, StepStats, FIELD_ADV_REGION, FIELD_NAME
                        field_shapes)
 
 LIB_PATH = REPO / "oracle" / "liboracle.so"
+from garm.build import ORACLE_FLAGS  # noqa: E402
+BUILD_FLAGS = "g++ -std=c++20 " + " ".join(ORACLE_FLAGS)
 
 STAGES = {"advect": 0, "compose": 1, "reinit": 2, "extrap_collider": 3, "rm_check": 4, "restart": 5,
           "body_force": 6, "project": 7, "extrap_air": 8, "enforce_bc": 9, "enforce_boundary_level_set": 10}

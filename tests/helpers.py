@@ -83,6 +83,18 @@ def velocity_check(g_u, o_u, fraction, rtol: float):
     return inner, ties
 
 
+# The level-set band the path's accuracy is stated on: cells within the reference's air
+# extrapolation radius of the interface, |φ| <= 15·dx (_airExtrapolationRadius,
+# Source/Core/LevelSetLiquid.h:93).  The reference carries the reference map only this
+# far into the air (extrapolateFieldsToAir) and clamps φ to 15·dx outside the advection
+# region (generateCurrentFields, LevelSetLiquid.cpp:1229-1233).  Beyond it the
+# reinitialisation (30 iterations at dτ = 0.9·dx) amplifies rounding where the normal
+# lies near a 3D diagonal, by up to about 1.4 per iteration (tests/test_oracle_kat.py
+# shows this on the oracle alone), so FP32 and FP64 runs legitimately differ there; the
+# same file and tests/test_gpu_far_field.py show those cells do not feed back into the band.
+LEVEL_SET_BAND = 15.0
+
+
 def band_error(a, b, ref_phi, dx: float, band: float = 3.0) -> float:
     """L∞ of a-b over cells with |ref_phi| <= band·dx (the accuracy band of the
     reference's own error measure, TestReinit.cpp:162-171 and TestAdvect2D.cpp:250-264)."""

@@ -15,7 +15,8 @@ import numpy as np
 import pytest
 
 from garm import capi, scenes
-from helpers import STATE_FIELDS, band_error, copy_state, host_default_config, linf, load_scene, rel, velocity_check
+from helpers import (LEVEL_SET_BAND, STATE_FIELDS, band_error, copy_state, host_default_config, linf, load_scene, oracle_spread,
+                     perturbed, rel, velocity_check)
 
 pytestmark = pytest.mark.gpu
 
@@ -237,26 +238,53 @@ def test_invalid_arguments(garm_lib):
 @pytest.mark.parametrize("name", ["dam3d", "drop3d", "dam2d"])
 def test_mixed_precision_within_1e3_dx(oracle_mod, garm_lib, capsys, name):
     """Mixed form (FP32 fields and stencils, FP64 dots/residual/refinement/RM test)
-    against the FP64 oracle: φ L∞ <= 1e-3·dx after one step; per-field errors printed."""
+    against the FP64 oracle after one step: φ L∞ <= 1e-3·dx over the level-set band
+    |φ| <= 15·dx (helpers.LEVEL_SET_BAND: the reference's air extrapolation radius;
+    beyond it the reinitialisation amplifies rounding, and those cells are shown not to
+    feed back, in test_oracle_kat.py and test_gpu_far_field.py), on every cell whose
+    one-step result the reference algorithm itself determines to 1e-4·dx.  That is
+    measured on the oracle: the same step with the initial φ and u changed by one or two
+    ulps (helpers.PERTURBATIONS).  On the drop, whose walls start with u·n = -1, the wall
+    condition's sign test (Boundary.cpp:104) flips on faces where the normal velocity is
+    zero up to rounding, so an ulp moves ξ there by 0.64·dx and φ by up to 0.06·dx in the
+    oracle alone; those cells are counted and printed, not gated."""
     sc = SCENES[name]()
+    dx = sc.grid.spacing
     cfg = host_default_config(precision=capi.PRECISION_MIXED)
     g = capi.Simulation(sc.grid, cfg)
-    o = oracle_mod.OracleSim(sc.grid, host_default_config())
     load_scene(g, sc)
-    load_scene(o, sc)
-    g.initialize(); o.initialize()
-    g.stage("restart"); o.stage("restart")
-    dt = next(scenes.frame_time_steps(o.max_speed, 1, 25, 1.0, sc.grid.spacing))
+    g.initialize()
+    g.stage("restart")
+    dt = next(scenes.frame_time_steps(g.max_speed, 1, 25, 1.0, dx))
+
+    def oracle_step(size, seed):
+        o = oracle_mod.OracleSim(sc.grid, host_default_config())
+        o.upload(capi.FIELD_LEVEL_SET, perturbed(sc.phi.ravel(), size, seed))
+        o.upload(capi.FIELD_VELOCITY, perturbed(sc.velocity, size, seed + 1))
+        o.initialize()
+        o.stage("restart")
+        o.advance(dt)
+        return o
+
+    o = oracle_step(0.0, 0)
+    _, spread = oracle_spread(lambda size, seed: oracle_step(size, seed).download(capi.FIELD_LEVEL_SET))
     sg = g.advance(dt)
-    o.advance(dt)
-    dx = sc.grid.spacing
     pg, po = g.download(capi.FIELD_LEVEL_SET), o.download(capi.FIELD_LEVEL_SET)
     ephi_all = linf(pg, po) / dx
-    ephi = band_error(pg, po, po, dx) / dx
+    ephi3 = band_error(pg, po, po, dx) / dx
+    band = np.abs(po) <= LEVEL_SET_BAND * dx
+    stable = band & (spread <= 1e-4 * dx)
+    d = np.abs(pg - po) / dx
+    ephi = float(np.max(d[stable], initial=0.0))
+    unstable = band & ~stable
+    with capsys.disabled():
+        print(f"\n[mixed vs FP64 oracle, {name}] band cells the oracle's own ulp spread leaves undetermined: "
+              f"{int(unstable.sum())} of {int(band.sum())} (oracle spread there up to {float(np.max(spread[unstable], initial=0)) / dx:.2e} dx, "
+              f"mixed error there up to {float(np.max(d[unstable], initial=0)):.2e} dx)")
     eu, ties = velocity_check(g.download(capi.FIELD_VELOCITY), o.download(capi.FIELD_VELOCITY), o.download(capi.FIELD_FRACTION), 1e-3)
     exi = linf(g.download(capi.FIELD_REF_MAP), o.download(capi.FIELD_REF_MAP)) / dx
     with capsys.disabled():
-        print(f"\n[mixed vs FP64 oracle, {name}] phi band(3dx) {ephi:.3e} dx, all cells {ephi_all:.3e} dx, "
+        print(f"\n[mixed vs FP64 oracle, {name}] phi band(15dx) {ephi:.3e} dx, band(3dx) {ephi3:.3e} dx, all cells {ephi_all:.3e} dx, "
               f"u rel (fluid faces) {eu:.3e}, wall ties {ties}, xi {exi:.3e} dx, "
               f"cg {sg['cg_iterations']} it / {sg['cg_refinements']} replacements, residual {sg['cg_residual']:.2e}")
     assert sg["status"] == capi.OK

@@ -86,6 +86,74 @@ def test_weno5_keeps_a_planar_sdf(oracle_mod):
     assert np.max(np.abs(out - phi)[inner]) < 1e-10
 
 
+def test_weno5_reinit_amplifies_rounding_along_3d_diagonals(oracle_mod):
+    """A property of the reference's constants, not of any port: Reinitialization::solve<5>
+    with dτ = 0.9·dx (LevelSetLiquid.cpp:1156) amplifies small perturbations of level sets
+    whose normal lies near a 3D diagonal.  Dimension by dimension, the TVD-RK3/WENO5 step
+    moves information at 0.9·(|n_x| + |n_y| + |n_z|) cells per step, 1.56 along (1,1,1)
+    against 0.9 along an axis.  A planar distance function is a fixed point, so the oracle
+    run twice, once on it and once on it times 1 + 1e-12·noise, shows the growth directly:
+    along (1,1,1) at dτ = 0.9·dx the 30 iterations amplify the difference 20-60 times
+    (also at 0.7·dx); along an axis they damp it, and at dτ = 0.5·dx it stays near its
+    size.  Away from the interface (beyond the reach of its
+    information, |φ| > 15·dx in a scene) FP32 and FP64 runs therefore differ by amplified
+    rounding, while inside the band they agree."""
+    n = 40
+    dx = 1.0 / n
+    c = (np.arange(n) + 0.5) * dx
+    Z, Y, X = np.meshgrid(c, c, c, indexing="ij")
+    noise = 1 + 1e-12 * np.random.default_rng(0).standard_normal((n, n, n))
+    inner = (slice(8, -8),) * 3
+
+    def gain(phi, cfl):
+        d_in = np.max(np.abs(phi * noise - phi)[inner])
+        d_out = np.max(np.abs(oracle_mod.reinit(phi * noise, dx, 30, cfl) - oracle_mod.reinit(phi, dx, 30, cfl))[inner])
+        return d_out / d_in
+
+    diag = (X + Y + Z) / np.sqrt(3) - 0.1
+    assert gain(diag, 0.9) > 10
+    assert gain(diag, 0.5) < 3
+    assert gain(X - 0.1, 0.9) < 1
+
+
+def test_far_field_does_not_feed_back_into_the_band(oracle_mod):
+    """The cells beyond the level-set band (|φ| > 15·dx) are where the reinitialisation
+    amplifies rounding (previous test).  Perturbing all of them by up to 0.1·dx, the size
+    of the FP32/FP64 difference there at 128^3, and restarting (φ0 = φ takes the perturbed
+    values into the state that later steps read) moves φ inside the band by at most
+    1e-3·dx and the velocity by at most 1e-4 of max|u| over the next three steps."""
+    from helpers import LEVEL_SET_BAND
+    sc = scenes.dam_break(3, 36)
+    dx = sc.grid.spacing
+
+    def evolved():
+        o = oracle_mod.OracleSim(sc.grid, host_default_config())
+        load_scene(o, sc)
+        o.initialize()
+        o.stage("restart")
+        for dt in scenes.frame_time_steps(o.max_speed, 3, 25, 1.0, dx):
+            o.advance(dt)
+        return o
+
+    a, b = evolved(), evolved()
+    phi = b.download(capi.FIELD_LEVEL_SET)
+    far = np.abs(phi) > LEVEL_SET_BAND * dx
+    assert far.sum() > phi.size // 4
+    b.upload(capi.FIELD_LEVEL_SET, phi + far * np.random.default_rng(1).uniform(-0.1, 0.1, phi.shape) * dx)
+    a.stage("restart")
+    b.stage("restart")
+    for dt in scenes.frame_time_steps(a.max_speed, 3, 25, 1.0, dx):
+        a.advance(dt)
+        b.advance(dt)
+        pa, pb = a.download(capi.FIELD_LEVEL_SET), b.download(capi.FIELD_LEVEL_SET)
+        band = np.abs(pa) <= LEVEL_SET_BAND * dx
+        assert np.max(np.abs(pa - pb)[band]) <= 1e-3 * dx
+        ua, ub = a.download(capi.FIELD_VELOCITY), b.download(capi.FIELD_VELOCITY)
+        assert np.max(np.abs(ua - ub)) <= 1e-4 * np.max(np.abs(ua))
+    a.close()
+    b.close()
+
+
 def test_restart_resets_reference_map(oracle_mod):
     sc = scenes.dam_break(2, 24)
     o = oracle_mod.OracleSim(sc.grid, host_default_config())
