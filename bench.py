@@ -54,11 +54,14 @@ def parse():
     p.add_argument("--no-default-build", action="store_true",
                    help="skip the same workload in the reference's default build (Newton restart + fast marching)")
     p.add_argument("--seed", type=int, default=0, help="drop: seed of the sphere's centre")
-    p.add_argument("--workload", choices=["dam", "batch", "serve", "drop", "reinit"], default="dam",
+    p.add_argument("--workload", choices=["dam", "batch", "serve", "drop", "reinit", "drift"], default="dam",
                    help="dam: the 128^3 dam break (default line, with mixed and batch sub-objects); "
                         "batch: 48 uneven pool scenes only; serve: the Poisson request stream only; "
                         "drop: the 256^3 drop into a pool, mixed against FP64 over K steps with per-field errors; "
-                        "reinit: the dam break's reinitialisation stage alone, K times after W (for profiling one kernel)")
+                        "reinit: the dam break's reinitialisation stage alone, K times after W (for profiling one kernel); "
+                        "drift: the FP64 form against the CPU oracle over K steps of the dam break (--dim 2 or 3), "
+                        "per-field differences and volumes at steps 1, 10, 50 and K")
+    p.add_argument("--dim", type=int, default=3, help="drift: 2 or 3")
     p.add_argument("--batch-scenes", type=int, default=48)
     p.add_argument("--batch-cg-cells", type=int, default=None,
                    help="batch: interior cells per pressure-solve block (default: the measured best)")
@@ -470,6 +473,45 @@ def run_drop(args, torch, stream, world: int, W: int, K: int) -> dict:
                      "errors_mixed_vs_fp64": errors}}
 
 
+def run_drift(args, torch) -> dict:
+    """The plain FP64 form and the CPU oracle (a bit-exact port of the reference's FP64 path,
+    tests/test_ref_pin.py) advance the same dam break with one dt sequence (the Simulator's
+    CFL-1 policy on the GPU's velocity) for K steps; per-field differences at steps 1, 10, 50
+    and K, and the volume diagnostic of both at every step."""
+    from garm import capi, scenes
+    from oracle import oracle as O
+    sc = scenes.dam_break(args.dim, args.n)
+    dx = sc.grid.spacing
+    g = capi.Simulation(sc.grid, capi.default_config(precision=capi.PRECISION_FP64, record_volume=1))
+    o = O.OracleSim(sc.grid, g.cfg)
+    for s in (g, o):
+        s.upload(capi.FIELD_LEVEL_SET, sc.phi.ravel())
+        s.upload(capi.FIELD_VELOCITY, sc.velocity)
+        s.initialize()
+        s.stage("restart")
+    K = args.steps
+    marks = {m for m in (1, 10, 50, K) if 1 <= m <= K}
+    rows, vg, vo, rg, ro = {}, [], [], 0, 0
+    t_cpu = 0.0
+    for k, dt in enumerate(scenes.frame_time_steps(g.max_speed, K, 25, 1.0, dx), 1):
+        sg = g.advance(dt)
+        t0 = time.perf_counter()
+        so = o.advance(dt)
+        t_cpu += time.perf_counter() - t0
+        rg += sg["restarted"]
+        ro += so["restarted"]
+        vg.append(sg["volume"])
+        vo.append(o.volume())
+        if k in marks:
+            rows[str(k)] = {"restarts_gpu": rg, "restarts_oracle": ro, **field_errors(g, o, dx),
+                            "volume_rel_diff": abs(vg[-1] - vo[-1]) / abs(vo[-1])}
+    g.close()
+    o.close()
+    return {"workload": f"{args.dim}D dam break {args.n}^{args.dim}, plain FP64 GPU form against the CPU oracle, {K} steps",
+            "drift": rows, "volume_drift_gpu": (vg[-1] - vg[0]) / vg[0], "volume_drift_oracle": (vo[-1] - vo[0]) / vo[0],
+            "cpu_s_per_step": t_cpu / K}
+
+
 def run_garm(args) -> None:
     import numpy as np
     import torch
@@ -497,6 +539,13 @@ def run_garm(args) -> None:
         if world > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
+        return
+    if args.workload == "drift":
+        sub = run_drift(args, torch)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": None, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+                              "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                              "data": "synthetic", "config": {"workload": sub.pop("workload"), "n": n}, **sub}), flush=True)
         return
     if args.workload in ("batch", "serve"):
         clocks = Clocks(local)

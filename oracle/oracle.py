@@ -70,25 +70,79 @@ def load() -> C.CDLL:
     return lib
 
 
+REF_LIB_PATH = REPO / "oracle" / "_ref" / "libgarmref.so"
+REF_BUILD = REPO / "oracle" / "build_ref.sh"
+_REF = None
+
+
+def ref_available() -> bool:
+    """True when the reference binary (oracle/_ref, built from the reference's own sources by
+    oracle/build_ref.sh) exists or can be built here."""
+    if REF_LIB_PATH.exists():
+        return True
+    return Path("/root/reference/Source/Core/LevelSetLiquid.cpp").exists()
+
+
+def load_ref() -> C.CDLL:
+    """The reference binary: the unmodified LevelSetLiquid<Dim> driven by oracle/ref_harness.cpp."""
+    global _REF
+    if _REF is not None:
+        return _REF
+    if not REF_LIB_PATH.exists():
+        import subprocess
+        subprocess.run(["sh", str(REF_BUILD)], check=True, stdout=subprocess.DEVNULL)
+    lib = C.CDLL(str(REF_LIB_PATH))
+    lib.ref_create.restype = C.c_void_p
+    lib.ref_create.argtypes = [C.POINTER(GridDesc), C.POINTER(Config)]
+    lib.ref_destroy.argtypes = [C.c_void_p]
+    lib.ref_field_bytes.restype = C.c_size_t
+    lib.ref_field_bytes.argtypes = [C.c_void_p, C.c_int]
+    lib.ref_upload.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]
+    lib.ref_download.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]
+    lib.ref_initialize.argtypes = [C.c_void_p]
+    lib.ref_restart.argtypes = [C.c_void_p]
+    lib.ref_advance.argtypes = [C.c_void_p, C.c_double, C.POINTER(StepStats)]
+    lib.ref_stage.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(StepStats), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.ref_max_speed.restype = C.c_double
+    lib.ref_max_speed.argtypes = [C.c_void_p]
+    lib.ref_volume.restype = C.c_double
+    lib.ref_volume.argtypes = [C.c_void_p]
+    lib.ref_profile.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    lib.ref_set_threads.argtypes = [C.c_int]
+    lib.ref_max_threads.restype = C.c_int
+    lib.ref_reinit.argtypes = [C.c_int, C.POINTER(C.c_int), C.c_double, C.POINTER(C.c_double), C.c_int, C.c_double]
+    _REF = lib
+    return lib
+
+
 def _dp(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
 class OracleSim:
-    """CPU FP64 LevelSetLiquid<Dim> with the same field/stage vocabulary as garm.capi.Simulation."""
+    """CPU FP64 LevelSetLiquid<Dim> with the same field/stage vocabulary as garm.capi.Simulation:
+    the port (garm_oracle.cpp)."""
+
+    PREFIX = "orc_"
+
+    def _lib(self) -> C.CDLL:
+        return load()
+
+    def _fn(self, name: str):
+        return getattr(self.lib, self.PREFIX + name)
 
     def __init__(self, grid: GridDesc, cfg: Config):
-        self.lib = load()
+        self.lib = self._lib()
         self.grid = grid
         self.cfg = cfg
-        self.h = self.lib.orc_create(C.byref(grid), C.byref(cfg))
+        self.h = self._fn("create")(C.byref(grid), C.byref(cfg))
         if not self.h:
-            raise ValueError("orc_create failed")
+            raise ValueError(f"{self.PREFIX}create failed")
         self.shapes = field_shapes(grid)
 
     def close(self):
         if self.h:
-            self.lib.orc_destroy(self.h)
+            self._fn("destroy")(self.h)
             self.h = None
 
     def __del__(self):
@@ -100,38 +154,38 @@ class OracleSim:
     def upload(self, field: int, data: np.ndarray) -> None:
         dtype = np.uint8 if field == FIELD_ADV_REGION else np.float64
         a = np.ascontiguousarray(data, dtype=dtype)
-        if self.lib.orc_upload(self.h, field, a.ctypes.data, a.nbytes) != OK:
+        if self._fn("upload")(self.h, field, a.ctypes.data, a.nbytes) != OK:
             raise ValueError(f"orc_upload {FIELD_NAMES[field]}")
 
     def download(self, field: int) -> np.ndarray:
-        n = self.lib.orc_field_bytes(self.h, field)
+        n = self._fn("field_bytes")(self.h, field)
         dtype = np.uint8 if field == FIELD_ADV_REGION else np.float64
         out = np.empty(n // np.dtype(dtype).itemsize, dtype=dtype)
-        if self.lib.orc_download(self.h, field, out.ctypes.data, out.nbytes) != OK:
+        if self._fn("download")(self.h, field, out.ctypes.data, out.nbytes) != OK:
             raise ValueError(f"orc_download {FIELD_NAMES[field]}")
         return out
 
     def initialize(self) -> int:
-        return self.lib.orc_initialize(self.h)
+        return self._fn("initialize")(self.h)
 
     def advance(self, dt: float) -> dict:
         st = StepStats()
-        rc = self.lib.orc_advance(self.h, float(dt), C.byref(st))
+        rc = self._fn("advance")(self.h, float(dt), C.byref(st))
         d = st.as_dict()
         d["status"] = rc
         return d
 
     def max_speed(self) -> float:
-        return self.lib.orc_max_speed(self.h)
+        return self._fn("max_speed")(self.h)
 
     def volume(self) -> float:
         """calculateVolume (LevelSetLiquid.cpp:1162-1190) of the current tmp level set."""
-        return self.lib.orc_volume(self.h)
+        return self._fn("volume")(self.h)
 
     def stage(self, name: str, arg: float = 0.0):
         st = StepStats()
         keep, tot, bad = C.c_int(), C.c_int(), C.c_int()
-        rc = self.lib.orc_stage(self.h, STAGES[name], float(arg), C.byref(st), C.byref(keep), C.byref(tot), C.byref(bad))
+        rc = self._fn("stage")(self.h, STAGES[name], float(arg), C.byref(st), C.byref(keep), C.byref(tot), C.byref(bad))
         if rc not in (OK, NOT_CONVERGED):
             raise ValueError(f"orc_stage {name}: {rc}")
         if name == "rm_check":
@@ -141,6 +195,37 @@ class OracleSim:
             d["status"] = rc
             return d
         return None
+
+
+class RefSim(OracleSim):
+    """The reference itself: LevelSetLiquid<Dim> from the reference's own sources
+    (oracle/_ref), with the port's field/stage vocabulary.  Only the reference's constants
+    (30 WENO5 iterations at 0.9, its restart test, 2000 solver iterations, FP64) are
+    accepted; rm_check returns (keep, -1, -1), the reference not exposing its counts."""
+
+    PREFIX = "ref_"
+
+    def _lib(self) -> C.CDLL:
+        return load_ref()
+
+    def profile(self) -> dict:
+        """The reference's own stage timers of the last step (LevelSetLiquid.cpp:601-606), seconds."""
+        out = (C.c_double * 4)()
+        self.lib.ref_profile(self.h, out)
+        return {"tadvect": out[0], "tproject": out[1], "trestart": out[2], "textrap": out[3]}
+
+
+def ref_reinit(phi: np.ndarray, spacing: float, iters: int, cfl: float) -> np.ndarray:
+    """Reinitialization::solve<5> of the reference binary on a bare cell field."""
+    a = np.ascontiguousarray(phi, dtype=np.float64).copy()
+    size = (C.c_int * 3)(*([int(x) for x in reversed(a.shape)] + [1] * (3 - a.ndim)))
+    if load_ref().ref_reinit(a.ndim, size, float(spacing), _dp(a), int(iters), float(cfl)) != OK:
+        raise ValueError("ref_reinit")
+    return a
+
+
+def ref_set_threads(n: int) -> None:
+    load_ref().ref_set_threads(int(n))
 
 
 def set_threads(n: int) -> None:
