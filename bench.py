@@ -62,6 +62,9 @@ def parse():
                         "drift: the FP64 form against the CPU oracle over K steps of the dam break (--dim 2 or 3), "
                         "per-field differences and volumes at steps 1, 10, 50 and K")
     p.add_argument("--dim", type=int, default=3, help="drift: 2 or 3")
+    p.add_argument("--spread", action="store_true",
+                   help="drift: also run the oracle from an initial state changed by one ulp and report its own "
+                        "deviation at the same steps (the reference algorithm's conditioning)")
     p.add_argument("--batch-scenes", type=int, default=48)
     p.add_argument("--batch-cg-cells", type=int, default=None,
                    help="batch: interior cells per pressure-solve block (default: the measured best)")
@@ -420,7 +423,10 @@ def run_drop(args, torch, stream, world: int, W: int, K: int) -> dict:
     sc = scenes.drop(n, seed=args.seed)
     dx = sc.grid.spacing
     sims = {}
-    for name, prec in (("fp64", capi.PRECISION_FP64), ("mixed", capi.PRECISION_MIXED)):
+    # mixed_fixed: the mixed form held to the FP64 form's restart schedule
+    # (garm_sim_set_restart_override before each step), which separates the drift of the
+    # fields from the restart decisions that the two roundings may take differently
+    for name, prec in (("fp64", capi.PRECISION_FP64), ("mixed", capi.PRECISION_MIXED), ("mixed_fixed", capi.PRECISION_MIXED)):
         s = capi.Simulation(sc.grid, capi.default_config(precision=prec), stream=stream.cuda_stream)
         s.upload(capi.FIELD_LEVEL_SET, sc.phi.ravel())
         s.upload(capi.FIELD_VELOCITY, sc.velocity)
@@ -432,25 +438,31 @@ def run_drop(args, torch, stream, world: int, W: int, K: int) -> dict:
     cg = {k: [] for k in sims}
     launches = {k: 0 for k in sims}
     restarts = {k: 0 for k in sims}
-    errors = {}
+    errors, errors_fixed = {}, {}
+    last_fp64_restart = 0
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(world)
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", 0)))
     clocks.start()
     for step, dt in enumerate(scenes.frame_time_steps(sims["fp64"].max_speed, K, 25, 1.0, dx), 1):
         for name, s in sims.items():
+            if name == "mixed_fixed":
+                s.set_restart_override(capi.RESTART_ALWAYS if last_fp64_restart else capi.RESTART_NEVER)
             l0 = s.launch_count()
             e0.record(stream)
             st = s.advance(dt)
             e1.record(stream)
             torch.cuda.synchronize()
             restarts[name] += st["restarted"]
+            if name == "fp64":
+                last_fp64_restart = st["restarted"]
             if step > W:
                 times[name].append(e0.elapsed_time(e1))
                 cg[name].append(st["cg_iterations"])
                 launches[name] += s.launch_count() - l0
         if step in marks:
             errors[str(step)] = field_errors(sims["mixed"], sims["fp64"], dx)
+            errors_fixed[str(step)] = field_errors(sims["mixed_fixed"], sims["fp64"], dx)
     clk = clocks.stop()
     timed = max(K - W, 1)
     legs = {}
@@ -468,6 +480,8 @@ def run_drop(args, torch, stream, world: int, W: int, K: int) -> dict:
             "workload": f"3D drop into a pool {n}^3 (seed {args.seed}), mixed and FP64 on one dt sequence, "
                         f"{K} steps, the first {W} untimed",
             "drop": {"fp64": legs["fp64"], "mixed": legs["mixed"],
+                     "mixed_on_fp64_restart_schedule": {"restarts": legs["mixed_fixed"]["restarts"],
+                                                        "errors_vs_fp64": errors_fixed},
                      "speedup_vs_fp64": legs["mixed"]["value"] / legs["fp64"]["value"],
                      "sphere": {"center": [float(c) for c in sc.meta["center"]], "radius": sc.meta["radius"]},
                      "errors_mixed_vs_fp64": errors}}
@@ -484,9 +498,20 @@ def run_drift(args, torch) -> dict:
     dx = sc.grid.spacing
     g = capi.Simulation(sc.grid, capi.default_config(precision=capi.PRECISION_FP64, record_volume=1))
     o = O.OracleSim(sc.grid, g.cfg)
-    for s in (g, o):
-        s.upload(capi.FIELD_LEVEL_SET, sc.phi.ravel())
-        s.upload(capi.FIELD_VELOCITY, sc.velocity)
+    sims = [g, o]
+    q = None
+    if args.spread:
+        import numpy as np
+        q = O.OracleSim(sc.grid, g.cfg)
+        sims.append(q)
+    for s in sims:
+        phi0, u0 = sc.phi.ravel(), sc.velocity
+        if s is q:  # every value scaled by 1 + U(-1e-15, 1e-15): one or two ulps
+            rng = np.random.default_rng(11)
+            phi0 = phi0 * (1 + 1e-15 * rng.uniform(-1, 1, phi0.shape))
+            u0 = u0 * (1 + 1e-15 * rng.uniform(-1, 1, u0.shape))
+        s.upload(capi.FIELD_LEVEL_SET, phi0)
+        s.upload(capi.FIELD_VELOCITY, u0)
         s.initialize()
         s.stage("restart")
     K = args.steps
@@ -498,6 +523,8 @@ def run_drift(args, torch) -> dict:
         t0 = time.perf_counter()
         so = o.advance(dt)
         t_cpu += time.perf_counter() - t0
+        if q is not None:
+            q.advance(dt)
         rg += sg["restarted"]
         ro += so["restarted"]
         vg.append(sg["volume"])
@@ -505,8 +532,10 @@ def run_drift(args, torch) -> dict:
         if k in marks:
             rows[str(k)] = {"restarts_gpu": rg, "restarts_oracle": ro, **field_errors(g, o, dx),
                             "volume_rel_diff": abs(vg[-1] - vo[-1]) / abs(vo[-1])}
-    g.close()
-    o.close()
+            if q is not None:
+                rows[str(k)]["oracle_ulp_spread"] = field_errors(q, o, dx)
+    for s in sims:
+        s.close()
     return {"workload": f"{args.dim}D dam break {args.n}^{args.dim}, plain FP64 GPU form against the CPU oracle, {K} steps",
             "drift": rows, "volume_drift_gpu": (vg[-1] - vg[0]) / vg[0], "volume_drift_oracle": (vo[-1] - vo[0]) / vo[0],
             "cpu_s_per_step": t_cpu / K}

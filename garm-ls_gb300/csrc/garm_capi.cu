@@ -802,6 +802,16 @@ garm_status garm_sim_set_clock(garm_sim *sim, unsigned frame_rate, double cfl) {
 	return sync(s);
 }
 
+garm_status garm_sim_set_restart_override(garm_sim *sim, int mode) {
+	if (!sim || mode < GARM_RESTART_AUTO || mode > GARM_RESTART_ALWAYS) return GARM_INVALID;
+	State &s = sim->s;
+	if (cudaMemcpyAsync(s.redI32 + kRestartOverride, &mode, sizeof(int), cudaMemcpyHostToDevice, s.stream) != cudaSuccess) {
+		cudaGetLastError();
+		return GARM_CUDA_ERROR;
+	}
+	return sync(s);
+}
+
 garm_status garm_sim_advance_auto(garm_sim *sim, int steps, garm_step_stats *stats) {
 	if (!sim || steps < 1) return GARM_INVALID;
 	return advanceAuto(sim->s, steps, stats);

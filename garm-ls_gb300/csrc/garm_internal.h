@@ -96,7 +96,7 @@ struct State {
 	int *cgInts = nullptr;
 	// reductions
 	unsigned long long *redU64 = nullptr;
-	int *redI32 = nullptr;
+	int *redI32 = nullptr;  // 16 ints: reduction counts; [kRestartOverride] the restart override
 	// device staging for AoS<->SoA transfers
 	void *stage = nullptr; size_t stageBytes = 0;
 	// every device allocation, freed by garm_sim_destroy
@@ -192,6 +192,8 @@ template <int D, typename T> garm_status copyField(State &s, void *dst, const vo
 // that has no cached or pinned launch plan runs the default column plan instead of
 // timing the candidates (no event creation, no stream synchronisation).
 template <int D, typename T> garm_status reinitRaw(cudaStream_t st, const int *size, double dx, T *phi, T *a, T *b, int iters, double cfl, int *err, bool tune = true);
+
+constexpr int kRestartOverride = 8;  // word of State::redI32 that garm_sim_set_restart_override sets
 
 inline garm_status cudaStatus(cudaError_t e) { return e == cudaSuccess ? GARM_OK : GARM_CUDA_ERROR; }
 // Work after forkAux(k) on s.aux runs beside work on s.stream until joinAux(k).

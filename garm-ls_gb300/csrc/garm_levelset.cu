@@ -1112,11 +1112,13 @@ __global__ void __launch_bounds__(kBlock) kCheckRefMap(int64_t N, const T *ori, 
 	}
 }
 
-// restartFlag = !(bad <= ratio * tot): the decision of advance (LevelSetLiquid.cpp:631)
+// restartFlag = !(bad <= ratio * tot): the decision of advance (LevelSetLiquid.cpp:631),
+// unless counts[kRestartOverride] holds a decision set by garm_sim_set_restart_override
+// (1: keep the reference map, 2: restart).
 __global__ void kRestartDecision(const int *counts, double ratio, int *flag, double *stats, const unsigned long long *counter) {
 	double *rec = stepRecord(stats, counter);
-	const int tot = counts[0], bad = counts[1];
-	const int restart = (1.0 * bad <= ratio * tot) ? 0 : 1;
+	const int tot = counts[0], bad = counts[1], force = counts[kRestartOverride];
+	const int restart = force == GARM_RESTART_NEVER ? 0 : force == GARM_RESTART_ALWAYS ? 1 : ((1.0 * bad <= ratio * tot) ? 0 : 1);
 	*flag = restart;
 	if (rec) { rec[kStRestarted] = restart; rec[kStRmTotal] = tot; rec[kStRmBad] = bad; }
 }

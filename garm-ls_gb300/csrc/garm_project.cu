@@ -178,55 +178,21 @@ struct CgArgs {
 __device__ __forceinline__ double ldcg(const double *p) { return *p; }
 __device__ __forceinline__ float ldcg(const float *p) { return *p; }
 
-// Block partial sums of NV values → partials[v*maxBlocks + blockIdx]
-template <int NV>
-__device__ __forceinline__ void blockPartials(double (&acc)[NV], double *partials, int maxBlocks, double *sh) {
-	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-	// the NV warp sums level by level, so their shuffles and additions overlap
-#pragma unroll
-	for (int o = 16; o > 0; o >>= 1) {
-		double y[NV];
-#pragma unroll
-		for (int v = 0; v < NV; v++) y[v] = __shfl_xor_sync(0xffffffffu, acc[v], o);
-#pragma unroll
-		for (int v = 0; v < NV; v++) acc[v] += y[v];
-	}
-	if (lane == 0) {
-#pragma unroll
-		for (int v = 0; v < NV; v++) sh[v * 16 + w] = acc[v];
-	}
-	__syncthreads();
-	if (threadIdx.x < NV) {
-		double s = 0;
-		for (int q = 0; q < (int)(blockDim.x >> 5); q++) s += sh[threadIdx.x * 16 + q];
-		partials[threadIdx.x * maxBlocks + blockIdx.x] = s;
-	}
-	__syncthreads();
-}
+// Shared memory of the reductions, in doubles: [0, 48) the warp sums of a block's partials
+// ([v*16 + w], as doubles or float pairs); [96, 98) reciprocals the mixed form keeps
+// across iterations; [kShOut, kShOut + 8) the grid totals broadcast to the block.
+constexpr int kShOut = 104, kShSize = 112;
 
-// Sum of the gridDim partials of slot v, identical in every block (a fixed
-// partition of the blocks over lanes and warps and fixed shuffle trees:
-// deterministic).  Thread t loads the partials of blocks t, t + blockDim, ..., all
-// NV values of a block together, so the whole grid's partials arrive in one L2
-// round trip; warp 0 sums the warp sums from shared memory, its lane 0 runs `fin`
-// on the totals (scalar work done once per block) and the results are broadcast.
-// Shared memory: sh[0, NOUT) holds the results, sh[8 + 32 v + w] the warp sums.
-template <int NV, int NOUT, typename Fin>
-__device__ __forceinline__ void gridTotals(const double *partials, int maxBlocks, double (&out)[NOUT], double *sh, Fin fin) {
-	static_assert(NOUT >= NV && NOUT <= 8, "outputs include the sums");
+// Block partial sums of NV values → partials[v*maxBlocks + blockIdx], then the block's
+// arrival at the grid barrier.  Warp sums go through shared memory to warp 0, whose lane 0
+// (thread 0) stores the partials and arrives: the __syncthreads before warp 0 reads the warp
+// sums orders every thread's earlier writes of the phase, and thread 0's release covers
+// them.  The caller waits with gridWait.
+template <int NV>
+__device__ __forceinline__ void blockPartials(double (&acc)[NV], double *partials, int maxBlocks, double *sh, unsigned *bar, unsigned &epoch) {
 	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-	const int nb = gridDim.x;
-	double t[NOUT];
-#pragma unroll
-	for (int v = 0; v < NV; v++) t[v] = 0;
-	for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-		double q[NV];
-#pragma unroll
-		for (int v = 0; v < NV; v++) q[v] = ldcg(partials + v * maxBlocks + b);
-#pragma unroll
-		for (int v = 0; v < NV; v++) t[v] += q[v];
-	}
-	auto warpTree = [&]() {
+	auto tree = [&](double (&t)[NV]) {
+		// the NV warp sums level by level, so their shuffles and additions overlap
 #pragma unroll
 		for (int o = 16; o > 0; o >>= 1) {
 			double y[NV];
@@ -236,29 +202,65 @@ __device__ __forceinline__ void gridTotals(const double *partials, int maxBlocks
 			for (int v = 0; v < NV; v++) t[v] += y[v];
 		}
 	};
-	if (w * 32 < nb) {
-		warpTree();
-		if (lane == 0) {
+	tree(acc);
+	if (lane == 0) {
 #pragma unroll
-			for (int v = 0; v < NV; v++) sh[8 + v * 32 + w] = t[v];
-		}
+		for (int v = 0; v < NV; v++) sh[v * 16 + w] = acc[v];
 	}
 	__syncthreads();
 	if (w == 0) {
-		const int nl = min(nw, (nb + 31) >> 5);
+		double t[NV];
 #pragma unroll
-		for (int v = 0; v < NV; v++) t[v] = lane < nl ? sh[8 + v * 32 + lane] : 0.0;
-		warpTree();
+		for (int v = 0; v < NV; v++) t[v] = lane < nw ? sh[v * 16 + lane] : 0.0;
+		tree(t);
+		if (lane == 0) {
+#pragma unroll
+			for (int v = 0; v < NV; v++) partials[v * maxBlocks + blockIdx.x] = t[v];
+			gridArrive(bar, epoch);
+		}
+	}
+}
+
+// Sum of the gridDim partials of slot v, identical in every block (a fixed partition of
+// the blocks over the lanes of warp 0 and a fixed shuffle tree: deterministic).  Lane l
+// loads the partials of blocks l, l + 32, ..., all NV values together, so the grid's
+// partials arrive in one L2 round trip; lane 0 runs `fin` on the totals (scalar work done
+// once per block) and the NOUT results reach the block through shared memory.  One block
+// barrier; the next writer of the results is this function in a later reduction, which no
+// thread reaches before every thread has read them.
+template <int NV, int NOUT, typename Fin>
+__device__ __forceinline__ void gridTotals(const double *partials, int maxBlocks, double (&out)[NOUT], double *sh, Fin fin) {
+	static_assert(NOUT >= NV && NOUT <= 8, "outputs include the sums");
+	const int lane = threadIdx.x & 31;
+	if (threadIdx.x < 32) {
+		const int nb = gridDim.x;
+		double t[NOUT];
+#pragma unroll
+		for (int v = 0; v < NV; v++) t[v] = 0;
+		for (int b = lane; b < nb; b += 32) {
+			double q[NV];
+#pragma unroll
+			for (int v = 0; v < NV; v++) q[v] = ldcg(partials + v * maxBlocks + b);
+#pragma unroll
+			for (int v = 0; v < NV; v++) t[v] += q[v];
+		}
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			double y[NV];
+#pragma unroll
+			for (int v = 0; v < NV; v++) y[v] = __shfl_xor_sync(0xffffffffu, t[v], o);
+#pragma unroll
+			for (int v = 0; v < NV; v++) t[v] += y[v];
+		}
 		if (lane == 0) {
 			fin(t);
 #pragma unroll
-			for (int v = 0; v < NOUT; v++) sh[v] = t[v];
+			for (int v = 0; v < NOUT; v++) sh[kShOut + v] = t[v];
 		}
 	}
 	__syncthreads();
 #pragma unroll
-	for (int v = 0; v < NOUT; v++) out[v] = sh[v];
-	__syncthreads();
+	for (int v = 0; v < NOUT; v++) out[v] = sh[kShOut + v];
 }
 
 struct NoFin { __device__ void operator()(double *) const {} };
@@ -335,9 +337,9 @@ __device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, NbW64 *enS, unsi
 	}
 	{
 		double acc[3] = {acc0, acc1, acc2};
-		blockPartials<3>(acc, a.partials, a.maxBlocks, sh);
+		blockPartials<3>(acc, a.partials, a.maxBlocks, sh, a.bar, epoch);
 	}
-	if (!gridSync(a.bar, a.err, epoch)) { *ok = false; return 0; }
+	if (!gridWait(a.bar, a.err, epoch)) { *ok = false; return 0; }
 	double tot[6];
 	gridTotals<3, 6>(a.partials, a.maxBlocks, tot, sh, [](double *t) { t[3] = 0; t[4] = t[0] / t[1]; t[5] = 0; });
 	double gamma = tot[0];
@@ -439,13 +441,13 @@ __device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, NbW64 *enS, unsi
 			}
 		}
 		double acc[3] = {g, d, rr};
-		blockPartials<3>(acc, a.partials, a.maxBlocks, sh);
+		blockPartials<3>(acc, a.partials, a.maxBlocks, sh, a.bar, epoch);
 		// β = γ/γ_old and α = γ/(δ - βγ/α_old) with the reciprocals of the known γ_old and
 		// γ_old·α_old formed before the barrier: one division after it
 		// (warp 0 alone, whose lane 0 finishes the totals)
 		double invG = 0, invGA = 0;
 		if (threadIdx.x < 32) { invG = 1.0 / gamma; invGA = invG / alpha; }
-		if (!gridSync(a.bar, a.err, epoch)) { *ok = false; it++; break; }
+		if (!gridWait(a.bar, a.err, epoch)) { *ok = false; it++; break; }
 		gridTotals<3, 6>(a.partials, a.maxBlocks, tot, sh, [invG, invGA, threshold](double *t) {
 			t[3] = t[0] * invG;
 			t[4] = t[0] / fma(-t[0] * t[0], invGA, t[1]);
@@ -467,7 +469,7 @@ __device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, NbW64 *enS, unsi
 // FP64 form: one PCG on the FP64 operator.
 template <int NB>
 __global__ void __launch_bounds__(kCgBlock) kPcgFp64(CgArgs a) {
-	__shared__ double sh[8 + 3 * 32];  // block partials, then the grid totals' warp sums
+	__shared__ double sh[kShSize];  // reductions (see kShOut)
 	const int n = *a.nDev;
 	double rr = 0, b2 = 0;
 	bool ok = true;
@@ -531,9 +533,10 @@ __device__ __forceinline__ void dfWarpSumN(DF (&v)[NV]) {
 		for (int q = 0; q < NV; q++) v[q] = dfMerge(v[q], w[q]);
 	}
 }
-// Block sums of NV double-float values → partials (as float pairs) [v*maxBlocks + blockIdx].
+// Block sums of NV double-float values → partials (as float pairs) [v*maxBlocks + blockIdx],
+// then the block's arrival at the grid barrier, as blockPartials.
 template <int NV>
-__device__ __forceinline__ void blockPartialsDF(DF (&acc)[NV], double *partials, int maxBlocks, double *sh) {
+__device__ __forceinline__ void blockPartialsDF(DF (&acc)[NV], double *partials, int maxBlocks, double *sh, unsigned *bar, unsigned &epoch) {
 	float2 *s2 = reinterpret_cast<float2 *>(sh);
 	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
 	dfWarpSumN<NV>(acc);
@@ -554,60 +557,44 @@ __device__ __forceinline__ void blockPartialsDF(DF (&acc)[NV], double *partials,
 		if (lane == 0) {
 #pragma unroll
 			for (int v = 0; v < NV; v++) p2[v * maxBlocks + blockIdx.x] = make_float2(x[v].hi, x[v].lo);
+			gridArrive(bar, epoch);
 		}
 	}
-	__syncthreads();
 }
-// Grid totals of NV double-float partials in the arrangement of gridTotals (one L2
-// round trip for all partials, warp sums in shared memory at sh + 8 as float pairs,
-// a fixed order), widened to FP64 by lane 0 of warp 0, which then runs `fin` on
-// them; the NOUT results are broadcast to the block.
+// Grid totals of NV double-float partials in the arrangement of gridTotals (warp 0 loads
+// every block's partials in one L2 round trip and sums them in a fixed order), widened to
+// FP64 by lane 0, which then runs `fin` on them; the NOUT results are broadcast to the
+// block through shared memory.
 template <int NV, int NOUT, typename Fin>
 __device__ __forceinline__ void gridTotalsDF(const double *partials, int maxBlocks, double (&out)[NOUT], double *sh, Fin fin) {
 	static_assert(NOUT >= NV && NOUT <= 8, "outputs include the sums");
-	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-	const int nb = gridDim.x;
-	const float2 *p2 = reinterpret_cast<const float2 *>(partials);
-	float2 *ws = reinterpret_cast<float2 *>(sh + 8);  // [32 v + w]
-	DF x[NV];
+	const int lane = threadIdx.x & 31;
+	if (threadIdx.x < 32) {
+		const int nb = gridDim.x;
+		const float2 *p2 = reinterpret_cast<const float2 *>(partials);
+		DF x[NV];
 #pragma unroll
-	for (int v = 0; v < NV; v++) x[v] = DF{0.f, 0.f};
-	for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-		float2 q[NV];
+		for (int v = 0; v < NV; v++) x[v] = DF{0.f, 0.f};
+		for (int b = lane; b < nb; b += 32) {
+			float2 q[NV];
 #pragma unroll
-		for (int v = 0; v < NV; v++) q[v] = p2[v * maxBlocks + b];  // ordered by gridSync, as ldcg
+			for (int v = 0; v < NV; v++) q[v] = p2[v * maxBlocks + b];  // ordered by the grid barrier, as ldcg
 #pragma unroll
-		for (int v = 0; v < NV; v++) x[v] = dfMerge(x[v], DF{q[v].x, q[v].y});
-	}
-	if (w * 32 < nb) {
-		dfWarpSumN<NV>(x);
-		if (lane == 0) {
-#pragma unroll
-			for (int v = 0; v < NV; v++) ws[v * 32 + w] = make_float2(x[v].hi, x[v].lo);
-		}
-	}
-	__syncthreads();
-	if (w == 0) {
-		const int nl = min(nw, (nb + 31) >> 5);
-#pragma unroll
-		for (int v = 0; v < NV; v++) {
-			x[v] = DF{0.f, 0.f};
-			if (lane < nl) { const float2 q = ws[v * 32 + lane]; x[v] = DF{q.x, q.y}; }
+			for (int v = 0; v < NV; v++) x[v] = dfMerge(x[v], DF{q[v].x, q[v].y});
 		}
 		dfWarpSumN<NV>(x);
-		double t[NOUT];
-#pragma unroll
-		for (int v = 0; v < NV; v++) t[v] = double(x[v].hi) + double(x[v].lo);
 		if (lane == 0) {
+			double t[NOUT];
+#pragma unroll
+			for (int v = 0; v < NV; v++) t[v] = double(x[v].hi) + double(x[v].lo);
 			fin(t);
 #pragma unroll
-			for (int v = 0; v < NOUT; v++) sh[v] = t[v];
+			for (int v = 0; v < NOUT; v++) sh[kShOut + v] = t[v];
 		}
 	}
 	__syncthreads();
 #pragma unroll
-	for (int v = 0; v < NOUT; v++) out[v] = sh[v];
-	__syncthreads();
+	for (int v = 0; v < NOUT; v++) out[v] = sh[kShOut + v];
 }
 
 // Power of two s with s·rms(r) in [1, 2): the FP32 system is solved for s·r so
@@ -653,9 +640,9 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 	{
 		double acc[1] = {0};
 		for (int64_t i = tid; i < n; i += nthr) { const double b = a.b[i]; acc[0] += b * b; }
-		blockPartials<1>(acc, a.partials, a.maxBlocks, sh);
+		blockPartials<1>(acc, a.partials, a.maxBlocks, sh, a.bar, epoch);
 	}
-	if (!gridSync(a.bar, a.err, epoch)) return;
+	if (!gridWait(a.bar, a.err, epoch)) return;
 	double b2v[1];
 	gridTotals<1, 1>(a.partials, a.maxBlocks, b2v, sh, NoFin{});
 	const double b2 = b2v[0];
@@ -683,9 +670,9 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 			dfAddProd(acc[0], bi, ui);
 			dfAddProd(acc[1], wi, ui);
 		}
-		blockPartialsDF<2>(acc, a.partials, a.maxBlocks, sh);
+		blockPartialsDF<2>(acc, a.partials, a.maxBlocks, sh, a.bar, epoch);
 	}
-	if (!gridSync(a.bar, a.err, epoch)) return;
+	if (!gridWait(a.bar, a.err, epoch)) return;
 	// tot: γ, δ, |r|^2, β, α, the replacement decision, FP32 β and α packed.  The lane
 	// that finishes the totals also keeps 1/γ and 1/(γα) for the next iteration's β and α
 	// in sh[96], sh[97], which no reduction touches.
@@ -785,7 +772,7 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 				}
 			}
 			cur ^= 1;
-			blockPartialsDF<3>(acc, a.partials, a.maxBlocks, sh);
+			blockPartialsDF<3>(acc, a.partials, a.maxBlocks, sh, a.bar, epoch);
 		}
 		// β = γ/γ_old and α = γ/den, den = δ - βγ/α_old = δ - γ²/(γ_old α_old), from the
 		// kept 1/γ_old and 1/(γ_old α_old).  One reciprocal, of q = γ·den, gives α = γ²/q
@@ -793,7 +780,7 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 		// reciprocal from an FP32 seed (2 ulp), a plain division outside its range.  The same
 		// lane decides whether the residual is replaced after this iteration.
 		const double gOld = gamma;
-		if (!gridSync(a.bar, a.err, epoch)) break;
+		if (!gridWait(a.bar, a.err, epoch)) break;
 		const int itNext = it + 1;
 		gridTotalsDF<3, 7>(a.partials, a.maxBlocks, tot, sh, [=](double *t) {
 			const double g = t[0];
@@ -840,9 +827,9 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 				a.r64[i] = ri;
 				acc2[0] += ri * ri;
 			}
-			blockPartials<1>(acc2, a.partials, a.maxBlocks, sh);
+			blockPartials<1>(acc2, a.partials, a.maxBlocks, sh, a.bar, epoch);
 		}
-		if (!gridSync(a.bar, a.err, epoch)) break;
+		if (!gridWait(a.bar, a.err, epoch)) break;
 		double tr[1];
 		gridTotals<1, 1>(a.partials, a.maxBlocks, tr, sh, NoFin{});
 		replOut++;
@@ -887,9 +874,9 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 				}
 			}
 			cur ^= 1;
-			blockPartialsDF<2>(acc, a.partials, a.maxBlocks, sh);
+			blockPartialsDF<2>(acc, a.partials, a.maxBlocks, sh, a.bar, epoch);
 		}
-		if (!gridSync(a.bar, a.err, epoch)) break;
+		if (!gridWait(a.bar, a.err, epoch)) break;
 		gridTotalsDF<2, 7>(a.partials, a.maxBlocks, tot, sh, [gOld, ratio2, alpha, sh](double *t) {
 			t[2] = 0;
 			t[3] = t[0] / (gOld * ratio2);
@@ -904,7 +891,7 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 }
 template <int NB>
 __global__ void __launch_bounds__(kCgBlock) kPcgMixed(CgArgs a) {
-	__shared__ double sh[8 + 3 * 32];  // block partials, then the grid totals' warp sums
+	__shared__ double sh[kShSize];  // reductions (see kShOut)
 	const int n = *a.nDev;
 	unsigned epoch = 0;
 	int it = 0, repl = 0;

@@ -57,4 +57,34 @@ __device__ inline bool gridSync(unsigned *bar, int *err, unsigned &epoch) {
 	return blockErr == 0;
 }
 
+// The two halves of gridSync for callers that order their block's writes themselves:
+// gridArrive (thread 0 only, after a __syncthreads that follows every write of the
+// phase, or after thread 0's own last write) and gridWait (every thread: thread 0 polls,
+// then the block passes __syncthreads).  The reductions of the pressure solve arrive
+// right after thread 0 stores the block's partial sums, which saves two block barriers
+// per grid barrier.
+__device__ __forceinline__ void gridArrive(unsigned *bar, unsigned &epoch) {
+	epoch += gridDim.x;
+	addRelease(bar, 1u);
+}
+__device__ inline bool gridWait(unsigned *bar, int *err, unsigned epoch) {
+	__shared__ int blockErr;
+	if (threadIdx.x == 0) {
+		unsigned long long spins = 0, start = 0;
+		int e;
+		for (;;) {
+			e = *(volatile int *)err;
+			if (ldAcquire(bar) >= epoch || e) break;
+			if ((++spins & 1023ull) == 0) {
+				const unsigned long long now = globalNs();
+				if (start == 0) start = now;
+				if (now - start > kBarrierWaitNs || spins > kBarrierSpinLimit) { atomicExch(err, 1); e = 1; break; }
+			}
+		}
+		blockErr = e;
+	}
+	__syncthreads();
+	return blockErr == 0;
+}
+
 }  // namespace garm

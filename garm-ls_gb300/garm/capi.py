@@ -87,6 +87,7 @@ _SIGS = {
     "garm_sim_finish_load": (C.c_int, [C.c_void_p]),
     "garm_sim_advance": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(StepStats)]),
     "garm_sim_set_clock": (C.c_int, [C.c_void_p, C.c_uint, C.c_double]),
+    "garm_sim_set_restart_override": (C.c_int, [C.c_void_p, C.c_int]),
     "garm_sim_advance_auto": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(StepStats)]),
     "garm_sim_graph_active": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "garm_reinit_plan_set": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int, C.c_int, C.c_int]),
@@ -142,6 +143,9 @@ def load(path: Path | str | None = None) -> C.CDLL:
 def check(status: int, what: str) -> None:
     if status != OK:
         raise GarmError(status, what)
+
+
+RESTART_AUTO, RESTART_NEVER, RESTART_ALWAYS = 0, 1, 2
 
 
 def default_config(**overrides) -> Config:
@@ -253,6 +257,10 @@ class Simulation:
         d = stats.as_dict()
         d["status"] = st
         return d
+
+    def set_restart_override(self, mode: int) -> None:
+        """garm_sim_set_restart_override: RESTART_AUTO, RESTART_NEVER or RESTART_ALWAYS."""
+        check(self.lib.garm_sim_set_restart_override(self.handle, int(mode)), "garm_sim_set_restart_override")
 
     def set_clock(self, frame_rate: int = 25, cfl: float = 1.0) -> None:
         check(self.lib.garm_sim_set_clock(self.handle, int(frame_rate), float(cfl)), "garm_sim_set_clock")

@@ -191,6 +191,15 @@ garm_status garm_sim_collect(garm_sim *sim, garm_step_stats *stats);
  * stream so each owns one).  stats (may be NULL) receives one record per scene.
  * A scene's results do not depend on the batch it runs in. */
 garm_status garm_batch_advance_auto(garm_sim *const *sims, int count, int steps, garm_step_stats *stats);
+/* Restart decision of the following steps (no reference counterpart): GARM_RESTART_AUTO is
+ * checkReferenceMap's test (LevelSetLiquid.cpp:631); NEVER keeps the reference map and ALWAYS
+ * restarts, whatever the test finds.  For experiments that hold one run's restart schedule
+ * fixed in another, e.g. the mixed form on the FP64 form's schedule.  Applies from the next
+ * step enqueued on the simulation's stream, captured step graphs included. */
+#define GARM_RESTART_AUTO 0
+#define GARM_RESTART_NEVER 1
+#define GARM_RESTART_ALWAYS 2
+garm_status garm_sim_set_restart_override(garm_sim *sim, int mode);
 /* 1 when garm_sim_advance_auto replays captured step graphs (no reference counterpart). */
 garm_status garm_sim_graph_active(const garm_sim *sim, int *active);
 /* Launch forms of the WENO5 reinitialisation sub-stages (no reference counterpart):

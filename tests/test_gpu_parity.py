@@ -158,6 +158,31 @@ def test_restart_branch_every_step(oracle_mod, garm_lib):
     assert linf(g.download(capi.FIELD_LEVEL_SET), o.download(capi.FIELD_LEVEL_SET)) <= 1e-6 * dx
 
 
+def test_restart_override(oracle_mod, garm_lib):
+    """garm_sim_set_restart_override: ALWAYS restarts every step, which is what the oracle
+    does with a restart test that always fails (rm_threshold = -1); NEVER keeps the
+    reference map although the test fails; AUTO returns to the test."""
+    sc = scenes.dam_break(3, 16)
+    g, o = pair(oracle_mod, sc, rm_threshold=-1.0)
+    f = capi.Simulation(sc.grid, host_default_config())
+    load_scene(f, sc)
+    for s in (g, o, f):
+        s.initialize()
+        s.stage("restart")
+    f.set_restart_override(capi.RESTART_ALWAYS)
+    dx = sc.grid.spacing
+    for dt in (0.01, 0.01):
+        assert f.advance(dt)["restarted"] == 1
+        o.advance(dt)
+        g.set_restart_override(capi.RESTART_NEVER)
+        assert g.advance(dt)["restarted"] == 0
+        g.set_restart_override(capi.RESTART_AUTO)
+    assert linf(f.download(capi.FIELD_LEVEL_SET), o.download(capi.FIELD_LEVEL_SET)) <= 1e-6 * dx
+    assert g.advance(0.01)["restarted"] == 1
+    with pytest.raises(capi.GarmError):
+        f.set_restart_override(3)
+
+
 def test_n_step_drift(oracle_mod, garm_lib, capsys):
     """Drift of φ, u and ξ after 12 steps with each side choosing its own dt."""
     sc = scenes.dam_break(3, 24)
