@@ -254,7 +254,7 @@ def reinit_roofline(sim, torch, stream, n_cells: int, esz: int, iters: int, peak
         peak, src = 6800.0, "fallback"
     plan = sim.reinit_plan()
     name = {"cells": "kReinitCells", "columns": "kReinitColumns", "sweeps": "kWenoSweep x3",
-            "tiled": "kReinitColumnsTiled (TMA-staged plane tiles)"}[plan["form"]]
+            "tiled": "kReinitColumnsTiled (TMA-staged plane tiles)", "pairs": "kReinitPairs"}[plan["form"]]
     hbm = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "peak_source": src, "unit": "GB/s",
            "frac": round(achieved / peak, 4), "traffic": None, "algorithmic_bytes_per_launch": int(bytes_per_launch)}
     out = {"kernel": f"{name} (WENO5 TVD-RK3 sub-stage)", "plan": plan, **hbm, "ms_per_launch": round(ms_per_launch, 4)}

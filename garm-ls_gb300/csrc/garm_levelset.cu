@@ -605,6 +605,146 @@ __global__ void __launch_bounds__(256) kReinitColumns(G<D, T> g, const T *__rest
 	columnWalk<D, T, Mode>(g, in, base, out, dt, pidx, w0, min(w0 + chunk, g.s[D - 1]), src);
 }
 
+// ---- Pair form (3D FP32): each thread owns two x-adjacent columns (x even and x + 1) and
+// walks them together along z.  Every per-cell quantity of the two cells is the pair of lanes
+// of one float2, so the z face sets, the Godunov terms and the update run as paired
+// instructions.  Of the three x face sets the two cells need (left of x, between x and x + 1,
+// right of x + 1), the outer two are one paired evaluation, the right one with its differences
+// in reverse order: a face set evaluated on reversed differences in the φ⁻ role gives the φ⁺
+// role of the face set itself (the smoothness indicators and the candidate stencils are
+// mirror images).  The shared middle face set is evaluated once and serves φ⁺ of x and φ⁻ of
+// x + 1.  The y axis is the paired cell form on the two columns.  Same formulas as the column
+// form; the FP32 rounding differs where operations are ordered differently.
+constexpr int kPairBlockMax = 256;
+__device__ __forceinline__ F2 ldg2(const float *p) { return {__ldg(reinterpret_cast<const float2 *>(p))}; }
+
+// The φ⁻ role of the face set on (E1..E5), both lanes.
+__device__ __forceinline__ Ratio2 faceRight2(F2 E1, F2 E2, F2 E3, F2 E4, F2 E5) {
+	const F2 Q = maxNonNeg2(maxNonNeg2(maxNonNeg2(mul2(E1, E1), mul2(E2, E2)), maxNonNeg2(mul2(E3, E3), mul2(E4, E4))), mul2(E5, E5));
+	const F2 eps = fma2(Q, f2(WenoConst<float>::epsScale), f2(WenoConst<float>::floorEps4));
+	const FaceWeights2 fw = faceWeights2(smoothL2(smoothG2(E1, E2, E3), E1, E2, E3), smoothM2(smoothG2(E2, E3, E4), E2, E4),
+	                                     smoothR2(smoothG2(E3, E4, E5), E3, E4, E5), eps);
+	return rightRole2(fw, stencil1_2(E1, E2, E3), stencil2_2(E2, E3, E4), stencil3_2(E3, E4, E5));
+}
+
+// godunovSq of the two cells of a pair (one per lane), each with its own sign of φ.
+__device__ __forceinline__ F2 godunovPair(bool negA, bool negB, const Ratio2 &m, const Ratio2 &p) {
+	const F2 a = mul2(m.num, negRecip2(m.den)), b = mul2(p.num, negRecip2(p.den));
+	const F2 x = f2(signBit(m.num.v.x) == negA ? a.v.x : 0.f, signBit(m.num.v.y) == negB ? a.v.y : 0.f);
+	const F2 y = f2(signBit(p.num.v.x) != negA ? b.v.x : 0.f, signBit(p.num.v.y) != negB ? b.v.y : 0.f);
+	return fma2(x, x, mul2(y, y));
+}
+
+// rkUpdate of the two cells of a pair.
+template <int Mode>
+__device__ __forceinline__ float2 rkUpdatePair(F2 f, F2 rawSum, float k, float dx, float dt, const float *base, int64_t id) {
+	const F2 grad = mul2(f2(sqrtf(rawSum.v.x), sqrtf(rawSum.v.y)), f2(k));
+	const F2 sp = mul2(f2(dx), grad);
+	const F2 q = fma2(f, f, mul2(sp, sp));
+	const F2 sgn = mul2(f, f2(rsqrtf(q.v.x), rsqrtf(q.v.y)));
+	const F2 adv = fma2(mul2(f2(dt), sgn), sub2(f2(1.f), grad), f);
+	if (Mode == 0) return adv.v;
+	const F2 b = ldg2(base + id);
+	if (Mode == 1) return mul2(fma2(b, f2(3.f), adv), f2(0.25f)).v;
+	return mul2(fma2(adv, f2(2.f), b), f2(1.f / 3.f)).v;
+}
+
+template <int Mode>
+__global__ void __launch_bounds__(kPairBlockMax) kReinitPairs(G<3, float> g, const float *__restrict__ in, const float *base, float *out, float dt, int chunk) {
+	pdlWait();
+	const int sx = g.s[0], sy = g.s[1], sz = g.s[2];
+	const int hx = sx >> 1;
+	const int q = int(blockIdx.x) * int(blockDim.x) + int(threadIdx.x);
+	if (q >= hx * sy) return;
+	const int w0 = int(blockIdx.y) * chunk;
+	if (w0 >= sz) return;
+	const int w1 = min(w0 + chunk, sz);
+	const int j = q / hx, i = (q - j * hx) * 2;
+	const int64_t plane = int64_t(sx) * sy;
+	const int pidx = i + j * sx;
+	const float *col = in + pidx;
+	const bool innerX = i >= 4 && i + 5 < sx, innerY = j >= 3 && j + 3 < sy;
+	const float k6 = g.inv * (1.0f / 6.0f);
+	const float dx = g.dx;
+	// z window of both columns: v[t] = φ at w0 - 3 + t (clamped)
+	F2 v[7];
+#pragma unroll
+	for (int t = 0; t < 7; t++) v[t] = ldg2(col + int64_t(min(max(w0 - 3 + t, 0), sz - 1)) * plane);
+	Ratio2 mW = faceRight2(sub2(v[1], v[0]), sub2(v[2], v[1]), sub2(v[3], v[2]), sub2(v[4], v[3]), sub2(v[5], v[4]));
+	F2 E1 = sub2(v[2], v[1]), E2 = sub2(v[3], v[2]), E3 = sub2(v[4], v[3]), E4 = sub2(v[5], v[4]), E5 = sub2(v[6], v[5]);
+	F2 S1 = mul2(E1, E1), S2 = mul2(E2, E2), S3 = mul2(E3, E3), S4 = mul2(E4, E4), S5 = mul2(E5, E5);
+	F2 gA = smoothG2(E1, E2, E3), gB = smoothG2(E2, E3, E4);
+	for (int w = w0; w < w1; w++) {
+		const int64_t id = int64_t(w) * plane + pidx;
+		const F2 f = v[3];
+		const bool negA = isNegative(f.v.x), negB = isNegative(f.v.y);
+		// z: the face set above the cell pair (values w-2 .. w+3)
+		const F2 gC = smoothG2(E3, E4, E5);
+		const F2 Q = maxNonNeg2(maxNonNeg2(maxNonNeg2(S1, S2), maxNonNeg2(S3, S4)), S5);
+		const FaceWeights2 fw = faceWeights2(smoothL2(gA, E1, E2, E3), smoothM2(gB, E2, E4), smoothR2(gC, E3, E4, E5),
+		                                     fma2(Q, f2(WenoConst<float>::epsScale), f2(WenoConst<float>::floorEps4)));
+		const Ratio2 pW = leftRole2(fw, stencil1_2(E5, E4, E3), stencil2_2(E4, E3, E2), stencil3_2(E3, E2, E1));
+		const Ratio2 mNext = rightRole2(fw, stencil1_2(E1, E2, E3), stencil2_2(E2, E3, E4), stencil3_2(E3, E4, E5));
+		F2 sum = godunovPair(negA, negB, mW, pW);
+		// x: values x-3 .. x+4 of the row
+		{
+			float u[8];
+			if (innerX) {
+#pragma unroll
+				for (int t = 0; t < 5; t++) {
+					const float2 a = __ldg(reinterpret_cast<const float2 *>(in + id + 2 * t - 4));
+					if (t > 0) u[2 * t - 1] = a.x;
+					if (2 * t < 8) u[2 * t] = a.y;
+				}
+			} else {
+				const float *row = in + (id - i);
+#pragma unroll
+				for (int t = 0; t < 8; t++) u[t] = ldg(row + min(max(i + t - 3, 0), sx - 1));
+			}
+			const float D1 = u[1] - u[0], D2 = u[2] - u[1], D3 = u[3] - u[2], D4 = u[4] - u[3], D5 = u[5] - u[4], D6 = u[6] - u[5], D7 = u[7] - u[6];
+			// outer face sets: lane x on (D1..D5) (φ⁻ of x), lane y on (D7..D3) reversed (φ⁺ of x + 1)
+			const Ratio2 outer = faceRight2(f2(D1, D7), f2(D2, D6), f2(D3, D5), f2(D4, D4), f2(D5, D3));
+			// the middle face set (D2..D6) once; its two roles as the lanes: φ⁺ of x, φ⁻ of x + 1
+			const float M = maxNonNeg(maxNonNeg(maxNonNeg(D2 * D2, D3 * D3), maxNonNeg(D4 * D4, D5 * D5)), D6 * D6);
+			const FaceWeights<float> wm = faceWeights(smoothL(smoothG(D2, D3, D4), D2, D3, D4), smoothM(smoothG(D3, D4, D5), D3, D5),
+			                                          smoothR(smoothG(D4, D5, D6), D4, D5, D6),
+			                                          fma(M, WenoConst<float>::epsScale, WenoConst<float>::floorEps4));
+			const F2 W1 = mul2(f2(0.1f), f2(wm.c, wm.a)), Wb = f2(wm.b), W3 = mul2(f2(0.3f), f2(wm.a, wm.c));
+			const F2 S1m = stencil1_2(f2(D6, D2), f2(D5, D3), f2(D4, D4));
+			const F2 S2m = stencil2_2(f2(D5, D3), f2(D4, D4), f2(D3, D5));
+			const F2 S3m = stencil3_2(f2(D4, D4), f2(D3, D5), f2(D2, D6));
+			const Ratio2 mid = {fma2(W1, S1m, fma2(Wb, S2m, mul2(W3, S3m))), add2(add2(W1, Wb), W3)};
+			const Ratio2 mX = {f2(outer.num.v.x, mid.num.v.y), f2(outer.den.v.x, mid.den.v.y)};
+			const Ratio2 pX = {f2(mid.num.v.x, outer.num.v.y), f2(mid.den.v.x, outer.den.v.y)};
+			sum = add2(sum, godunovPair(negA, negB, mX, pX));
+		}
+		// y: the paired cell form on the two columns
+		{
+			F2 yv[7];
+#pragma unroll
+			for (int t = 0; t < 7; t++) {
+				if (t == 3) { yv[t] = f; continue; }
+				yv[t] = innerY ? ldg2(in + id + int64_t(t - 3) * sx) : ldg2(in + (id - int64_t(j) * sx) + int64_t(min(max(j + t - 3, 0), sy - 1)) * sx);
+			}
+			Ratio2 mY, pY;
+			wenoCell2(yv, mY, pY);
+			sum = add2(sum, godunovPair(negA, negB, mY, pY));
+		}
+		*reinterpret_cast<float2 *>(out + id) = rkUpdatePair<Mode>(f, sum, k6, dx, dt, base, id);
+		// slide the window one cell up
+		if (w + 1 < w1) {
+			const F2 zn = ldg2(col + int64_t(min(w + 4, sz - 1)) * plane);
+#pragma unroll
+			for (int t = 0; t < 6; t++) v[t] = v[t + 1];
+			v[6] = zn;
+			E1 = E2; E2 = E3; E3 = E4; E4 = E5; E5 = sub2(v[6], v[5]);
+			S1 = S2; S2 = S3; S3 = S4; S4 = S5; S5 = mul2(E5, E5);
+			gA = gB; gB = gC;
+			mW = mNext;
+		}
+	}
+}
+
 // ---- Tiled column form (3D FP32): the in-plane stencils of each z-plane read a tile of
 // the plane that the tensor memory accelerator (TMA) stages into shared memory.  A block
 // is a 32 x 4 patch of columns; the tile holds x0-4 .. x0+35 (the start rounded down to a
@@ -879,7 +1019,14 @@ __global__ void __launch_bounds__(256) kWenoSweep(G<D, T> g, const T *__restrict
 // form, the column form or the sweep form, with `block` threads and `chunk`
 // cells per thread.  Chosen by timing (reinitPlanFor) and cached per device
 // and shape.
-enum ReinitForm { kFormCells = GARM_REINIT_CELLS, kFormColumns = GARM_REINIT_COLUMNS, kFormSweeps = GARM_REINIT_SWEEPS, kFormTiled = GARM_REINIT_TILED };
+enum ReinitForm { kFormCells = GARM_REINIT_CELLS, kFormColumns = GARM_REINIT_COLUMNS, kFormSweeps = GARM_REINIT_SWEEPS, kFormTiled = GARM_REINIT_TILED,
+                  kFormPairs = GARM_REINIT_PAIRS };
+
+// The pair form reads and writes float2: rows of even length and 8-byte aligned planes.
+static bool pairsApply(const G<3, float> &g, const void *in, const void *base, const void *out) {
+	const auto a8 = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 7) == 0; };
+	return g.s[0] % 2 == 0 && a8(in) && a8(out) && (!base || a8(base));
+}
 struct ReinitPlan { int form = kFormColumns, block = 128, chunk = 8; float ms = 0; };
 
 template <int D, typename T, int A, int Mode>
@@ -904,6 +1051,12 @@ static int launchReinit(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g,
 		return D;
 	}
 	if constexpr (D == 3 && sizeof(T) == 4) {
+		if (pl.form == kFormPairs && pairsApply(g, in, base, out)) {
+			const int pairs = (g.s[0] / 2) * g.s[1];
+			const dim3 grid((pairs + pl.block - 1) / pl.block, (g.s[2] + pl.chunk - 1) / pl.chunk);
+			launchPdl(kReinitPairs<Mode>, grid, dim3(pl.block), st, g, (const float *)in, (const float *)base, (float *)out, float(dt), pl.chunk);
+			return 1;
+		}
 		CUtensorMap map;
 		if (pl.form == kFormTiled && tiledMap((const float *)in, g, &map)) {
 			const dim3 grid((g.s[0] + kTileX - 1) / kTileX, (g.s[1] + kTileY - 1) / kTileY, (g.s[2] + pl.chunk - 1) / pl.chunk);
@@ -911,7 +1064,7 @@ static int launchReinit(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g,
 			return 1;
 		}
 	}
-	// the column form (also the tiled form where it does not apply)
+	// the column form (also the tiled and pair forms where they do not apply)
 	const int block = pl.form == kFormTiled ? kTileX * kTileY : pl.block;
 	const int plane = g.s[0] * (D == 3 ? g.s[1] : 1);
 	const int sw = g.s[D - 1];
@@ -964,8 +1117,12 @@ static ReinitPlan reinitPlanFor(cudaStream_t st, const G<D, T> &g, const T *phi,
 	colWalks.erase(std::unique(colWalks.begin(), colWalks.end()), colWalks.end());
 	for (int b : {64, 128, 256})
 		for (int c : colWalks) cand.push_back({kFormColumns, b, c});
-	if (D == 3 && sizeof(T) == 4)
+	if (D == 3 && sizeof(T) == 4) {
 		for (int c : {4, 8, 16, 32}) cand.push_back({kFormTiled, kTileX * kTileY, c});
+		if (g.s[0] % 2 == 0)
+			for (int b : {64, 128, 256})
+				for (int c : colWalks) cand.push_back({kFormPairs, b, c});
+	}
 	// sweeps: walks that split the longest axis into 2-8 equal pieces, plus short fixed ones
 	int longest = 0;
 	for (int a = 0; a < D; a++) longest = std::max(longest, g.s[a]);

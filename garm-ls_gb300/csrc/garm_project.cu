@@ -180,8 +180,9 @@ __device__ __forceinline__ float ldcg(const float *p) { return *p; }
 
 // Shared memory of the reductions, in doubles: [0, 48) the warp sums of a block's partials
 // ([v*16 + w], as doubles or float pairs); [96, 98) reciprocals the mixed form keeps
-// across iterations; [kShOut, kShOut + 8) the grid totals broadcast to the block.
-constexpr int kShOut = 104, kShSize = 112;
+// across iterations; [kShOut, kShOut + 8) the grid totals broadcast to the block;
+// [kShStage, kShSize) the grid's partials staged for warp 0 ([v * kStageBlocks + block]).
+constexpr int kShOut = 104, kShStage = 112, kStageBlocks = 256, kShSize = kShStage + 3 * kStageBlocks;
 
 // Block partial sums of NV values → partials[v*maxBlocks + blockIdx], then the block's
 // arrival at the grid barrier.  Warp sums go through shared memory to warp 0, whose lane 0
@@ -222,27 +223,33 @@ __device__ __forceinline__ void blockPartials(double (&acc)[NV], double *partial
 }
 
 // Sum of the gridDim partials of slot v, identical in every block (a fixed partition of
-// the blocks over the lanes of warp 0 and a fixed shuffle tree: deterministic).  Lane l
-// loads the partials of blocks l, l + 32, ..., all NV values together, so the grid's
-// partials arrive in one L2 round trip; lane 0 runs `fin` on the totals (scalar work done
-// once per block) and the NOUT results reach the block through shared memory.  One block
-// barrier; the next writer of the results is this function in a later reduction, which no
-// thread reaches before every thread has read them.
+// the blocks over the lanes of warp 0 and a fixed shuffle tree: deterministic).  Thread t
+// loads the NV partials of block t into shared memory, so the grid's partials arrive in
+// one L2 round trip; warp 0 sums them there (lane l: blocks l, l + 32, ...), lane 0 runs
+// `fin` on the totals (scalar work done once per block) and the NOUT results reach the
+// block through shared memory.  The next writer of the staged partials or of the results
+// is this function in a later reduction, which no thread reaches before every thread has
+// passed the block barriers after it.
 template <int NV, int NOUT, typename Fin>
 __device__ __forceinline__ void gridTotals(const double *partials, int maxBlocks, double (&out)[NOUT], double *sh, Fin fin) {
-	static_assert(NOUT >= NV && NOUT <= 8, "outputs include the sums");
-	const int lane = threadIdx.x & 31;
+	static_assert(NOUT >= NV && NOUT <= 8 && NV <= 3, "outputs include the sums");
+	const int lane = threadIdx.x & 31, nb = gridDim.x;
+	double *stage = sh + kShStage;
+	for (int b = threadIdx.x; b < min(nb, kStageBlocks); b += blockDim.x) {
+		double q[NV];
+#pragma unroll
+		for (int v = 0; v < NV; v++) q[v] = ldcg(partials + v * maxBlocks + b);
+#pragma unroll
+		for (int v = 0; v < NV; v++) stage[v * kStageBlocks + b] = q[v];
+	}
+	__syncthreads();
 	if (threadIdx.x < 32) {
-		const int nb = gridDim.x;
 		double t[NOUT];
 #pragma unroll
 		for (int v = 0; v < NV; v++) t[v] = 0;
 		for (int b = lane; b < nb; b += 32) {
-			double q[NV];
 #pragma unroll
-			for (int v = 0; v < NV; v++) q[v] = ldcg(partials + v * maxBlocks + b);
-#pragma unroll
-			for (int v = 0; v < NV; v++) t[v] += q[v];
+			for (int v = 0; v < NV; v++) t[v] += b < kStageBlocks ? stage[v * kStageBlocks + b] : ldcg(partials + v * maxBlocks + b);
 		}
 #pragma unroll
 		for (int o = 16; o > 0; o >>= 1) {
@@ -561,26 +568,34 @@ __device__ __forceinline__ void blockPartialsDF(DF (&acc)[NV], double *partials,
 		}
 	}
 }
-// Grid totals of NV double-float partials in the arrangement of gridTotals (warp 0 loads
-// every block's partials in one L2 round trip and sums them in a fixed order), widened to
-// FP64 by lane 0, which then runs `fin` on them; the NOUT results are broadcast to the
-// block through shared memory.
+// Grid totals of NV double-float partials in the arrangement of gridTotals (every block's
+// partials staged in shared memory in one L2 round trip, warp 0 summing them in a fixed
+// order), widened to FP64 by lane 0, which then runs `fin` on them; the NOUT results are
+// broadcast to the block through shared memory.
 template <int NV, int NOUT, typename Fin>
 __device__ __forceinline__ void gridTotalsDF(const double *partials, int maxBlocks, double (&out)[NOUT], double *sh, Fin fin) {
-	static_assert(NOUT >= NV && NOUT <= 8, "outputs include the sums");
-	const int lane = threadIdx.x & 31;
+	static_assert(NOUT >= NV && NOUT <= 8 && NV <= 3, "outputs include the sums");
+	const int lane = threadIdx.x & 31, nb = gridDim.x;
+	const float2 *p2 = reinterpret_cast<const float2 *>(partials);
+	float2 *stage = reinterpret_cast<float2 *>(sh + kShStage);
+	for (int b = threadIdx.x; b < min(nb, kStageBlocks); b += blockDim.x) {
+		float2 q[NV];
+#pragma unroll
+		for (int v = 0; v < NV; v++) q[v] = p2[v * maxBlocks + b];  // ordered by the grid barrier, as ldcg
+#pragma unroll
+		for (int v = 0; v < NV; v++) stage[v * kStageBlocks + b] = q[v];
+	}
+	__syncthreads();
 	if (threadIdx.x < 32) {
-		const int nb = gridDim.x;
-		const float2 *p2 = reinterpret_cast<const float2 *>(partials);
 		DF x[NV];
 #pragma unroll
 		for (int v = 0; v < NV; v++) x[v] = DF{0.f, 0.f};
 		for (int b = lane; b < nb; b += 32) {
-			float2 q[NV];
 #pragma unroll
-			for (int v = 0; v < NV; v++) q[v] = p2[v * maxBlocks + b];  // ordered by the grid barrier, as ldcg
-#pragma unroll
-			for (int v = 0; v < NV; v++) x[v] = dfMerge(x[v], DF{q[v].x, q[v].y});
+			for (int v = 0; v < NV; v++) {
+				const float2 q = b < kStageBlocks ? stage[v * kStageBlocks + b] : p2[v * maxBlocks + b];
+				x[v] = dfMerge(x[v], DF{q.x, q.y});
+			}
 		}
 		dfWarpSumN<NV>(x);
 		if (lane == 0) {

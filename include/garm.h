@@ -204,13 +204,16 @@ garm_status garm_sim_set_restart_override(garm_sim *sim, int mode);
 garm_status garm_sim_graph_active(const garm_sim *sim, int *active);
 /* Launch forms of the WENO5 reinitialisation sub-stages (no reference counterpart):
  * one thread per cell; threads walking columns along the last axis; one pass
- * per axis, threads walking lines of that axis; or (3D FP32) columns whose in-plane
+ * per axis, threads walking lines of that axis; (3D FP32) columns whose in-plane
  * stencils read tiles of each plane staged in shared memory by TMA, 128 threads per
- * block (other precisions and shapes run the column form). */
+ * block; or (3D FP32, rows of even length) threads walking two x-adjacent columns
+ * as the two lanes of paired FP32 instructions, sharing the x face set between them
+ * (other precisions and shapes run the column form). */
 #define GARM_REINIT_CELLS 0
 #define GARM_REINIT_COLUMNS 1
 #define GARM_REINIT_SWEEPS 2
 #define GARM_REINIT_TILED 3
+#define GARM_REINIT_PAIRS 4
 /* The launch plan the reinitialisation autotuner chose for this simulation's grid:
  * form, threads per block, cells each thread walks and the timed sub-stage in ms.
  * Plans are tuned once per grid shape, precision and device in the process, on

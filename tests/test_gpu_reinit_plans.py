@@ -1,8 +1,11 @@
 """Every launch plan of the WENO5 reinitialisation (one thread per cell, columns
-along the last axis, one sweep per axis, or columns reading TMA-staged plane tiles,
-with several block sizes and walk lengths) gives the oracle's result, on ragged 2D and 3D shapes whose sizes are
-not multiples of any block or chunk, and for iteration counts that leave the
-result in each of the three rotating planes."""
+along the last axis, one sweep per axis, columns reading TMA-staged plane tiles, or
+pairs of x-adjacent columns walked together, with several block sizes and walk
+lengths) gives the oracle's result, on ragged 2D and 3D shapes whose sizes are not
+multiples of any block or chunk, and for iteration counts that leave the result in
+each of the three rotating planes.  Shapes with rows of odd length run the column
+form in place of the pair form; rows of 6 and 10 cells put every pair, or all but
+one, within reach of the clamped edges."""
 from __future__ import annotations
 
 import numpy as np
@@ -15,7 +18,8 @@ pytestmark = pytest.mark.gpu
 
 PLANS = [("cells", 256, 0), ("columns", 64, 1), ("columns", 64, 4), ("columns", 128, 8), ("columns", 96, 32),
          ("columns", 256, 200), ("sweeps", 32, 1), ("sweeps", 64, 3), ("sweeps", 128, 16), ("sweeps", 256, 64),
-         ("sweeps", 64, 500), ("tiled", 128, 1), ("tiled", 128, 5), ("tiled", 128, 8), ("tiled", 128, 100)]
+         ("sweeps", 64, 500), ("tiled", 128, 1), ("tiled", 128, 5), ("tiled", 128, 8), ("tiled", 128, 100),
+         ("pairs", 32, 1), ("pairs", 64, 8), ("pairs", 128, 5), ("pairs", 256, 200)]
 
 
 def _field(shape, seed):
@@ -35,7 +39,8 @@ def _field(shape, seed):
 
 # (72, 20, 24): rows of 16-byte multiples, so the tiled form stages the planes of its interior
 # blocks by TMA while its edge blocks walk with global loads
-@pytest.mark.parametrize("shape,iters", [((37, 29), 12), ((23, 31, 41), 12), ((45, 6, 9), 7), ((5, 40, 3), 8), ((72, 20, 24), 9)])
+@pytest.mark.parametrize("shape,iters", [((37, 29), 12), ((23, 31, 41), 12), ((45, 6, 9), 7), ((5, 40, 3), 8), ((72, 20, 24), 9),
+                                         ((6, 9, 11), 10), ((10, 13, 17), 11)])
 def test_plans_match_oracle(oracle_mod, garm_lib, shape, iters):
     phi0, dx = _field(shape, seed=len(shape))
     ref = oracle_mod.reinit(phi0, dx, iters, 0.5)
