@@ -843,8 +843,9 @@ def run_garm(args) -> None:
 
 
 def run_reference(args) -> None:
-    """The reference's FP64 CPU path (the oracle port; the reference itself needs Eigen
-    and yaml-cpp, absent here) on the same workload, all host threads."""
+    """The reference's FP64 CPU path on the same workload, all host threads: the oracle port,
+    which gives the same bits as the reference's own code compiled from its sources
+    (tests/test_ref_pin.py); those sources are not on the GPU machine, the port is."""
     rank, _, world = dist_env()
     if rank != 0:
         return
@@ -878,7 +879,9 @@ def run_reference(args) -> None:
         "data": "synthetic",
         "config": dam_config(n, "fp64", world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
-                         "sample": f"{K} full oracle steps of the {n}^3 dam break; warm-up capped at 1 step"},
+                         "sample": f"{K} full oracle steps of the {n}^3 dam break; warm-up capped at 1 step; "
+                                   "the oracle equals the reference's own code bit for bit (2D 128^2, 200 steps)",
+                         "build": O.BUILD_FLAGS},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
