@@ -183,6 +183,7 @@ def state_fields():
 PROFILED_PLANS = {  # (form, precision) -> ncu summary of that WENO5 sub-stage at 128^3
     ("sweeps", "fp64"): "weno_sweeps_fp64_dam_break_128.txt",
     ("columns", "mixed"): "weno_columns_f32_dam_break_128.txt",
+    ("pairs", "mixed"): "weno_pairs_f32_dam_break_128.txt",
 }
 
 
@@ -195,9 +196,13 @@ def profiled_pipe(plan: dict, precision: str, n: int):
         return None
     metric = "sm__inst_executed_pipe_fp64.avg.pct_of_peak_sustained_active" if precision == "fp64" \
         else "smsp__issue_active.avg.pct_of_peak_sustained_active"
-    vals = [float(ln.split()[1]) for ln in p.read_text().splitlines() if ln.startswith(metric)]
+    text = p.read_text().splitlines()
+    vals = [float(ln.split()[1]) for ln in text if ln.startswith(metric)]
     if not vals:
-        return None
+        frac = [float(ln.split(":")[1]) for ln in text if ln.startswith("issue_active_frac:")]
+        if not frac:
+            return None
+        vals = [100 * frac[0]]
     return {"pipe": "fp64" if precision == "fp64" else "issue", "metric": metric,
             "frac": round(sum(vals) / len(vals) / 100, 3), "source": f"profiles/{name}"}
 
