@@ -64,7 +64,8 @@ def parse():
     p.add_argument("--dim", type=int, default=3, help="drift: 2 or 3")
     p.add_argument("--spread", action="store_true",
                    help="drift: also run the oracle from an initial state changed by one ulp and report its own "
-                        "deviation at the same steps (the reference algorithm's conditioning)")
+                        "deviation at the same steps (the reference algorithm's conditioning); drop: the same with "
+                        "the FP64 GPU form")
     p.add_argument("--batch-scenes", type=int, default=48)
     p.add_argument("--batch-cg-cells", type=int, default=None,
                    help="batch: interior cells per pressure-solve block (default: the measured best)")
@@ -431,10 +432,20 @@ def run_drop(args, torch, stream, world: int, W: int, K: int) -> dict:
     # mixed_fixed: the mixed form held to the FP64 form's restart schedule
     # (garm_sim_set_restart_override before each step), which separates the drift of the
     # fields from the restart decisions that the two roundings may take differently
-    for name, prec in (("fp64", capi.PRECISION_FP64), ("mixed", capi.PRECISION_MIXED), ("mixed_fixed", capi.PRECISION_MIXED)):
+    # fp64_ulp: the FP64 form started from a state one or two ulps away (every value scaled by
+    # 1 + U(-1e-15, 1e-15)), the algorithm's own spread to read the mixed form's errors against
+    forms = [("fp64", capi.PRECISION_FP64), ("mixed", capi.PRECISION_MIXED), ("mixed_fixed", capi.PRECISION_MIXED)]
+    if args.spread:
+        forms.append(("fp64_ulp", capi.PRECISION_FP64))
+    for name, prec in forms:
         s = capi.Simulation(sc.grid, capi.default_config(precision=prec), stream=stream.cuda_stream)
-        s.upload(capi.FIELD_LEVEL_SET, sc.phi.ravel())
-        s.upload(capi.FIELD_VELOCITY, sc.velocity)
+        phi0, u0 = sc.phi.ravel(), sc.velocity
+        if name == "fp64_ulp":
+            rng = np.random.default_rng(11)
+            phi0 = phi0 * (1 + 1e-15 * rng.uniform(-1, 1, phi0.shape))
+            u0 = u0 * (1 + 1e-15 * rng.uniform(-1, 1, u0.shape))
+        s.upload(capi.FIELD_LEVEL_SET, phi0)
+        s.upload(capi.FIELD_VELOCITY, u0)
         s.initialize()
         s.stage("restart")
         sims[name] = s
@@ -443,7 +454,7 @@ def run_drop(args, torch, stream, world: int, W: int, K: int) -> dict:
     cg = {k: [] for k in sims}
     launches = {k: 0 for k in sims}
     restarts = {k: 0 for k in sims}
-    errors, errors_fixed = {}, {}
+    errors, errors_fixed, errors_ulp = {}, {}, {}
     last_fp64_restart = 0
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(world)
@@ -468,6 +479,8 @@ def run_drop(args, torch, stream, world: int, W: int, K: int) -> dict:
         if step in marks:
             errors[str(step)] = field_errors(sims["mixed"], sims["fp64"], dx)
             errors_fixed[str(step)] = field_errors(sims["mixed_fixed"], sims["fp64"], dx)
+            if "fp64_ulp" in sims:
+                errors_ulp[str(step)] = field_errors(sims["fp64_ulp"], sims["fp64"], dx)
     clk = clocks.stop()
     timed = max(K - W, 1)
     legs = {}
@@ -487,6 +500,8 @@ def run_drop(args, torch, stream, world: int, W: int, K: int) -> dict:
             "drop": {"fp64": legs["fp64"], "mixed": legs["mixed"],
                      "mixed_on_fp64_restart_schedule": {"restarts": legs["mixed_fixed"]["restarts"],
                                                         "errors_vs_fp64": errors_fixed},
+                     "fp64_one_ulp_away": ({"restarts": legs["fp64_ulp"]["restarts"], "errors_vs_fp64": errors_ulp}
+                                           if "fp64_ulp" in legs else None),
                      "speedup_vs_fp64": legs["mixed"]["value"] / legs["fp64"]["value"],
                      "sphere": {"center": [float(c) for c in sc.meta["center"]], "radius": sc.meta["radius"]},
                      "errors_mixed_vs_fp64": errors}}
