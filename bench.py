@@ -198,12 +198,20 @@ def profiled_pipe(plan: dict, precision: str, n: int):
     metric = "sm__inst_executed_pipe_fp64.avg.pct_of_peak_sustained_active" if precision == "fp64" \
         else "smsp__issue_active.avg.pct_of_peak_sustained_active"
     text = p.read_text().splitlines()
-    vals = [float(ln.split()[1]) for ln in text if ln.startswith(metric)]
-    if not vals:
-        frac = [float(ln.split(":")[1]) for ln in text if ln.startswith("issue_active_frac:")]
-        if not frac:
-            return None
+    frac = [float(ln.split(":")[1]) for ln in text if ln.startswith("issue_active_frac:")]
+    if frac and precision != "fp64":
         vals = [100 * frac[0]]
+    else:
+        vals = []
+        for ln in text:
+            parts = ln.split()
+            if ln.startswith(metric) and len(parts) > 1:
+                try:
+                    vals.append(float(parts[1]))
+                except ValueError:
+                    pass
+    if not vals:
+        return None
     return {"pipe": "fp64" if precision == "fp64" else "issue", "metric": metric,
             "frac": round(sum(vals) / len(vals) / 100, 3), "source": f"profiles/{name}"}
 

@@ -52,3 +52,16 @@ def test_planted_differences_are_found(oracle_mod):
     assert np.isclose(e["phi_rms_dx"], 0.25 / np.sqrt(phi.size), rtol=1e-9)
     assert np.isclose(e["xi_linf_dx"], 0.5, rtol=1e-9)
     assert e["u_linf_rel_fluid_faces"] == 0.0
+
+
+def test_profiles_named_by_the_bench_parse():
+    """Every ncu summary the bench reads for its roofline (bench.PROFILED_PLANS) yields the
+    compute fraction and the DRAM traffic per launch, and the FP64 one its operation count."""
+    for (form, precision) in bench.PROFILED_PLANS:
+        plan = {"form": form}
+        pipe = bench.profiled_pipe(plan, precision, 128)
+        assert pipe is not None and 0 < pipe["frac"] <= 1, (form, precision)
+        traffic = bench.profiled_traffic(plan, precision, 128)
+        assert traffic is not None and traffic > 0, (form, precision)
+    ops = bench.profiled_fp64_ops({"form": "sweeps"})
+    assert ops is not None and 100 < ops < 1000
