@@ -54,18 +54,14 @@ def parse():
     p.add_argument("--no-default-build", action="store_true",
                    help="skip the same workload in the reference's default build (Newton restart + fast marching)")
     p.add_argument("--seed", type=int, default=0, help="drop: seed of the sphere's centre")
-    p.add_argument("--workload", choices=["dam", "batch", "serve", "drop", "reinit", "drift"], default="dam",
+    p.add_argument("--workload", choices=["dam", "batch", "serve", "drop", "reinit"], default="dam",
                    help="dam: the 128^3 dam break (default line, with mixed and batch sub-objects); "
                         "batch: 48 uneven pool scenes only; serve: the Poisson request stream only; "
                         "drop: the 256^3 drop into a pool, mixed against FP64 over K steps with per-field errors; "
-                        "reinit: the dam break's reinitialisation stage alone, K times after W (for profiling one kernel); "
-                        "drift: the FP64 form against the CPU oracle over K steps of the dam break (--dim 2 or 3), "
-                        "per-field differences and volumes at steps 1, 10, 50 and K")
-    p.add_argument("--dim", type=int, default=3, help="drift: 2 or 3")
+                        "reinit: the dam break's reinitialisation stage alone, K times after W (for profiling one kernel)")
     p.add_argument("--spread", action="store_true",
-                   help="drift: also run the oracle from an initial state changed by one ulp and report its own "
-                        "deviation at the same steps (the reference algorithm's conditioning); drop: the same with "
-                        "the FP64 GPU form")
+                   help="drop: also run the FP64 form from an initial state changed by one ulp and report its "
+                        "deviation at the same steps (the algorithm's own conditioning)")
     p.add_argument("--batch-scenes", type=int, default=48)
     p.add_argument("--batch-cg-cells", type=int, default=None,
                    help="batch: interior cells per pressure-solve block (default: the measured best)")
@@ -515,60 +511,6 @@ def run_drop(args, torch, stream, world: int, W: int, K: int) -> dict:
                      "errors_mixed_vs_fp64": errors}}
 
 
-def run_drift(args, torch) -> dict:
-    """The plain FP64 form and the CPU oracle (a bit-exact port of the reference's FP64 path,
-    tests/test_ref_pin.py) advance the same dam break with one dt sequence (the Simulator's
-    CFL-1 policy on the GPU's velocity) for K steps; per-field differences at steps 1, 10, 50
-    and K, and the volume diagnostic of both at every step."""
-    from garm import capi, scenes
-    from oracle import oracle as O
-    sc = scenes.dam_break(args.dim, args.n)
-    dx = sc.grid.spacing
-    g = capi.Simulation(sc.grid, capi.default_config(precision=capi.PRECISION_FP64, record_volume=1))
-    o = O.OracleSim(sc.grid, g.cfg)
-    sims = [g, o]
-    q = None
-    if args.spread:
-        import numpy as np
-        q = O.OracleSim(sc.grid, g.cfg)
-        sims.append(q)
-    for s in sims:
-        phi0, u0 = sc.phi.ravel(), sc.velocity
-        if s is q:  # every value scaled by 1 + U(-1e-15, 1e-15): one or two ulps
-            rng = np.random.default_rng(11)
-            phi0 = phi0 * (1 + 1e-15 * rng.uniform(-1, 1, phi0.shape))
-            u0 = u0 * (1 + 1e-15 * rng.uniform(-1, 1, u0.shape))
-        s.upload(capi.FIELD_LEVEL_SET, phi0)
-        s.upload(capi.FIELD_VELOCITY, u0)
-        s.initialize()
-        s.stage("restart")
-    K = args.steps
-    marks = {m for m in (1, 10, 50, K) if 1 <= m <= K}
-    rows, vg, vo, rg, ro = {}, [], [], 0, 0
-    t_cpu = 0.0
-    for k, dt in enumerate(scenes.frame_time_steps(g.max_speed, K, 25, 1.0, dx), 1):
-        sg = g.advance(dt)
-        t0 = time.perf_counter()
-        so = o.advance(dt)
-        t_cpu += time.perf_counter() - t0
-        if q is not None:
-            q.advance(dt)
-        rg += sg["restarted"]
-        ro += so["restarted"]
-        vg.append(sg["volume"])
-        vo.append(o.volume())
-        if k in marks:
-            rows[str(k)] = {"restarts_gpu": rg, "restarts_oracle": ro, **field_errors(g, o, dx),
-                            "volume_rel_diff": abs(vg[-1] - vo[-1]) / abs(vo[-1])}
-            if q is not None:
-                rows[str(k)]["oracle_ulp_spread"] = field_errors(q, o, dx)
-    for s in sims:
-        s.close()
-    return {"workload": f"{args.dim}D dam break {args.n}^{args.dim}, plain FP64 GPU form against the CPU oracle, {K} steps",
-            "drift": rows, "volume_drift_gpu": (vg[-1] - vg[0]) / vg[0], "volume_drift_oracle": (vo[-1] - vo[0]) / vo[0],
-            "cpu_s_per_step": t_cpu / K}
-
-
 def run_garm(args) -> None:
     import numpy as np
     import torch
@@ -596,13 +538,6 @@ def run_garm(args) -> None:
         if world > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
-        return
-    if args.workload == "drift":
-        sub = run_drift(args, torch)
-        if rank == 0:
-            print(json.dumps({"metric": METRIC, "value": None, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
-                              "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                              "data": "synthetic", "config": {"workload": sub.pop("workload"), "n": n}, **sub}), flush=True)
         return
     if args.workload in ("batch", "serve"):
         clocks = Clocks(local)
