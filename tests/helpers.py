@@ -231,7 +231,12 @@ def conditioning_parity(gpu, base, spread, scale, tight: float = 1e-9) -> dict:
     }
 
 
-def assert_conditioning_parity(stats: dict, tight: float = 1e-9, share_slack: float = 0.03, q_factor: float = 10.0) -> None:
+def assert_conditioning_parity(stats: dict, tight: float = 1e-9, share_slack: float = 0.03, q_factor: float = 2.5) -> None:
+    """The GPU's deviation from the oracle within the oracle's own spread under ulp changes:
+    the share of elements agreeing to `tight` at most `share_slack` below the oracle's, and
+    the 99th percentile and the maximum at most q_factor times the oracle's.  Measured on
+    GB300 the largest ratio is 1.6 (the 99th percentile, fast-marching steps on the 3D dam
+    break); 2.5 leaves room for the few perturbations the spread is estimated from."""
     assert stats["agree_gpu"] >= stats["agree_oracle"] - share_slack, stats
     assert stats["q99_gpu"] <= max(q_factor * stats["q99_oracle"], tight), stats
     assert stats["max_gpu"] <= max(q_factor * stats["max_oracle"], tight), stats
