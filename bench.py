@@ -65,6 +65,8 @@ def parse():
     p.add_argument("--batch-scenes", type=int, default=48)
     p.add_argument("--batch-cg-cells", type=int, default=None,
                    help="batch: interior cells per pressure-solve block (default: the measured best)")
+    p.add_argument("--batch-streams", type=int, default=None,
+                   help="batch: streams the scenes share, round robin (default: one per scene)")
     p.add_argument("--reinit-plan", default=None, metavar="FORM,THREADS,CELLS",
                    help="pin the reinitialisation launch plan of the dam-break grid instead of autotuning it")
     p.add_argument("--requests", type=int, default=48, help="serve: number of requests")
@@ -362,9 +364,10 @@ def run_batch(args, torch, world: int, W: int, K: int) -> dict:
     # each scene's pressure solve takes one SM per 131072 interior cells (2-32 SMs here), so the
     # solves of different scenes run side by side instead of each taking the whole GPU
     cfg.cg_cells_per_block = args.batch_cg_cells or BATCH_CG_CELLS_PER_BLOCK
-    streams = [torch.cuda.Stream() for _ in scs]
+    streams = [torch.cuda.Stream() for _ in range(min(args.batch_streams or len(scs), len(scs)))]
     sims = []
-    for sc, st in zip(scs, streams):
+    for i, sc in enumerate(scs):
+        st = streams[i % len(streams)]
         sim = capi.Simulation(sc.grid, cfg, stream=st.cuda_stream)
         sim.upload(capi.FIELD_LEVEL_SET, sc.phi.ravel())
         sim.upload(capi.FIELD_VELOCITY, sc.velocity)
@@ -425,7 +428,7 @@ def run_batch(args, torch, world: int, W: int, K: int) -> dict:
             "speedup_vs_sequential": value / seq_value,
             "interior_cells": cells, "sizes": sorted({int(round(sc.interior_cells ** (1 / 3))) for sc in scs}),
             "resident_bytes": resident, "graph_replay": graphs, "gpu_launches": launches,
-            "cg_cells_per_block": cfg.cg_cells_per_block,
+            "cg_cells_per_block": cfg.cg_cells_per_block, "streams": len(streams),
             "p50_scene_step_ms": float(np.percentile(per_step, 50)), "p99_scene_step_ms": float(np.percentile(per_step, 99)),
             "dtype": "f32 storage+math, f64 dots/residual/refinement/RM test",
             "workload": f"{len(scs)} pool scenes, n uniform in {{64,96,128,160}}, 1-3 spheres, mixed, "

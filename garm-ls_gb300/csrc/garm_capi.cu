@@ -149,6 +149,8 @@ garm_status allocState(State &s) {
 	GARM_TRY(dalloc(s, &s.scanBlock, size_t(gridFor(s.N)) * 4 + 64));
 	GARM_TRY(dalloc(s, &s.nUnknownsDev, 64));
 	GARM_TRY(dalloc(s, &s.ent64, N * 16 * 2 * D));
+	GARM_TRY(dalloc(s, &s.rowHdr, N * 4));
+	GARM_TRY(dalloc(s, &s.rowIdx, N * 4 * (2 * D - 2)));
 	GARM_TRY(dalloc(s, &s.diag, N * 8));
 	GARM_TRY(dalloc(s, &s.invd, N * 8));
 	GARM_TRY(dalloc(s, &s.rhs, N * 8));

@@ -85,6 +85,43 @@ __global__ void __launch_bounds__(kBlock) kScatterUnknowns(int64_t N, const int 
 struct __align__(16) NbW64 { int nb; int pad; double w; };
 struct __align__(8) NbW32 { int nb; float w; };
 
+// Compact rows, read by the solves whose unknowns outnumber what they hold on chip (those
+// stream every row from memory in every iteration).  hdr bit q (q < 2D): entry q present;
+// bit 8 + q: its weight is exactly 1.  The neighbours of the x entries (q = 0, 1) are the
+// unknowns i - 1 and i + 1: unknowns are numbered in cell order, x fastest, so a present x
+// neighbour is the adjacent unknown.  idx holds the neighbour ids of the y and z entries
+// ([i][q - 2]); a row with a weight other than 1 reads its weights from the full rows.
+// 20 bytes a row in 3D (12 in 2D) instead of 48 (FP32 weights) or 96 (FP64).
+template <int NB> struct RowIdx;
+template <> struct RowIdx<4> { using T = int2; };
+template <> struct RowIdx<6> { using T = int4; };
+template <int NB> struct RowC { unsigned h; typename RowIdx<NB>::T q; };
+template <int NB>
+__device__ __forceinline__ RowC<NB> loadRow(const unsigned *hdr, const int *idx, int64_t i) {
+	return RowC<NB>{hdr[i], reinterpret_cast<const typename RowIdx<NB>::T *>(idx)[i]};
+}
+// The entries of unknown i as {neighbour (-1: none), weight} (E: NbW32 or NbW64), decoded
+// with selects; only a row with a weight other than 1 loads (all of) its weights.
+template <int NB, typename E>
+__device__ __forceinline__ void decodeRow(const RowC<NB> &r, int64_t i, const E *ent, int64_t S, E (&e)[NB]) {
+	int far[NB - 2];
+	far[0] = r.q.x; far[1] = r.q.y;
+	if constexpr (NB == 6) { far[2] = r.q.z; far[3] = r.q.w; }
+	constexpr unsigned all = (1u << NB) - 1;
+#pragma unroll
+	for (int k = 0; k < NB; k++) {
+		e[k] = E{};
+		const int nb = k == 0 ? int(i - 1) : k == 1 ? int(i + 1) : far[k < 2 ? 0 : k - 2];
+		e[k].nb = (r.h >> k & 1u) ? nb : -1;
+		e[k].w = 1;
+	}
+	if ((r.h >> 8 & all) != (r.h & all)) {
+#pragma unroll
+		for (int k = 0; k < NB; k++)
+			if (r.h >> k & 1u) e[k].w = ent[k * S + i].w;
+	}
+}
+
 // ---------------------------------------------------------------------------
 // rows of the ghost-fluid Poisson matrix
 // ---------------------------------------------------------------------------
@@ -99,6 +136,8 @@ struct BuildIO {
 	double *diag, *invd, *rhs;
 	NbW32 *ent32;
 	float *diag32, *invd32;
+	unsigned *hdr;
+	int *idx;
 	int64_t stride;
 };
 
@@ -112,6 +151,8 @@ __global__ void __launch_bounds__(kBlock) kBuildSystem(Geom geom, BuildIO<D, T> 
 	int i, j, k; cg.coord(id, i, j, k);
 	const double pc = double(io.phi[id]);
 	double dg = 0, div = 0;
+	unsigned hdr = 0;
+	int far[2 * D - 2];
 #pragma unroll
 	for (int q = 0; q < 2 * D; q++) {
 		const int a = q >> 1, o = q & 1;
@@ -136,7 +177,12 @@ __global__ void __launch_bounds__(kBlock) kBuildSystem(Geom geom, BuildIO<D, T> 
 		if (w < 1) div += side * (1 - w) * double(io.bv[a][fid]);
 		io.ent[q * io.stride + r] = NbW64{nb, 0, wt};
 		if (io.ent32) io.ent32[q * io.stride + r] = NbW32{nb, float(wt)};
+		if (nb >= 0) hdr |= (1u << q) | (wt == 1 ? 1u << (8 + q) : 0u);
+		if (q >= 2) far[q - 2] = nb;
 	}
+	io.hdr[r] = hdr;
+#pragma unroll
+	for (int q = 0; q < 2 * D - 2; q++) io.idx[int64_t(r) * (2 * D - 2) + q] = far[q];
 	io.rhs[r] = div;
 	io.diag[r] = dg;
 	io.invd[r] = dg != 0 ? 1 / dg : 1;  // Eigen DiagonalPreconditioner
@@ -152,6 +198,8 @@ struct CgArgs {
 	const double *diag, *invd;
 	const NbW32 *ent32;
 	const float *diag32, *invd32;
+	const unsigned *hdr;  // compact rows (see decodeRow)
+	const int *idx;
 	int64_t stride;
 	const double *b;
 	double *x;       // FP64 solution (pressure)
@@ -433,13 +481,13 @@ __device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, NbW64 *enS, unsi
 			}
 		} else {
 			for (int64_t i = tid; i < n; i += nthr) {
+				E e[NB];
+				decodeRow<NB>(loadRow<NB>(a.hdr, a.idx, i), i, ent, S, e);
 				const V uni = uG[i];
 				V wni = dg[i] * uni;
 #pragma unroll
-				for (int k = 0; k < NB; k++) {
-					const E e = ent[k * S + i];
-					if (e.nb >= 0) wni = fma(-e.w, uG[e.nb], wni);
-				}
+				for (int k = 0; k < NB; k++)
+					if (e[k].nb >= 0) wni = fma(-e[k].w, uG[e[k].nb], wni);
 				const V rni = st[i].r;
 				st[i].w = wni;
 				g = fma(rni, uni, g);
@@ -772,17 +820,19 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 					V p0 = p32[i], x0 = x32[i], p1 = p32[j], x1 = x32[j];
 					const V d0 = dg[i], d1 = dg[j];
 					E e0[NB], e1[NB];
-#pragma unroll
-					for (int k = 0; k < NB; k++) { e0[k] = ent[k * S + i]; e1[k] = ent[k * S + j]; }
+					decodeRow<NB>(loadRow<NB>(a.hdr, a.idx, i), i, ent, S, e0);
+					decodeRow<NB>(loadRow<NB>(a.hdr, a.idx, j), j, ent, S, e1);
 					update(m0, d0, p0, x0, [&](int k) { return e0[k]; }, m0, p0, x0);
 					update(m1, d1, p1, x1, [&](int k) { return e1[k]; }, m1, p1, x1);
 					sn[i] = m0; p32[i] = p0; x32[i] = x0;
 					sn[j] = m1; p32[j] = p1; x32[j] = x1;
 				}
 				if (i < n) {
+					E e0[NB];
+					decodeRow<NB>(loadRow<NB>(a.hdr, a.idx, i), i, ent, S, e0);
 					Pack<V> m = sc[i];
 					V pv = p32[i], xv = x32[i];
-					update(m, dg[i], pv, xv, [&](int k) { return ent[k * S + i]; }, m, pv, xv);
+					update(m, dg[i], pv, xv, [&](int k) { return e0[k]; }, m, pv, xv);
 					sn[i] = m; p32[i] = pv; x32[i] = xv;
 				}
 			}
@@ -1001,6 +1051,7 @@ garm_status projectAsync(State &s, bool record) {
 	bio.grid2mat = s.grid2mat;
 	bio.ent = (NbW64 *)s.ent64; bio.diag = s.diag; bio.invd = s.invd; bio.rhs = s.rhs;
 	bio.ent32 = s.mixed ? (NbW32 *)s.ent32 : nullptr; bio.diag32 = s.mixed ? s.diag32 : nullptr; bio.invd32 = s.mixed ? s.invd32 : nullptr;
+	bio.hdr = s.rowHdr; bio.idx = s.rowIdx;
 	bio.stride = s.N;
 	kBuildSystem<D, T><<<nbC, kBlock, 0, s.stream>>>(s.geom, bio); s.launches++;
 	GARM_CHECK_LAUNCH();
@@ -1009,6 +1060,7 @@ garm_status projectAsync(State &s, bool record) {
 	a.nDev = s.nUnknownsDev;
 	a.ent = (const NbW64 *)s.ent64; a.diag = s.diag; a.invd = s.invd;
 	a.ent32 = (const NbW32 *)s.ent32; a.diag32 = s.diag32; a.invd32 = s.invd32;
+	a.hdr = s.rowHdr; a.idx = s.rowIdx;
 	a.stride = s.N;
 	a.b = s.rhs;
 	a.x = s.pres;
