@@ -341,7 +341,7 @@ def stage_ms(sim, dx: float, steps: int = 3) -> dict:
     return {name: round(statistics.median(r[i] for r in rows), 4) for i, name in enumerate(capi.STAGE_NAMES)}
 
 
-BATCH_CG_CELLS_PER_BLOCK = 131072  # measured best for the 48-scene batch (32768: 212M, 65536: 219M, 131072: 226M, 262144: 211M cell-steps/s)
+BATCH_CG_CELLS_PER_BLOCK = 131072  # measured best for the 48-scene batch (65536: 268M, 131072: 277M, 262144: 257M cell-steps/s)
 
 
 def batch_scenes(count: int, seed: int = 0):

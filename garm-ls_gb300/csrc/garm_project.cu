@@ -480,9 +480,15 @@ __device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, NbW64 *enS, unsi
 				rr = fma(me[c].r, me[c].r, rr);
 			}
 		} else {
+			// each row is loaded one unknown ahead, so that the neighbour gathers issue
+			// together with the unknown's own loads
+			RowC<NB> q{};
+			if (tid < n) q = loadRow<NB>(a.hdr, a.idx, tid);
 			for (int64_t i = tid; i < n; i += nthr) {
+				const RowC<NB> row = q;
+				if (i + nthr < n) q = loadRow<NB>(a.hdr, a.idx, i + nthr);
 				E e[NB];
-				decodeRow<NB>(loadRow<NB>(a.hdr, a.idx, i), i, ent, S, e);
+				decodeRow<NB>(row, i, ent, S, e);
 				const V uni = uG[i];
 				V wni = dg[i] * uni;
 #pragma unroll
