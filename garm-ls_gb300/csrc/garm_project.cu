@@ -577,6 +577,40 @@ __device__ __forceinline__ DF dfMerge(DF a, DF b) {
 	const float hi = __fadd_rn(s.hi, lo);
 	return {hi, __fsub_rn(lo, __fsub_rn(hi, s.hi))};
 }
+// Scalar double-float arithmetic for the mixed solve's recurrences (β, α and the kept
+// 1/γ, 1/(γα)), so that they run on the FP32 pipe: at GB300's FP64 issue rate the
+// lane that forms them spent about 1 us per iteration on a chain of some 30 FP64
+// instructions.  Products follow Dekker's algorithm with the exact FMA product error; the
+// reciprocal is the correctly rounded FP32 reciprocal refined by one Newton–Raphson step
+// on the double-float value (Joldes, Muller & Popescu, "Tight and rigorous error bounds
+// for basic building blocks of double-word arithmetic", ACM TOMS 44, 2017).  Relative
+// error about 2^-44, the accuracy of the double-float dot products they are formed from.
+__device__ __forceinline__ DF dfQuick(float hi, float lo) {  // renormalise (|hi| >= |lo|)
+	const float s = __fadd_rn(hi, lo);
+	return {s, __fsub_rn(lo, __fsub_rn(s, hi))};
+}
+__device__ __forceinline__ DF dfMul(DF a, DF b) {
+	const float p = __fmul_rn(a.hi, b.hi);
+	float e = fmaf(a.hi, b.hi, -p);
+	e = fmaf(a.hi, b.lo, e);
+	e = fmaf(a.lo, b.hi, e);
+	return dfQuick(p, e);
+}
+__device__ __forceinline__ DF dfNeg(DF a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ DF dfRecip(DF b) {
+	const float y = __frcp_rn(b.hi);
+	const float r = fmaf(-b.lo, y, fmaf(-b.hi, y, 1.0f));  // 1 - b·y
+	return dfQuick(y, __fmul_rn(y, r));
+}
+// a < b for normalised double-floats
+__device__ __forceinline__ bool dfLess(DF a, DF b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ DF dfFromDouble(double x) { const float hi = float(x); return {hi, float(x - double(hi))}; }
+__device__ __forceinline__ double dfToDouble(DF a) { return double(a.hi) + double(a.lo); }
+// A double-float carried in the bits of one double: broadcast through shared memory and
+// kept across iterations without FP64 instructions.
+__device__ __forceinline__ double dfPack(DF a) { return __hiloint2double(__float_as_int(a.hi), __float_as_int(a.lo)); }
+__device__ __forceinline__ DF dfUnpack(double p) { return {__int_as_float(__double2hiint(p)), __int_as_float(__double2loint(p))}; }
+
 __device__ __forceinline__ DF dfWarpSum(DF v) {
 #pragma unroll
 	for (int o = 16; o > 0; o >>= 1) v = dfMerge(v, DF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)});
@@ -622,41 +656,39 @@ __device__ __forceinline__ void blockPartialsDF(DF (&acc)[NV], double *partials,
 		}
 	}
 }
-// Grid totals of NV double-float partials in the arrangement of gridTotals (every block's
-// partials staged in shared memory in one L2 round trip, warp 0 summing them in a fixed
-// order), widened to FP64 by lane 0, which then runs `fin` on them; the NOUT results are
-// broadcast to the block through shared memory.
+// Grid totals of NV double-float partials for the mixed solve's iterations, without the
+// widening to FP64: warp 0 loads every block's partials itself, lane l those of blocks
+// l, l + 32, ... all at once (one L2 round trip, no staging), and sums them in that fixed
+// order and a fixed shuffle tree; lane 0 hands the NV totals to
+// fin(const DF *totals, double *out), which fills the NOUT words broadcast to the block
+// through shared memory.
 template <int NV, int NOUT, typename Fin>
-__device__ __forceinline__ void gridTotalsDF(const double *partials, int maxBlocks, double (&out)[NOUT], double *sh, Fin fin) {
-	static_assert(NOUT >= NV && NOUT <= 8 && NV <= 3, "outputs include the sums");
+__device__ __forceinline__ void gridTotalsDFRaw(const double *partials, int maxBlocks, double (&out)[NOUT], double *sh, Fin fin) {
+	static_assert(NOUT <= 8 && NV <= 3, "broadcast words");
 	const int lane = threadIdx.x & 31, nb = gridDim.x;
-	const float2 *p2 = reinterpret_cast<const float2 *>(partials);
-	float2 *stage = reinterpret_cast<float2 *>(sh + kShStage);
-	for (int b = threadIdx.x; b < min(nb, kStageBlocks); b += blockDim.x) {
-		float2 q[NV];
-#pragma unroll
-		for (int v = 0; v < NV; v++) q[v] = p2[v * maxBlocks + b];  // ordered by the grid barrier, as ldcg
-#pragma unroll
-		for (int v = 0; v < NV; v++) stage[v * kStageBlocks + b] = q[v];
-	}
-	__syncthreads();
+	const float2 *p2 = reinterpret_cast<const float2 *>(partials);  // ordered by the grid barrier, as ldcg
 	if (threadIdx.x < 32) {
 		DF x[NV];
 #pragma unroll
 		for (int v = 0; v < NV; v++) x[v] = DF{0.f, 0.f};
-		for (int b = lane; b < nb; b += 32) {
+		constexpr int U = 5;  // 160 blocks in one round trip
+		float2 q[U][NV];
 #pragma unroll
-			for (int v = 0; v < NV; v++) {
-				const float2 q = b < kStageBlocks ? stage[v * kStageBlocks + b] : p2[v * maxBlocks + b];
-				x[v] = dfMerge(x[v], DF{q.x, q.y});
-			}
+		for (int u = 0; u < U; u++)
+#pragma unroll
+			for (int v = 0; v < NV; v++) q[u][v] = lane + 32 * u < nb ? p2[v * maxBlocks + lane + 32 * u] : make_float2(0.f, 0.f);
+#pragma unroll
+		for (int u = 0; u < U; u++)
+#pragma unroll
+			for (int v = 0; v < NV; v++) x[v] = dfMerge(x[v], DF{q[u][v].x, q[u][v].y});
+		for (int b = lane + 32 * U; b < nb; b += 32) {
+#pragma unroll
+			for (int v = 0; v < NV; v++) { const float2 r = p2[v * maxBlocks + b]; x[v] = dfMerge(x[v], DF{r.x, r.y}); }
 		}
 		dfWarpSumN<NV>(x);
 		if (lane == 0) {
 			double t[NOUT];
-#pragma unroll
-			for (int v = 0; v < NV; v++) t[v] = double(x[v].hi) + double(x[v].lo);
-			fin(t);
+			fin(x, t);
 #pragma unroll
 			for (int v = 0; v < NOUT; v++) sh[kShOut + v] = t[v];
 		}
@@ -678,8 +710,8 @@ __device__ __forceinline__ double unitScale(double sumSq, int n) {
 // phase per iteration: each thread updates its own unknowns and recomputes, from
 // last iteration's packed {r, w, s} of its neighbours, their new u with the owner's
 // fma/mul sequence, so bit-identically, which gives w = A u without a second
-// barrier; the packed state is double-buffered.  FP32 vectors and element arithmetic, double-float dot products widened to FP64 per
-// block, FP64 scalars) with FP64 residual replacement (van der Vorst & Ye,
+// barrier; the packed state is double-buffered.  FP32 vectors and element arithmetic,
+// double-float dot products and scalar recurrences) with FP64 residual replacement (van der Vorst & Ye,
 // "Residual replacement strategies for Krylov subspace iterative methods",
 // SIAM J. Sci. Comput. 22, 2000, as used by reliable-update mixed-precision CG).
 // The FP32 iterates x32 are a scaled correction to the FP64 solution x64.
@@ -742,17 +774,21 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 		blockPartialsDF<2>(acc, a.partials, a.maxBlocks, sh, a.bar, epoch);
 	}
 	if (!gridWait(a.bar, a.err, epoch)) return;
-	// tot: γ, δ, |r|^2, β, α, the replacement decision, FP32 β and α packed.  The lane
-	// that finishes the totals also keeps 1/γ and 1/(γα) for the next iteration's β and α
-	// in sh[96], sh[97], which no reduction touches.
-	double tot[7];
-	gridTotalsDF<2, 7>(a.partials, a.maxBlocks, tot, sh, [sh](double *t) {
-		t[2] = 0; t[3] = 0; t[4] = t[0] / t[1]; t[5] = 0; t[6] = packFloats(t[3], t[4]);
-		sh[96] = 1.0 / t[0]; sh[97] = sh[96] / t[4];
+	// tot, broadcast as bits: γ and α as double-floats, the replacement decision (non-zero:
+	// replace), the FP32 β and α packed.  The lane that finishes the totals also keeps 1/γ
+	// and 1/(γα), as double-floats, for the next iteration's β and α in sh[96], sh[97],
+	// which no reduction touches.
+	double tot[4];
+	gridTotalsDFRaw<2, 4>(a.partials, a.maxBlocks, tot, sh, [sh](const DF *x, double *t) {
+		const DF ig = dfRecip(x[0]), al = dfMul(x[0], dfRecip(x[1]));
+		t[0] = dfPack(x[0]); t[1] = dfPack(al); t[2] = 0; t[3] = dfPack(DF{0.f, al.hi});
+		sh[96] = dfPack(ig); sh[97] = dfPack(dfMul(ig, dfRecip(al)));
 	});
 	const double drop2 = a.drop * a.drop;
 	const int maxIter = a.maxIter, replaceEvery = a.replaceEvery;
-	double gamma = tot[0], lastTrue = b2;
+	double gamma = tot[0], lastTrue = b2;  // gamma: γ as a packed double-float
+	// replaced once |r|^2 of the scaled system falls below max(drop^2 |r_true|^2, threshold)·s^2
+	DF limit = dfFromDouble(fmax(drop2 * lastTrue, threshold) * (scale * scale));
 	int cur = 0, it = 0, lastReplace = 0;
 	// on-chip copies (used when every thread owns at most kRegUnknowns unknowns)
 	// the register form's matrix rows, in shared memory [slot][entry][thread]
@@ -781,8 +817,8 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 	}
 	while (it < a.maxIter) {
 		// ---- one fused C-G iteration ----
-		const double alpha = tot[4];
-		const V bV = packedHi(tot[6]), aV = packedLo(tot[6]);
+		const double alphaPacked = tot[1];
+		const V bV = packedHi(tot[3]), aV = packedLo(tot[3]);
 		{
 			const Pack<V> *__restrict__ sc = stb[cur];
 			Pack<V> *__restrict__ sn = stb[cur ^ 1];
@@ -847,30 +883,31 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 		}
 		// β = γ/γ_old and α = γ/den, den = δ - βγ/α_old = δ - γ²/(γ_old α_old), from the
 		// kept 1/γ_old and 1/(γ_old α_old).  One reciprocal, of q = γ·den, gives α = γ²/q
-		// and the next pair: 1/γ = den/q and 1/(γα) = den/γ².  It is the Newton–Raphson
-		// reciprocal from an FP32 seed (2 ulp), a plain division outside its range.  The same
-		// lane decides whether the residual is replaced after this iteration.
-		const double gOld = gamma;
+		// and the next pair: 1/γ = den/q and 1/(γα) = den/γ², all in double-float
+		// arithmetic.  The same lane decides whether the residual is replaced after this
+		// iteration.
+		const double gOldPacked = gamma;
 		if (!gridWait(a.bar, a.err, epoch)) break;
 		const int itNext = it + 1;
-		gridTotalsDF<3, 7>(a.partials, a.maxBlocks, tot, sh, [=](double *t) {
-			const double g = t[0];
-			t[3] = g * sh[96];
-			const double den = fma(-g * g, sh[97], t[1]);
-			const double q = g * den;
-			const double rq = recipRange(q) ? recipPos(q) : 1.0 / q;
-			t[4] = (g * g) * rq;
-			const double invG = den * rq;
-			sh[96] = invG;
-			sh[97] = (invG * invG) * den;
-			const double s2 = scale * scale;
+		gridTotalsDFRaw<3, 4>(a.partials, a.maxBlocks, tot, sh, [=](const DF *x, double *t) {
+			const DF g = x[0];
+			const DF beta = dfMul(g, dfUnpack(sh[96]));
+			const DF gg = dfMul(g, g);
+			const DF den = dfMerge(x[1], dfNeg(dfMul(gg, dfUnpack(sh[97]))));
+			const DF rq = dfRecip(dfMul(g, den));
+			const DF al = dfMul(gg, rq);
+			const DF invG = dfMul(den, rq);
+			sh[96] = dfPack(invG);
+			sh[97] = dfPack(dfMul(dfMul(invG, invG), den));
 			const bool due = replaceEvery > 0 && itNext - lastReplace >= replaceEvery;
-			t[5] = (t[2] < drop2 * lastTrue * s2 || t[2] < threshold * s2 || itNext >= maxIter || due) ? 1.0 : 0.0;
-			t[6] = packFloats(t[3], t[4]);
+			t[0] = dfPack(g);
+			t[1] = dfPack(al);
+			t[2] = (dfLess(x[2], limit) || itNext >= maxIter || due) ? 1.0 : 0.0;
+			t[3] = dfPack(DF{beta.hi, al.hi});  // packedHi: β, packedLo: α
 		});
 		it = itNext;
 		gamma = tot[0];
-		if (!flagSet(tot[5])) continue;
+		if (!flagSet(tot[2])) continue;
 		lastReplace = it;
 
 		// ---- residual replacement ----
@@ -912,6 +949,7 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 		const V ratio = V(newScale / scale);  // a power of two
 		const double ratio2 = (newScale / scale) * (newScale / scale);
 		scale = newScale;
+		limit = dfFromDouble(fmax(drop2 * lastTrue, threshold) * (scale * scale));
 		{
 			const Pack<V> *__restrict__ sc = stb[cur];
 			Pack<V> *__restrict__ sn = stb[cur ^ 1];
@@ -948,13 +986,17 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 			blockPartialsDF<2>(acc, a.partials, a.maxBlocks, sh, a.bar, epoch);
 		}
 		if (!gridWait(a.bar, a.err, epoch)) break;
-		gridTotalsDF<2, 7>(a.partials, a.maxBlocks, tot, sh, [gOld, ratio2, alpha, sh](double *t) {
+		gridTotalsDFRaw<2, 4>(a.partials, a.maxBlocks, tot, sh, [gOldPacked, ratio2, alphaPacked, sh](const DF *x, double *t) {
+			// β and α after a replacement in FP64 (a few times per solve)
+			const double g = dfToDouble(x[0]), d = dfToDouble(x[1]);
+			const double beta = g / (dfToDouble(dfUnpack(gOldPacked)) * ratio2);
+			const double al = g / (d - beta * g / dfToDouble(dfUnpack(alphaPacked)));
+			t[0] = dfPack(x[0]);
+			t[1] = dfPack(dfFromDouble(al));
 			t[2] = 0;
-			t[3] = t[0] / (gOld * ratio2);
-			t[4] = t[0] / (t[1] - t[3] * t[0] / alpha);
-			t[5] = 0;
-			t[6] = packFloats(t[3], t[4]);
-			sh[96] = 1.0 / t[0]; sh[97] = sh[96] / t[4];
+			t[3] = packFloats(beta, al);
+			sh[96] = dfPack(dfFromDouble(1.0 / g));
+			sh[97] = dfPack(dfFromDouble(1.0 / (g * al)));
 		});
 		gamma = tot[0];
 	}
