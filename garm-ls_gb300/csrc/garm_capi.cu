@@ -150,7 +150,7 @@ garm_status allocState(State &s) {
 	GARM_TRY(dalloc(s, &s.nUnknownsDev, 64));
 	GARM_TRY(dalloc(s, &s.ent64, N * 16 * 2 * D));
 	GARM_TRY(dalloc(s, &s.rowHdr, N * 4));
-	GARM_TRY(dalloc(s, &s.rowIdx, N * 4 * (2 * D - 2)));
+	GARM_TRY(dalloc(s, &s.rowIdx, N * 4 * (D == 3 ? 2 : 1)));
 	GARM_TRY(dalloc(s, &s.diag, N * 8));
 	GARM_TRY(dalloc(s, &s.invd, N * 8));
 	GARM_TRY(dalloc(s, &s.rhs, N * 8));

@@ -80,8 +80,8 @@ struct State {
 	int nUnknowns = 0;
 	void *ent64 = nullptr;      // [2D][N] {neighbour unknown id (-1: none), weight w}, matrix entry -w (FP64)
 	void *ent32 = nullptr;      // the same entries with FP32 weights (mixed)
-	unsigned *rowHdr = nullptr; // compact rows of the streamed solves: [N] presence/unit-weight bits,
-	int *rowIdx = nullptr;      // [N][2D-2] neighbour ids of the y and z entries
+	unsigned *rowHdr = nullptr; // compact rows of the streamed solves: [N] presence bits, full-row flag, y distances
+	int *rowIdx = nullptr;      // [N][2] neighbour ids of the z entries (3D)
 	double *diag = nullptr, *invd = nullptr, *rhs = nullptr, *pres = nullptr;
 	float *diag32 = nullptr, *invd32 = nullptr;
 	// PCG work vectors: packed {r, w, s, 1/diag} per unknown (double-buffered, in the

@@ -86,39 +86,40 @@ struct __align__(16) NbW64 { int nb; int pad; double w; };
 struct __align__(8) NbW32 { int nb; float w; };
 
 // Compact rows, read by the solves whose unknowns outnumber what they hold on chip (those
-// stream every row from memory in every iteration).  hdr bit q (q < 2D): entry q present;
-// bit 8 + q: its weight is exactly 1.  The neighbours of the x entries (q = 0, 1) are the
-// unknowns i - 1 and i + 1: unknowns are numbered in cell order, x fastest, so a present x
-// neighbour is the adjacent unknown.  idx holds the neighbour ids of the y and z entries
-// ([i][q - 2]); a row with a weight other than 1 reads its weights from the full rows.
-// 20 bytes a row in 3D (12 in 2D) instead of 48 (FP32 weights) or 96 (FP64).
-template <int NB> struct RowIdx;
-template <> struct RowIdx<4> { using T = int2; };
-template <> struct RowIdx<6> { using T = int4; };
-template <int NB> struct RowC { unsigned h; typename RowIdx<NB>::T q; };
+// stream every row from memory in every iteration).  Unknowns are numbered in cell order,
+// x fastest, so the neighbours of the x entries (q = 0, 1) are the unknowns i - 1 and
+// i + 1, and a y neighbour lies at most one row of cells (sx) away.  The header word:
+//   bits 0..2D-1   entry q present
+//   bit 7          take this row's entries (neighbour and weight) from the full rows: some
+//                  weight is not exactly 1, or a y distance does not fit 12 bits
+//   bits 8..19     i minus the y- neighbour's id
+//   bits 20..31    the y+ neighbour's id minus i
+// idx holds the z neighbours' ids ([i][q - 4], 3D only).  12 bytes a row in 3D (4 in 2D)
+// instead of 48 (FP32 weights) or 96 (FP64).
+constexpr unsigned kRowFull = 1u << 7;
+constexpr int kRowDeltaMax = 4095;
+template <int NB> struct RowC { unsigned h; int2 z; };
 template <int NB>
 __device__ __forceinline__ RowC<NB> loadRow(const unsigned *hdr, const int *idx, int64_t i) {
-	return RowC<NB>{hdr[i], reinterpret_cast<const typename RowIdx<NB>::T *>(idx)[i]};
+	if constexpr (NB == 6) return RowC<NB>{hdr[i], reinterpret_cast<const int2 *>(idx)[i]};
+	else return RowC<NB>{hdr[i], make_int2(-1, -1)};
 }
 // The entries of unknown i as {neighbour (-1: none), weight} (E: NbW32 or NbW64), decoded
-// with selects; only a row with a weight other than 1 loads (all of) its weights.
+// with selects; only a row flagged full loads its entries.
 template <int NB, typename E>
 __device__ __forceinline__ void decodeRow(const RowC<NB> &r, int64_t i, const E *ent, int64_t S, E (&e)[NB]) {
-	int far[NB - 2];
-	far[0] = r.q.x; far[1] = r.q.y;
-	if constexpr (NB == 6) { far[2] = r.q.z; far[3] = r.q.w; }
-	constexpr unsigned all = (1u << NB) - 1;
+	const int ii = int(i);
+	const int nbs[6] = {ii - 1, ii + 1, ii - int(r.h >> 8 & 0xfffu), ii + int(r.h >> 20), r.z.x, r.z.y};
 #pragma unroll
 	for (int k = 0; k < NB; k++) {
 		e[k] = E{};
-		const int nb = k == 0 ? int(i - 1) : k == 1 ? int(i + 1) : far[k < 2 ? 0 : k - 2];
-		e[k].nb = (r.h >> k & 1u) ? nb : -1;
+		e[k].nb = (r.h >> k & 1u) ? nbs[k] : -1;
 		e[k].w = 1;
 	}
-	if ((r.h >> 8 & all) != (r.h & all)) {
+	if (r.h & kRowFull) {
 #pragma unroll
 		for (int k = 0; k < NB; k++)
-			if (r.h >> k & 1u) e[k].w = ent[k * S + i].w;
+			if (r.h >> k & 1u) { const E f = ent[k * S + i]; e[k].nb = f.nb; e[k].w = f.w; }
 	}
 }
 
@@ -152,7 +153,7 @@ __global__ void __launch_bounds__(kBlock) kBuildSystem(Geom geom, BuildIO<D, T> 
 	const double pc = double(io.phi[id]);
 	double dg = 0, div = 0;
 	unsigned hdr = 0;
-	int far[2 * D - 2];
+	int zid[2] = {-1, -1};
 #pragma unroll
 	for (int q = 0; q < 2 * D; q++) {
 		const int a = q >> 1, o = q & 1;
@@ -177,12 +178,19 @@ __global__ void __launch_bounds__(kBlock) kBuildSystem(Geom geom, BuildIO<D, T> 
 		if (w < 1) div += side * (1 - w) * double(io.bv[a][fid]);
 		io.ent[q * io.stride + r] = NbW64{nb, 0, wt};
 		if (io.ent32) io.ent32[q * io.stride + r] = NbW32{nb, float(wt)};
-		if (nb >= 0) hdr |= (1u << q) | (wt == 1 ? 1u << (8 + q) : 0u);
-		if (q >= 2) far[q - 2] = nb;
+		if (nb >= 0) {
+			hdr |= 1u << q;
+			if (wt != 1) hdr |= kRowFull;
+			if (q == 2 || q == 3) {
+				const int dist = q == 2 ? r - nb : nb - r;
+				if (dist >= 1 && dist <= kRowDeltaMax) hdr |= unsigned(dist) << (q == 2 ? 8 : 20);
+				else hdr |= kRowFull;
+			}
+		}
+		if (q >= 4) zid[q - 4] = nb;
 	}
 	io.hdr[r] = hdr;
-#pragma unroll
-	for (int q = 0; q < 2 * D - 2; q++) io.idx[int64_t(r) * (2 * D - 2) + q] = far[q];
+	if (D == 3) { io.idx[int64_t(r) * 2] = zid[0]; io.idx[int64_t(r) * 2 + 1] = zid[1]; }
 	io.rhs[r] = div;
 	io.diag[r] = dg;
 	io.invd[r] = dg != 0 ? 1 / dg : 1;  // Eigen DiagonalPreconditioner
@@ -731,8 +739,8 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 	const int64_t tid = int64_t(blockIdx.x) * blockDim.x + threadIdx.x, nthr = int64_t(gridDim.x) * blockDim.x;
 	const int64_t S = a.stride;
 	const E *__restrict__ ent = a.ent32;
-	const V *__restrict__ dg = a.diag32;
 	const V *__restrict__ invd = a.invd32;
+	const V *__restrict__ dg = a.diag32;
 	Pack<V> *stb[2] = {(Pack<V> *)a.pack32[0], (Pack<V> *)a.pack32[1]};
 	V *__restrict__ x32 = a.e32;
 	V *__restrict__ p32 = a.p32;
@@ -803,8 +811,8 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 			own[c] = i < n;
 			pp[c] = V(0); xx[c] = V(0);
 			if (own[c]) {
-				dgi[c] = dg[i];
 				me[c] = stb[0][i];
+				dgi[c] = dg[i];
 #pragma unroll
 				for (int k = 0; k < NB; k++) en(c, k) = ent[k * S + i];
 			} else {
@@ -978,7 +986,8 @@ __device__ void pcgMixedReplace(const CgArgs &a, int n, double *sh, NbW32 *enS, 
 					}
 			} else {
 				for (int64_t i = tid; i < n; i += nthr) {
-					sn[i] = rebuild(i, sc[i], dg[i], [&](int k) { return ent[k * S + i]; });
+					const Pack<V> m = sc[i];
+					sn[i] = rebuild(i, m, dg[i], [&](int k) { return ent[k * S + i]; });
 					p32[i] *= ratio;
 				}
 			}
