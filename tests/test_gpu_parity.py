@@ -380,3 +380,29 @@ def test_pressure_solve_block_layouts(oracle_mod, garm_lib, precision):
         assert rel(pg, po) <= tol, f"{per_block}: pressure rel err {rel(pg, po):.3e}"
         pressures.append(pg)
     assert rel(pressures[0], pressures[2]) <= tol
+
+
+@pytest.mark.parametrize("precision", [capi.PRECISION_FP64, capi.PRECISION_MIXED])
+def test_pressure_solve_rows_longer_than_compact_reach(oracle_mod, garm_lib, precision):
+    """The streamed solve's compact rows hold the y neighbours as distances of at most 4095
+    unknowns; longer rows take their entries from the full rows.  A 2D grid of 4600 x 8
+    interior cells whose liquid (x < 0.95) puts about 4370 unknowns in each row, solved on
+    one block (the streamed form), matches the oracle's pressure."""
+    nx, ny = 4600, 8
+    dx = 1.0 / nx
+    grid = capi.grid_desc(2, [nx + 4, ny + 4], dx, [0.5, ny * dx / 2], 2)
+    pos = scenes.cell_positions(grid)
+    phi = scenes.box_sdf(pos, [-1.0, -1.0], [1.95, 2.0])
+    sc = scenes.Scene("wide_rows_2d", grid, np.ascontiguousarray(phi), scenes.zero_velocity(grid))
+    cfg = dict(precision=precision, cg_cells_per_block=10 ** 9)
+    g, o = pair(oracle_mod, sc, **cfg)
+    for s in (g, o):
+        s.initialize()
+        s.stage("body_force", 1e-3)
+    so, sg = o.stage("project"), g.stage("project")
+    assert sg["status"] == capi.OK and sg["unknowns"] == so["unknowns"] > 4 * 512
+    assert sg["cg_residual"] <= 1e-8
+    tol = 1e-5 if precision == capi.PRECISION_FP64 else 1e-4
+    err = rel(g.download(capi.FIELD_PRESSURE), o.download(capi.FIELD_PRESSURE))
+    print(f"\n[rows of ~{so['unknowns'] // ny} unknowns, precision {precision}] pressure rel err {err:.2e}, {sg['cg_iterations']} it")
+    assert err <= tol
