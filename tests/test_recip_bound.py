@@ -51,8 +51,8 @@ def test_reciprocal_within_two_ulp():
 
 
 def test_reciprocal_over_the_pressure_solve_range():
-    """The same reciprocal forms the mixed pressure solve's step sizes from γ·(p·Ap), which
-    it accepts anywhere in [2^-124, 2^125) and otherwise divides."""
+    """The same bound over the reciprocal's whole accepted range, [2^-124, 2^125) (its
+    callers divide outside it)."""
     rng = random.Random(9)
     worst = 0.0
     for n in range(2000):
