@@ -54,8 +54,9 @@ def parse():
     p.add_argument("--no-default-build", action="store_true",
                    help="skip the same workload in the reference's default build (Newton restart + fast marching)")
     p.add_argument("--seed", type=int, default=0, help="drop: seed of the sphere's centre")
-    p.add_argument("--workload", choices=["dam", "batch", "serve", "drop", "reinit"], default="dam",
+    p.add_argument("--workload", choices=["dam", "dam2d", "batch", "serve", "drop", "reinit"], default="dam",
                    help="dam: the 128^3 dam break (default line, with mixed and batch sub-objects); "
+                        "dam2d: the 2D dam break on a 128^2 grid, FP64 and mixed, with the CPU oracle beside them; "
                         "batch: 48 uneven pool scenes only; serve: the Poisson request stream only; "
                         "drop: the 256^3 drop into a pool, mixed against FP64 over K steps with per-field errors; "
                         "reinit: the dam break's reinitialisation stage alone, K times after W (for profiling one kernel)")
@@ -539,6 +540,68 @@ def run_drop(args, torch, stream, world: int, W: int, K: int) -> dict:
                      "errors_mixed_vs_fp64": errors}}
 
 
+def run_dam2d(args, torch, stream, world: int, W: int, K: int) -> dict:
+    """The 2D dam break {x < 0.4, y < 0.6} on an n^2 MAC grid (the reference's CPU-runnable
+    workload), plain FP64 and mixed, K device-resident steps each after W (graph replay, dt
+    on the device), timed with CUDA events; beside them the CPU oracle (the reference's FP64
+    path, bit-identical to it) on the same K steps with all host threads."""
+    from garm import capi, scenes
+    n = args.n
+    sc = scenes.dam_break(2, n)
+    dx = sc.grid.spacing
+    legs = {}
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    launches = 0
+    for name, prec in (("fp64", capi.PRECISION_FP64), ("mixed", capi.PRECISION_MIXED)):
+        s = capi.Simulation(sc.grid, capi.default_config(precision=prec), stream=stream.cuda_stream)
+        s.upload(capi.FIELD_LEVEL_SET, sc.phi.ravel())
+        s.upload(capi.FIELD_VELOCITY, sc.velocity)
+        s.initialize()
+        s.stage("restart")
+        s.set_clock(25, 1.0)
+        s.advance_auto(W)
+        barrier(world)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = s.launch_count()
+        e0.record(stream)
+        st = s.advance_auto(K)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = reduce_max(e0.elapsed_time(e1), world)
+        if name == "fp64":
+            launches = s.launch_count() - l0
+        legs[name] = {"value": world * n * n * K / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / K,
+                      "cg_iterations_last_step": st["cg_iterations"], "graph_replay": s.graph_active()}
+        s.close()
+    clk = clocks.stop()
+    legs["mixed"]["speedup_vs_fp64"] = legs["mixed"]["value"] / legs["fp64"]["value"]
+    out = {"value": legs["fp64"]["value"], "ms_per_step": legs["fp64"]["ms_per_step"], "clocks": clk,
+           "gpu_launches": launches, "mixed": legs["mixed"],
+           "workload": f"2D dam break {n}^2 MAC grid, plain FP64 form, {K} steps after {W}"}
+    if int(os.environ.get("RANK", 0)) == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        sys.path.insert(0, str(REPO / "tests"))
+        from helpers import host_default_config, load_scene
+        o = O.OracleSim(sc.grid, host_default_config())
+        load_scene(o, sc)
+        o.initialize()
+        o.stage("restart")
+        gen = scenes.frame_time_steps(o.max_speed, W + K, 25, 1.0, dx)
+        for _ in range(W):
+            o.advance(next(gen))
+        t0 = time.perf_counter()
+        for _ in range(K):
+            o.advance(next(gen))
+        secs = time.perf_counter() - t0
+        o.close()
+        out["cpu_baseline"] = {"value": n * n * K / secs, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+                               "sample": f"{K} oracle steps of the {n}^2 dam break after {W} ({secs:.2f} s)",
+                               "build": O.BUILD_FLAGS}
+    return out
+
+
 def run_garm(args) -> None:
     import numpy as np
     import torch
@@ -563,6 +626,23 @@ def run_garm(args) -> None:
                                          "l2": "no flush: device state larger than L2"},
                               "clocks": sub["clocks"], "gpu_launches": sub["gpu_launches"], "drop": sub["drop"]}),
                   flush=True)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    if args.workload == "dam2d":
+        sub = run_dam2d(args, torch, stream, world, W, K)
+        if rank == 0:
+            line = {"metric": METRIC, "value": sub["value"], "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+                    "ms_per_step": sub["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                    "dtype": "f64", "data": "synthetic",
+                    "config": {"workload": sub["workload"], "n": n, "dim": 2, "cfl": 1.0, "frame_rate": 25,
+                               "reinit": "WENO5 x30 every step", "pcg_tol": 1e-08, "replicas": world,
+                               "l2": "no flush: the 2D state fits in L2; each step re-reads it"},
+                    "clocks": sub["clocks"], "gpu_launches": sub["gpu_launches"], "mixed": sub["mixed"]}
+            if "cpu_baseline" in sub:
+                line["cpu_baseline"] = sub["cpu_baseline"]
+            print(json.dumps(line), flush=True)
         if world > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
