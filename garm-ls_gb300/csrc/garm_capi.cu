@@ -884,7 +884,7 @@ garm_status garm_reinit_plan_set(int dim, int precision, const int *size, int fo
 	if ((dim != 2 && dim != 3) || !size || (precision != GARM_PRECISION_FP64 && precision != GARM_PRECISION_MIXED)) return GARM_INVALID;
 	for (int a = 0; a < dim; a++) if (size[a] <= 0) return GARM_INVALID;
 	if (form != GARM_REINIT_CELLS && form != GARM_REINIT_COLUMNS && form != GARM_REINIT_SWEEPS && form != GARM_REINIT_TILED &&
-	    form != GARM_REINIT_PAIRS) return GARM_INVALID;
+	    form != GARM_REINIT_PAIRS && form != GARM_REINIT_PAIRS_TILED) return GARM_INVALID;
 	if (threads != 0 && form != GARM_REINIT_CELLS) {
 		if (cells_per_thread < 1) return GARM_INVALID;
 		if (threads < 32 || threads > 256 || threads % 32 != 0) return GARM_INVALID;

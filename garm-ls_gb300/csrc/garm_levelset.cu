@@ -857,16 +857,202 @@ __global__ void __launch_bounds__(kTileX * kTileY) kReinitColumnsTiled(const __g
 	columnWalk<3, float, Mode>(g, in, base, out, dt, (x0 + tx) + (y0 + ty) * sx, w0, w1, src);
 }
 
+// ---- Tiled pair form (3D FP32): the pair form with the in-plane stencils read from a tile of
+// each z-plane staged in shared memory by the tensor memory accelerator.  A block is 16 pairs
+// (32 cells) by 8 rows of columns; its tile holds x0-4 .. x0+35 (the start on a 16-byte
+// boundary, as TMA requires) and y0-3 .. y0+10 of one plane.  The block walks `chunk`
+// planes through a ring of four slots.  Each slot has two mbarriers: `full` completes when
+// the plane's bytes have landed (one elected thread arms it and issues the copy), `empty`
+// when every warp of the block has passed the plane (one arrival per warp).  Thread 0 refills
+// the slot of the plane before the one its warp has just finished, so up to three planes are
+// staged ahead and no warp waits at a block-wide barrier.  Stencil positions are clamped to
+// the grid (clamp-to-edge) before they are looked up in the tile: the clamped position
+// always lies inside the tile, so the zero fill TMA writes beyond the grid's edges is never
+// read.  Every wait is bounded (kTileWaitNs): past it the block sets the error flag, thread 0
+// waits (again bounded) for the copies it issued, and the block returns.
+constexpr int kPtX = 16, kPtY = 8, kPtSlots = 4;
+constexpr int kPtRow = 2 * kPtX + 8, kPtRows = kPtY + 6;
+constexpr int kPtBytes = kPtRow * kPtRows * 4;
+constexpr int kPtStride = (kPtBytes + 127) / 128 * 128;
+
+// Bounded wait on one phase of an mbarrier in shared memory; false after kTileWaitNs.
+__device__ __forceinline__ bool mbarWait(unsigned bar, unsigned parity) {
+	unsigned done = 0;
+	unsigned long long start = 0;
+	for (unsigned it = 0;; it++) {
+		asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+		             : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+		if (done) return true;
+		if ((it & 255u) == 0) {
+			const unsigned long long now = globalNs();
+			if (start == 0) start = now;
+			else if (now - start > kTileWaitNs) return false;
+		}
+	}
+}
+
+template <int Mode>
+__global__ void __launch_bounds__(kPtX * kPtY, 4) kReinitPairsTiled(const __grid_constant__ CUtensorMap map, G<3, float> g, const float *__restrict__ in,
+                                                                    const float *base, float *out, float dt, int chunk, int *err) {
+	pdlWait();
+	__shared__ __align__(128) unsigned char ring[kPtSlots * kPtStride];
+	__shared__ __align__(8) unsigned long long fullBar[kPtSlots], emptyBar[kPtSlots];
+	const int sx = g.s[0], sy = g.s[1], sz = g.s[2];
+	const int tpx = int(threadIdx.x) % kPtX, ty = int(threadIdx.x) / kPtX;
+	const int x0 = int(blockIdx.x) * (2 * kPtX), y0 = int(blockIdx.y) * kPtY;
+	const int w0 = int(blockIdx.z) * chunk;
+	if (w0 >= sz) return;  // the whole block
+	const int w1 = min(w0 + chunk, sz);
+	const int i = x0 + 2 * tpx, j = y0 + ty;
+	const bool active = i < sx && j < sy;  // rows have even length, so i + 1 < sx too
+	const int64_t plane = int64_t(sx) * sy;
+	const int pidx = min(i, sx - 2) + min(j, sy - 1) * sx;  // inactive threads walk a valid column they do not store
+	const float *col = in + pidx;
+	const bool innerX = i >= 4 && i + 5 < sx, innerY = j >= 3 && j + 3 < sy;
+	const int lxi = i - x0 + 4, lyj = j - y0 + 3;  // the thread's own cell in tile coordinates
+	const float k6 = g.inv * (1.0f / 6.0f);
+	const float dx = g.dx;
+	const unsigned ringBase = smemAddr(ring);
+	if (threadIdx.x == 0) {
+		for (int q = 0; q < kPtSlots; q++) {
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smemAddr(fullBar + q)) : "memory");
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smemAddr(emptyBar + q)), "r"(int(blockDim.x) / 32) : "memory");
+		}
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+		asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+	}
+	__syncthreads();
+	auto issue = [&](int w) {  // thread 0
+		const int slot = (w - w0) % kPtSlots;
+		const unsigned bar = smemAddr(fullBar + slot), dst = ringBase + slot * kPtStride;
+		asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(kPtBytes) : "memory");
+		asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+		             :: "r"(dst), "l"(reinterpret_cast<unsigned long long>(&map)), "r"(x0 - 4), "r"(y0 - 3), "r"(w), "r"(bar) : "memory");
+	};
+	int issued = min(w1, w0 + kPtSlots);  // planes [w0, issued) have been requested
+	if (threadIdx.x == 0)
+		for (int w = w0; w < issued; w++) issue(w);
+	// Gives up: flag the error; thread 0 waits (bounded) for the planes it requested and has
+	// not seen land, so that no copy is left writing into the shared memory of a block that
+	// has returned.
+	auto giveUp = [&](int consumed) {
+		atomicExch(err, 1);
+		if (threadIdx.x == 0)
+			for (int w = consumed; w < issued; w++) mbarWait(smemAddr(fullBar + (w - w0) % kPtSlots), unsigned((w - w0) / kPtSlots) & 1u);
+	};
+	// z window of both columns: v[t] = φ at w0 - 3 + t (clamped)
+	F2 v[7];
+#pragma unroll
+	for (int t = 0; t < 7; t++) v[t] = ldg2(col + int64_t(min(max(w0 - 3 + t, 0), sz - 1)) * plane);
+	Ratio2 mW = faceRight2(sub2(v[1], v[0]), sub2(v[2], v[1]), sub2(v[3], v[2]), sub2(v[4], v[3]), sub2(v[5], v[4]));
+	F2 E1 = sub2(v[2], v[1]), E2 = sub2(v[3], v[2]), E3 = sub2(v[4], v[3]), E4 = sub2(v[5], v[4]), E5 = sub2(v[6], v[5]);
+	F2 S1 = mul2(E1, E1), S2 = mul2(E2, E2), S3 = mul2(E3, E3), S4 = mul2(E4, E4), S5 = mul2(E5, E5);
+	F2 gA = smoothG2(E1, E2, E3), gB = smoothG2(E2, E3, E4);
+	for (int w = w0; w < w1; w++) {
+		const int slot = (w - w0) % kPtSlots;
+		// the warp waits together and gives up together (a warp-uniform decision keeps every lane
+		// at the __syncwarp below)
+		if (!__all_sync(0xffffffffu, mbarWait(smemAddr(fullBar + slot), unsigned((w - w0) / kPtSlots) & 1u))) { giveUp(w); return; }
+		const float *tile = reinterpret_cast<const float *>(ring + slot * kPtStride);
+		const int64_t id = int64_t(w) * plane + pidx;
+		const F2 f = v[3];
+		const bool negA = isNegative(f.v.x), negB = isNegative(f.v.y);
+		// z: the face set above the cell pair (values w-2 .. w+3)
+		const F2 gC = smoothG2(E3, E4, E5);
+		const F2 Q = maxNonNeg2(maxNonNeg2(maxNonNeg2(S1, S2), maxNonNeg2(S3, S4)), S5);
+		const FaceWeights2 fw = faceWeights2(smoothL2(gA, E1, E2, E3), smoothM2(gB, E2, E4), smoothR2(gC, E3, E4, E5),
+		                                     fma2(Q, f2(WenoConst<float>::epsScale), f2(WenoConst<float>::floorEps4)));
+		const Ratio2 pW = leftRole2(fw, stencil1_2(E5, E4, E3), stencil2_2(E4, E3, E2), stencil3_2(E3, E2, E1));
+		const Ratio2 mNext = rightRole2(fw, stencil1_2(E1, E2, E3), stencil2_2(E2, E3, E4), stencil3_2(E3, E4, E5));
+		F2 sum = godunovPair(negA, negB, mW, pW);
+		// x: values x-3 .. x+4 of the row, from the tile
+		{
+			float u[8];
+			const float *row = tile + lyj * kPtRow;
+			if (innerX) {
+#pragma unroll
+				for (int t = 0; t < 5; t++) {
+					const float2 a = *reinterpret_cast<const float2 *>(row + lxi + 2 * t - 4);
+					if (t > 0) u[2 * t - 1] = a.x;
+					if (2 * t < 8) u[2 * t] = a.y;
+				}
+			} else {
+#pragma unroll
+				for (int t = 0; t < 8; t++) u[t] = row[min(max(i + t - 3, 0), sx - 1) - x0 + 4];
+			}
+			const float D1 = u[1] - u[0], D2 = u[2] - u[1], D3 = u[3] - u[2], D4 = u[4] - u[3], D5 = u[5] - u[4], D6 = u[6] - u[5], D7 = u[7] - u[6];
+			const Ratio2 outer = faceRight2(f2(D1, D7), f2(D2, D6), f2(D3, D5), f2(D4, D4), f2(D5, D3));
+			const float M = maxNonNeg(maxNonNeg(maxNonNeg(D2 * D2, D3 * D3), maxNonNeg(D4 * D4, D5 * D5)), D6 * D6);
+			const FaceWeights<float> wm = faceWeights(smoothL(smoothG(D2, D3, D4), D2, D3, D4), smoothM(smoothG(D3, D4, D5), D3, D5),
+			                                          smoothR(smoothG(D4, D5, D6), D4, D5, D6),
+			                                          fma(M, WenoConst<float>::epsScale, WenoConst<float>::floorEps4));
+			const F2 W1 = mul2(f2(0.1f), f2(wm.c, wm.a)), Wb = f2(wm.b), W3 = mul2(f2(0.3f), f2(wm.a, wm.c));
+			const F2 S1m = stencil1_2(f2(D6, D2), f2(D5, D3), f2(D4, D4));
+			const F2 S2m = stencil2_2(f2(D5, D3), f2(D4, D4), f2(D3, D5));
+			const F2 S3m = stencil3_2(f2(D4, D4), f2(D3, D5), f2(D2, D6));
+			const Ratio2 mid = {fma2(W1, S1m, fma2(Wb, S2m, mul2(W3, S3m))), add2(add2(W1, Wb), W3)};
+			const Ratio2 mX = {f2(outer.num.v.x, mid.num.v.y), f2(outer.den.v.x, mid.den.v.y)};
+			const Ratio2 pX = {f2(mid.num.v.x, outer.num.v.y), f2(mid.den.v.x, outer.den.v.y)};
+			sum = add2(sum, godunovPair(negA, negB, mX, pX));
+		}
+		// y: the paired cell form on the two columns, from the tile
+		{
+			F2 yv[7];
+#pragma unroll
+			for (int t = 0; t < 7; t++) {
+				if (t == 3) { yv[t] = f; continue; }
+				const int ly = innerY ? lyj + t - 3 : min(max(j + t - 3, 0), sy - 1) - y0 + 3;
+				yv[t] = F2{*reinterpret_cast<const float2 *>(tile + ly * kPtRow + lxi)};
+			}
+			Ratio2 mY, pY;
+			wenoCell2(yv, mY, pY);
+			sum = add2(sum, godunovPair(negA, negB, mY, pY));
+		}
+		const float2 res = rkUpdatePair<Mode>(f, sum, k6, dx, dt, base, id);
+		if (active) *reinterpret_cast<float2 *>(out + id) = res;
+		// this warp is done with plane w
+		__syncwarp();
+		if ((threadIdx.x & 31) == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smemAddr(emptyBar + slot)) : "memory");
+		// thread 0 refills the slot of plane w - 1 once every warp has passed it (warp 0 gives up
+		// together if that wait runs out)
+		if (threadIdx.x < 32 && w - 1 >= w0 && issued < w1) {
+			bool ok = true;
+			if (threadIdx.x == 0) {
+				const int wr = w - 1, rs = (wr - w0) % kPtSlots;
+				ok = mbarWait(smemAddr(emptyBar + rs), unsigned((wr - w0) / kPtSlots) & 1u);
+				if (ok) {
+					asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+					issue(issued);
+				}
+			}
+			if (!__shfl_sync(0xffffffffu, int(ok), 0)) { giveUp(w + 1); return; }
+			issued++;
+		}
+		// slide the window one cell up
+		if (w + 1 < w1) {
+			const F2 zn = ldg2(col + int64_t(min(w + 4, sz - 1)) * plane);
+#pragma unroll
+			for (int t = 0; t < 6; t++) v[t] = v[t + 1];
+			v[6] = zn;
+			E1 = E2; E2 = E3; E3 = E4; E4 = E5; E5 = sub2(v[6], v[5]);
+			S1 = S2; S2 = S3; S3 = S4; S4 = S5; S5 = mul2(E5, E5);
+			gA = gB; gB = gC;
+			mW = mNext;
+		}
+	}
+}
+
 // Tensor maps of the planes the tiled form reads, per (address, shape); encoded on the host
 // (cuTensorMapEncodeTiled through the runtime's driver entry point) on first use.
 namespace {
 struct MapKey {
-	const void *p; int sx, sy, sz;
+	const void *p; int sx, sy, sz, box;  // box: 0 the tiled column form's, 1 the tiled pair form's
 	bool operator<(const MapKey &o) const {
 		if (p != o.p) return p < o.p;
 		if (sx != o.sx) return sx < o.sx;
 		if (sy != o.sy) return sy < o.sy;
-		return sz < o.sz;
+		if (sz != o.sz) return sz < o.sz;
+		return box < o.box;
 	}
 };
 std::mutex g_mapMutex;
@@ -886,13 +1072,14 @@ PFN_cuTensorMapEncodeTiled_v12000 encodeTiled() {
 }
 }  // namespace
 
-// The tensor map of plane `in` of a 3D FP32 grid, or false when the tiled form cannot
-// read it (rows not a multiple of 16 bytes, an unaligned address, no encoder).
-static bool tiledMap(const float *in, const G<3, float> &g, CUtensorMap *out) {
+// The tensor map of plane `in` of a 3D FP32 grid with the tile box of the tiled column form
+// (boxId 0) or of the tiled pair form (1), or false when it cannot be read that way (rows
+// not a multiple of 16 bytes, an unaligned address, no encoder).
+static bool tiledMap(const float *in, const G<3, float> &g, CUtensorMap *out, int boxId = 0) {
 	const int sx = g.s[0], sy = g.s[1], sz = g.s[2];
 	if (sx % 4 != 0 || (reinterpret_cast<uintptr_t>(in) & 15) != 0) return false;
 	std::lock_guard<std::mutex> lock(g_mapMutex);
-	const MapKey key{in, sx, sy, sz};
+	const MapKey key{in, sx, sy, sz, boxId};
 	auto it = g_maps.find(key);
 	if (it != g_maps.end()) { *out = it->second; return true; }
 	PFN_cuTensorMapEncodeTiled_v12000 enc = encodeTiled();
@@ -900,7 +1087,7 @@ static bool tiledMap(const float *in, const G<3, float> &g, CUtensorMap *out) {
 	CUtensorMap m;
 	const cuuint64_t dims[3] = {cuuint64_t(sx), cuuint64_t(sy), cuuint64_t(sz)};
 	const cuuint64_t strides[2] = {cuuint64_t(sx) * 4, cuuint64_t(sx) * cuuint64_t(sy) * 4};
-	const cuuint32_t box[3] = {cuuint32_t(kTileRow), cuuint32_t(kTileRows), 1};
+	const cuuint32_t box[3] = {cuuint32_t(boxId ? kPtRow : kTileRow), cuuint32_t(boxId ? kPtRows : kTileRows), 1};
 	const cuuint32_t elem[3] = {1, 1, 1};
 	if (enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(in), dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
 	        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
@@ -1020,7 +1207,7 @@ __global__ void __launch_bounds__(256) kWenoSweep(G<D, T> g, const T *__restrict
 // cells per thread.  Chosen by timing (reinitPlanFor) and cached per device
 // and shape.
 enum ReinitForm { kFormCells = GARM_REINIT_CELLS, kFormColumns = GARM_REINIT_COLUMNS, kFormSweeps = GARM_REINIT_SWEEPS, kFormTiled = GARM_REINIT_TILED,
-                  kFormPairs = GARM_REINIT_PAIRS };
+                  kFormPairs = GARM_REINIT_PAIRS, kFormPairsTiled = GARM_REINIT_PAIRS_TILED };
 
 // The pair form reads and writes float2: rows of even length and 8-byte aligned planes.
 static bool pairsApply(const G<3, float> &g, const void *in, const void *base, const void *out) {
@@ -1058,6 +1245,17 @@ static int launchReinit(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g,
 			return 1;
 		}
 		CUtensorMap map;
+		if (pl.form == kFormPairsTiled && pairsApply(g, in, base, out) && tiledMap((const float *)in, g, &map, 1)) {
+			const dim3 grid((g.s[0] + 2 * kPtX - 1) / (2 * kPtX), (g.s[1] + kPtY - 1) / kPtY, (g.s[2] + pl.chunk - 1) / pl.chunk);
+			launchPdl(kReinitPairsTiled<Mode>, grid, dim3(kPtX * kPtY), st, map, g, (const float *)in, (const float *)base, (float *)out, float(dt), pl.chunk, err);
+			return 1;
+		}
+		if (pl.form == kFormPairsTiled && pairsApply(g, in, base, out)) {  // rows not a multiple of 16 bytes: the pair form
+			const int pairs = (g.s[0] / 2) * g.s[1];
+			const dim3 grid((pairs + 128 - 1) / 128, (g.s[2] + pl.chunk - 1) / pl.chunk);
+			launchPdl(kReinitPairs<Mode>, grid, dim3(128), st, g, (const float *)in, (const float *)base, (float *)out, float(dt), pl.chunk);
+			return 1;
+		}
 		if (pl.form == kFormTiled && tiledMap((const float *)in, g, &map)) {
 			const dim3 grid((g.s[0] + kTileX - 1) / kTileX, (g.s[1] + kTileY - 1) / kTileY, (g.s[2] + pl.chunk - 1) / pl.chunk);
 			launchPdl(kReinitColumnsTiled<Mode>, grid, dim3(kTileX * kTileY), st, map, g, (const float *)in, (const float *)base, (float *)out, float(dt), pl.chunk, err);
@@ -1065,7 +1263,7 @@ static int launchReinit(const ReinitPlan &pl, cudaStream_t st, const G<D, T> &g,
 		}
 	}
 	// the column form (also the tiled and pair forms where they do not apply)
-	const int block = pl.form == kFormTiled ? kTileX * kTileY : pl.block;
+	const int block = pl.form == kFormTiled ? kTileX * kTileY : pl.form == kFormPairsTiled ? kPtX * kPtY : pl.block;
 	const int plane = g.s[0] * (D == 3 ? g.s[1] : 1);
 	const int sw = g.s[D - 1];
 	const dim3 grid((plane + block - 1) / block, (sw + pl.chunk - 1) / pl.chunk);
@@ -1119,9 +1317,12 @@ static ReinitPlan reinitPlanFor(cudaStream_t st, const G<D, T> &g, const T *phi,
 		for (int c : colWalks) cand.push_back({kFormColumns, b, c});
 	if (D == 3 && sizeof(T) == 4) {
 		for (int c : {4, 8, 16, 32}) cand.push_back({kFormTiled, kTileX * kTileY, c});
-		if (g.s[0] % 2 == 0)
+		if (g.s[0] % 2 == 0) {
 			for (int b : {64, 128, 256})
 				for (int c : colWalks) cand.push_back({kFormPairs, b, c});
+			if (g.s[0] % 4 == 0)
+				for (int c : colWalks) cand.push_back({kFormPairsTiled, kPtX * kPtY, c});
+		}
 	}
 	// sweeps: walks that split the longest axis into 2-8 equal pieces, plus short fixed ones
 	int longest = 0;
@@ -1170,7 +1371,7 @@ garm_status pinReinitPlan(int dim, int esz, const int *size, int form, int block
 	if (block == 0) { g_plans.erase(key); return GARM_OK; }
 	ReinitPlan pl;
 	pl.form = form;
-	pl.block = form == kFormCells ? kBlock : form == kFormTiled ? kTileX * kTileY : block;
+	pl.block = form == kFormCells ? kBlock : form == kFormTiled ? kTileX * kTileY : form == kFormPairsTiled ? kPtX * kPtY : block;
 	pl.chunk = form == kFormCells ? 0 : chunk;
 	g_plans[key] = pl;
 	return GARM_OK;

@@ -20,7 +20,7 @@ STATUS_NAMES = {OK: "ok", INVALID: "invalid", OOM: "oom", NOT_CONVERGED: "not_co
                 CUDA_ERROR: "cuda_error", TIMEOUT: "timeout", UNSUPPORTED: "unsupported"}
 
 PRECISION_FP64, PRECISION_MIXED = 0, 1
-REINIT_FORMS = ["cells", "columns", "sweeps", "tiled", "pairs"]  # GARM_REINIT_CELLS, _COLUMNS, _SWEEPS, _TILED, _PAIRS
+REINIT_FORMS = ["cells", "columns", "sweeps", "tiled", "pairs", "pairs_tiled"]  # GARM_REINIT_CELLS, _COLUMNS, _SWEEPS, _TILED, _PAIRS, _PAIRS_TILED
 
 # garm_field
 (FIELD_VELOCITY, FIELD_LEVEL_SET, FIELD_REF_MAP, FIELD_REF_MAP_GRAD, FIELD_REF_LEVEL_SET, FIELD_REF_LEVEL_SET_GRAD,

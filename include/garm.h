@@ -207,13 +207,16 @@ garm_status garm_sim_graph_active(const garm_sim *sim, int *active);
  * per axis, threads walking lines of that axis; (3D FP32) columns whose in-plane
  * stencils read tiles of each plane staged in shared memory by TMA, 128 threads per
  * block; or (3D FP32, rows of even length) threads walking two x-adjacent columns
- * as the two lanes of paired FP32 instructions, sharing the x face set between them
- * (other precisions and shapes run the column form). */
+ * as the two lanes of paired FP32 instructions, sharing the x face set between them;
+ * or (3D FP32, rows of a multiple of 4 cells) that pair form with its in-plane stencils
+ * read from TMA-staged plane tiles, 128 threads per block (other precisions and shapes
+ * run the column form, or the pair form for even rows). */
 #define GARM_REINIT_CELLS 0
 #define GARM_REINIT_COLUMNS 1
 #define GARM_REINIT_SWEEPS 2
 #define GARM_REINIT_TILED 3
 #define GARM_REINIT_PAIRS 4
+#define GARM_REINIT_PAIRS_TILED 5
 /* The launch plan the reinitialisation autotuner chose for this simulation's grid:
  * form, threads per block, cells each thread walks and the timed sub-stage in ms.
  * Plans are tuned once per grid shape, precision and device in the process, on

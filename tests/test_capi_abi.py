@@ -84,7 +84,7 @@ def test_header_constants_match_the_binding():
     assert count == len(fields) == len(capi.FIELD_NAMES)
     for name, value in fields.items():
         assert getattr(capi, "FIELD_" + name) == value, name
-    forms = {m.group(1).lower(): int(m.group(2)) for m in re.finditer(r"#define GARM_REINIT_([A-Z]+) (\d+)", text)}
+    forms = {m.group(1).lower(): int(m.group(2)) for m in re.finditer(r"#define GARM_REINIT_([A-Z_]+) (\d+)", text)}
     assert forms == {f: i for i, f in enumerate(capi.REINIT_FORMS)}
 
 

@@ -1,7 +1,7 @@
 """Every launch plan of the WENO5 reinitialisation (one thread per cell, columns
-along the last axis, one sweep per axis, columns reading TMA-staged plane tiles, or
-pairs of x-adjacent columns walked together, with several block sizes and walk
-lengths) gives the oracle's result, on ragged 2D and 3D shapes whose sizes are not
+along the last axis, one sweep per axis, columns reading TMA-staged plane tiles,
+pairs of x-adjacent columns walked together, or those pairs reading TMA-staged plane
+tiles, with several block sizes and walk lengths) gives the oracle's result, on ragged 2D and 3D shapes whose sizes are not
 multiples of any block or chunk, and for iteration counts that leave the result in
 each of the three rotating planes.  Shapes with rows of odd length run the column
 form in place of the pair form; rows of 6 and 10 cells put every pair, or all but
@@ -19,7 +19,8 @@ pytestmark = pytest.mark.gpu
 PLANS = [("cells", 256, 0), ("columns", 64, 1), ("columns", 64, 4), ("columns", 128, 8), ("columns", 96, 32),
          ("columns", 256, 200), ("sweeps", 32, 1), ("sweeps", 64, 3), ("sweeps", 128, 16), ("sweeps", 256, 64),
          ("sweeps", 64, 500), ("tiled", 128, 1), ("tiled", 128, 5), ("tiled", 128, 8), ("tiled", 128, 100),
-         ("pairs", 32, 1), ("pairs", 64, 8), ("pairs", 128, 5), ("pairs", 256, 200)]
+         ("pairs", 32, 1), ("pairs", 64, 8), ("pairs", 128, 5), ("pairs", 256, 200),
+         ("pairs_tiled", 128, 1), ("pairs_tiled", 128, 3), ("pairs_tiled", 128, 8), ("pairs_tiled", 128, 200)]
 
 
 def _field(shape, seed):
@@ -39,8 +40,10 @@ def _field(shape, seed):
 
 # (72, 20, 24): rows of 16-byte multiples, so the tiled form stages the planes of its interior
 # blocks by TMA while its edge blocks walk with global loads
+# (36, 11, 13), (8, 5, 7), (4, 9, 6): rows of a multiple of 4 cells, so the tiled pair form stages
+# its planes by TMA, with threads beyond the grid and clamped stencils reaching every tile edge
 @pytest.mark.parametrize("shape,iters", [((37, 29), 12), ((23, 31, 41), 12), ((45, 6, 9), 7), ((5, 40, 3), 8), ((72, 20, 24), 9),
-                                         ((6, 9, 11), 10), ((10, 13, 17), 11)])
+                                         ((6, 9, 11), 10), ((10, 13, 17), 11), ((36, 11, 13), 9), ((8, 5, 7), 7), ((4, 9, 6), 8)])
 def test_plans_match_oracle(oracle_mod, garm_lib, shape, iters):
     phi0, dx = _field(shape, seed=len(shape))
     ref = oracle_mod.reinit(phi0, dx, iters, 0.5)
