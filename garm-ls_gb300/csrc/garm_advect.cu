@@ -114,7 +114,22 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 3 : 1) kAdvectRefMap(
 
 	// traceDrv<2> (Advection.h:71-82); grd is row-major here: grd[a*D+b] = ∂u_a/∂x_b
 	T vel0[D], grd0[D * D], vel1[D], grd1[D * D];
-	sampleFlow<D, T, true>(vv, pos, vel0, grd0);
+	// The first sample is at the cell centre itself.  In face grid a the centre lies half a
+	// cell from the two faces of the cell along a and on a node along the other axes, so the
+	// trilinear sample of u_a and of its gradient there is the mean of the cell's two a-faces
+	// (LinearIntrpl's weights are exactly 1/2 and 0/1 there; only their rounding is skipped).
+#pragma unroll
+	for (int a = 0; a < D; a++) {
+		const G<D, T> &ga = vv.fg[a];
+		const int64_t lo = ga.idx(ci, cj, ck);
+		const int64_t hi = ga.idx(ci + (a == 0), cj + (a == 1), ck + (a == 2));
+		vel0[a] = (ldg(vv.u[a] + lo) + ldg(vv.u[a] + hi)) * T(0.5);
+#pragma unroll
+		for (int b = 0; b < D; b++) {
+			const T *gp = vv.grad[a * 3 + b];
+			grd0[a * D + b] = (ldg(gp + lo) + ldg(gp + hi)) * T(0.5);
+		}
+	}
 	T pos1[3] = {T(0), T(0), T(0)};
 #pragma unroll
 	for (int a = 0; a < D; a++) pos1[a] = pos[a] + vel0[a] * mdt;
@@ -268,7 +283,26 @@ __global__ void __launch_bounds__(kBlock) kAdvectVelocity(Geom geom, VelView<D, 
 	g.coord(id, i, j, k);
 	T pos[3] = {g.pos(0, i), g.pos(1, j), D == 3 ? g.pos(2, k) : T(0)};
 	T vel0[D], vel1[D];
-	sampleFlow<D, T, false>(vv, pos, vel0, nullptr);
+	// The flow at the face centre itself (the trace's first sample).  In the face's own grid
+	// that is the node value.  In another face grid b the centre lies half a cell from the
+	// nodes along the face's axis and along b, and on a node along the third axis, so the
+	// trilinear sample there is the mean of four values, at the same clamp-to-edge indices
+	// (LinearIntrpl's weights are exactly 1/2 there; only their rounding is skipped).
+#pragma unroll
+	for (int b = 0; b < D; b++) {
+		if (b == axis) { vel0[b] = ldg(vv.u[b] + id); continue; }
+		const G<D, T> &gb = vv.fg[b];
+		T s = T(0);
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			const int sa = q & 1, sb = q >> 1;  // lower or upper node along `axis`, along b
+			const int xi = i - int(axis == 0 && sa == 0) + int(b == 0 && sb == 1);
+			const int yj = j - int(axis == 1 && sa == 0) + int(b == 1 && sb == 1);
+			const int zk = k - int(axis == 2 && sa == 0) + int(b == 2 && sb == 1);
+			s += ldg(vv.u[b] + gb.cidx(xi, yj, zk));
+		}
+		vel0[b] = s * T(0.25);
+	}
 	T p1[3] = {T(0), T(0), T(0)};
 #pragma unroll
 	for (int a = 0; a < D; a++) p1[a] = pos[a] + vel0[a] * mdt;
