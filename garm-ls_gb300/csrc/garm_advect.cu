@@ -84,7 +84,7 @@ __device__ __forceinline__ void sampleFlow(const VelView<D, T> &v, const T *p, T
 #pragma unroll
 			for (int b = 0; b < D; b++) grd[a * D + b] = out[1 + b];
 		} else {
-			vel[a] = lerp<D, T>(v.u[a], v.fg[a], p);
+			vel[a] = lerpNested<D, T>(v.u[a], v.fg[a], p);
 		}
 	}
 }

@@ -136,6 +136,31 @@ __device__ __forceinline__ T lerp(const T *__restrict__ f, const G<D, T> &g, con
 	}
 }
 
+// The same trilinear (bilinear) sample as `lerp`, evaluated as nested one-dimensional
+// interpolations a + f·(b - a), x first: 7 (3) of them, against 8 weight products and
+// their sum.  Equal to `lerp` up to rounding.
+template <int D, typename T>
+__device__ __forceinline__ T lerpNested(const T *__restrict__ f, const G<D, T> &g, const T *p) {
+	const int li = g.lower(0, p[0]), lj = g.lower(1, p[1]);
+	const T fx = g.frac(0, p[0], li), fy = g.frac(1, p[1], lj);
+	const int i0 = g.cx(li), i1 = g.cx(li + 1), j0 = g.cy(lj), j1 = g.cy(lj + 1);
+	auto mix = [](T a, T b, T t) { return fma(t, b - a, a); };
+	if (D == 2) {
+		const T r0 = mix(ldg(f + g.idx(i0, j0, 0)), ldg(f + g.idx(i1, j0, 0)), fx);
+		const T r1 = mix(ldg(f + g.idx(i0, j1, 0)), ldg(f + g.idx(i1, j1, 0)), fx);
+		return mix(r0, r1, fy);
+	} else {
+		const int lk = g.lower(2, p[2]);
+		const T fz = g.frac(2, p[2], lk);
+		const int k0 = g.cz(lk), k1 = g.cz(lk + 1);
+		const T r00 = mix(ldg(f + g.idx(i0, j0, k0)), ldg(f + g.idx(i1, j0, k0)), fx);
+		const T r10 = mix(ldg(f + g.idx(i0, j1, k0)), ldg(f + g.idx(i1, j1, k0)), fx);
+		const T r01 = mix(ldg(f + g.idx(i0, j0, k1)), ldg(f + g.idx(i1, j0, k1)), fx);
+		const T r11 = mix(ldg(f + g.idx(i0, j1, k1)), ldg(f + g.idx(i1, j1, k1)), fx);
+		return mix(mix(r00, r10, fy), mix(r01, r11, fy), fz);
+	}
+}
+
 // Trilinear sample of NP planes that share one grid (one set of weights).
 template <int D, typename T, int NP>
 __device__ __forceinline__ void lerpN(const T *const *f, const G<D, T> &g, const T *p, T *out) {
