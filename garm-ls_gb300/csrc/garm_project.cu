@@ -328,6 +328,92 @@ __device__ __forceinline__ void gridTotals(const double *partials, int maxBlocks
 
 struct NoFin { __device__ void operator()(double *) const {} };
 
+// The FP64 solve's reductions, with their FP64 additions spread over one warp per SM
+// sub-partition rather than a butterfly in all sixteen warps: GB300 issues a warp's FP64
+// instruction about every 64 cycles per sub-partition, so the additions, not the shuffles,
+// set the cost.  Block partials: every thread stages its NV values in shared memory; warps
+// 0-3 each sum a quarter of them (lane l: threads l, l + 32, ... of the quarter, then the
+// butterfly); lanes v < NV of warp 0 add the four quarter sums of value v in order and
+// store the block's partials, and thread 0 arrives at the grid barrier (the __syncwarp
+// orders lanes 1..NV-1's stores before its release).
+template <int NV>
+__device__ __forceinline__ void blockPartials64(double (&acc)[NV], double *partials, int maxBlocks, double *sh, unsigned *bar, unsigned &epoch) {
+	static_assert(NV <= 3, "staged values");
+	__shared__ double stage[3 * kCgBlock];
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, n = blockDim.x, quarter = n / 4;
+#pragma unroll
+	for (int v = 0; v < NV; v++) stage[v * n + threadIdx.x] = acc[v];
+	__syncthreads();
+	if (w < 4) {
+		double t[NV];
+#pragma unroll
+		for (int v = 0; v < NV; v++) {
+			t[v] = 0;
+			for (int q = lane; q < quarter; q += 32) t[v] += stage[v * n + w * quarter + q];
+		}
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			double y[NV];
+#pragma unroll
+			for (int v = 0; v < NV; v++) y[v] = __shfl_xor_sync(0xffffffffu, t[v], o);
+#pragma unroll
+			for (int v = 0; v < NV; v++) t[v] += y[v];
+		}
+		if (lane == 0) {
+#pragma unroll
+			for (int v = 0; v < NV; v++) sh[v * 16 + w] = t[v];
+		}
+	}
+	__syncthreads();
+	if (w == 0) {
+		if (lane < NV) {
+			double q = sh[lane * 16];
+			q += sh[lane * 16 + 1];
+			q += sh[lane * 16 + 2];
+			q += sh[lane * 16 + 3];
+			partials[lane * maxBlocks + blockIdx.x] = q;
+		}
+		__syncwarp();
+		if (lane == 0) gridArrive(bar, epoch);
+	}
+}
+
+// Grid totals for the FP64 solve: warp v sums value v's block partials (lane l: blocks l,
+// l + 32, ..., then the butterfly, the order of gridTotals), so the NV sums run on
+// different sub-partitions; thread 0 then runs `fin` on the totals and the NOUT results
+// reach the block through shared memory.
+template <int NV, int NOUT, typename Fin>
+__device__ __forceinline__ void gridTotals64(const double *partials, int maxBlocks, double (&out)[NOUT], double *sh, Fin fin) {
+	static_assert(NOUT >= NV && NOUT <= 8 && NV <= 3, "outputs include the sums");
+	const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nb = gridDim.x;
+	if (w < NV) {
+		constexpr int U = 5;  // 160 blocks in one round trip
+		double q[U];
+#pragma unroll
+		for (int u = 0; u < U; u++) q[u] = lane + 32 * u < nb ? ldcg(partials + w * maxBlocks + lane + 32 * u) : 0.0;
+		double t = 0;
+#pragma unroll
+		for (int u = 0; u < U; u++)
+			if (lane + 32 * u < nb) t += q[u];
+		for (int b = lane + 32 * U; b < nb; b += 32) t += ldcg(partials + w * maxBlocks + b);
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+		if (lane == 0) sh[kShOut + w] = t;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double t[NOUT];
+#pragma unroll
+		for (int v = 0; v < NV; v++) t[v] = sh[kShOut + v];
+		fin(t);
+#pragma unroll
+		for (int v = 0; v < NOUT; v++) sh[kShOut + v] = t[v];
+	}
+	__syncthreads();
+#pragma unroll
+	for (int v = 0; v < NOUT; v++) out[v] = sh[kShOut + v];
+}
+
 // Scalar work of an iteration is done once, by the lane that finishes the grid totals,
 // and handed to the block through the broadcast totals: a decision as 0.0 / 1.0 and
 // the FP32 β, α packed into the bits of one double.  The other threads read both with
@@ -400,11 +486,11 @@ __device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, NbW64 *enS, unsi
 	}
 	{
 		double acc[3] = {acc0, acc1, acc2};
-		blockPartials<3>(acc, a.partials, a.maxBlocks, sh, a.bar, epoch);
+		blockPartials64<3>(acc, a.partials, a.maxBlocks, sh, a.bar, epoch);
 	}
 	if (!gridWait(a.bar, a.err, epoch)) { *ok = false; return 0; }
 	double tot[6];
-	gridTotals<3, 6>(a.partials, a.maxBlocks, tot, sh, [](double *t) { t[3] = 0; t[4] = t[0] / t[1]; t[5] = 0; });
+	gridTotals64<3, 6>(a.partials, a.maxBlocks, tot, sh, [](double *t) { t[3] = 0; t[4] = t[0] / t[1]; t[5] = 0; });
 	double gamma = tot[0];
 	const double rhsNorm2 = tot[2];
 	*outB2 = rhsNorm2;
@@ -510,14 +596,14 @@ __device__ int pcgFp64Split(const CgArgs &a, int n, double *sh, NbW64 *enS, unsi
 			}
 		}
 		double acc[3] = {g, d, rr};
-		blockPartials<3>(acc, a.partials, a.maxBlocks, sh, a.bar, epoch);
+		blockPartials64<3>(acc, a.partials, a.maxBlocks, sh, a.bar, epoch);
 		// β = γ/γ_old and α = γ/(δ - βγ/α_old) with the reciprocals of the known γ_old and
 		// γ_old·α_old formed before the barrier: one division after it
 		// (warp 0 alone, whose lane 0 finishes the totals)
 		double invG = 0, invGA = 0;
 		if (threadIdx.x < 32) { invG = 1.0 / gamma; invGA = invG / alpha; }
 		if (!gridWait(a.bar, a.err, epoch)) { *ok = false; it++; break; }
-		gridTotals<3, 6>(a.partials, a.maxBlocks, tot, sh, [invG, invGA, threshold](double *t) {
+		gridTotals64<3, 6>(a.partials, a.maxBlocks, tot, sh, [invG, invGA, threshold](double *t) {
 			t[3] = t[0] * invG;
 			t[4] = t[0] / fma(-t[0] * t[0], invGA, t[1]);
 			t[5] = t[2] < threshold ? 1.0 : 0.0;  // converged
