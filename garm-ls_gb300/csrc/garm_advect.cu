@@ -289,20 +289,7 @@ __global__ void __launch_bounds__(kBlock) kAdvectVelocity(Geom geom, VelView<D, 
 	// trilinear sample there is the mean of four values, at the same clamp-to-edge indices
 	// (LinearIntrpl's weights are exactly 1/2 there; only their rounding is skipped).
 #pragma unroll
-	for (int b = 0; b < D; b++) {
-		if (b == axis) { vel0[b] = ldg(vv.u[b] + id); continue; }
-		const G<D, T> &gb = vv.fg[b];
-		T s = T(0);
-#pragma unroll
-		for (int q = 0; q < 4; q++) {
-			const int sa = q & 1, sb = q >> 1;  // lower or upper node along `axis`, along b
-			const int xi = i - int(axis == 0 && sa == 0) + int(b == 0 && sb == 1);
-			const int yj = j - int(axis == 1 && sa == 0) + int(b == 1 && sb == 1);
-			const int zk = k - int(axis == 2 && sa == 0) + int(b == 2 && sb == 1);
-			s += ldg(vv.u[b] + gb.cidx(xi, yj, zk));
-		}
-		vel0[b] = s * T(0.25);
-	}
+	for (int b = 0; b < D; b++) vel0[b] = faceCentreSample<D, T>(vv.u[b], vv.fg[b], b, axis, i, j, k, id);
 	T p1[3] = {T(0), T(0), T(0)};
 #pragma unroll
 	for (int a = 0; a < D; a++) p1[a] = pos[a] + vel0[a] * mdt;

@@ -136,6 +136,27 @@ __device__ __forceinline__ T lerp(const T *__restrict__ f, const G<D, T> &g, con
 	}
 }
 
+// `lerp` of a field on face grid b (`gb`) at the centre of face (i, j, k) of face grid
+// `axis`.  For b == axis that is the node value.  Otherwise the centre lies half a cell from
+// the nodes of grid b along `axis` and along b, and on a node along the third axis, so the
+// trilinear sample is the mean of four values at the same clamp-to-edge indices (the
+// weights are exactly 1/2; only their rounding is skipped).  b is a compile-time index in
+// the callers' unrolled loops.
+template <int D, typename T>
+__device__ __forceinline__ T faceCentreSample(const T *__restrict__ f, const G<D, T> &gb, int b, int axis, int i, int j, int k, int64_t ownId) {
+	if (b == axis) return ldg(f + ownId);
+	T s = T(0);
+#pragma unroll
+	for (int q = 0; q < 4; q++) {
+		const int sa = q & 1, sb = q >> 1;  // lower or upper node along `axis`, along b
+		const int xi = i - int(axis == 0 && sa == 0) + int(b == 0 && sb == 1);
+		const int yj = j - int(axis == 1 && sa == 0) + int(b == 1 && sb == 1);
+		const int zk = k - int(axis == 2 && sa == 0) + int(b == 2 && sb == 1);
+		s += ldg(f + gb.cidx(xi, yj, zk));
+	}
+	return s * T(0.25);
+}
+
 // The same trilinear (bilinear) sample as `lerp`, evaluated as nested one-dimensional
 // interpolations a + f·(b - a), x first: 7 (3) of them, against 8 weight products and
 // their sum.  Equal to `lerp` up to rounding.
