@@ -1446,14 +1446,16 @@ __global__ void __launch_bounds__(kBlock) kCheckRefMap(int64_t N, const T *ori, 
 #pragma unroll
 			for (int q = 0; q < D * D; q++) m[q] = double(pi.p[q][id]);
 			auto dot = [&](int p, int q) { double s = m[p * D + 0] * m[q * D + 0]; for (int k = 1; k < D; k++) s = fma(m[p * D + k], m[q * D + k], s); return s; };
+			// cos² > θ of a pair of columns, (a·b)²/(|a|²|b|²) > θ, tested as (a·b)² > θ|a|²|b|²:
+			// the same decision without the divisions (about ten FP64 instructions each on
+			// GB300); a zero column gives false in both forms.
 			if (D == 2) {
 				const double ab = dot(0, 1);
-				if (ab * ab / dot(0, 0) / dot(1, 1) > threshold) bad = 1;
+				if (ab * ab > threshold * (dot(0, 0) * dot(1, 1))) bad = 1;
 			} else {
 				const double aa = dot(0, 0), bb = dot(1, 1), cc = dot(2, 2);
 				const double ab = dot(0, 1), ac = dot(0, 2), bc = dot(1, 2);
-				const double vab = ab * ab / aa / bb, vac = ac * ac / aa / cc, vbc = bc * bc / bb / cc;
-				if (vab > threshold || vac > threshold || vbc > threshold) bad = 1;
+				if (ab * ab > threshold * (aa * bb) || ac * ac > threshold * (aa * cc) || bc * bc > threshold * (bb * cc)) bad = 1;
 			}
 		}
 	}
