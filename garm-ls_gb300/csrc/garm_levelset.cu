@@ -219,6 +219,14 @@ __device__ __forceinline__ double pow2NegExp(double x) {
 __device__ __forceinline__ float pow2NegExp(float x) {
 	return __int_as_float((254 << 23) - (__float_as_int(x) & 0x7f800000));
 }
+// x·2^-e for the same x: x's significand in [1, 2), equal to x * pow2NegExp(x) (an exact
+// product) but formed on the integer pipe by setting the exponent field to the bias.
+__device__ __forceinline__ double significandOf(double x) {
+	return __hiloint2double((__double2hiint(x) & 0x000fffff) | 0x3ff00000, __double2loint(x));
+}
+__device__ __forceinline__ float significandOf(float x) {
+	return __int_as_float((__float_as_int(x) & 0x007fffff) | 0x3f800000);
+}
 
 // max of two non-negative, non-NaN values.  For such values the IEEE bit
 // patterns order like the numbers, so an integer max gives exactly fmax and
@@ -1114,15 +1122,21 @@ garm_status tiledReinitStatus(cudaStream_t st, const int *err) {
 // (2000, "Weighted ENO schemes for Hamilton-Jacobi equations"), an exact
 // rewrite of the same weights: a central part 12C(i) = 7(D_i + D_{i+1}) -
 // (D_{i-1} + D_{i+2}) shared by both one-sided derivatives of cell i, and a
-// correction in the face's third differences T1 = a-2b+c, T2 = b-2c+d of its
-// second differences a..d, whose smoothness indicators are
+// correction in T1 = a-2b+c and T2 = b-2c+d, built from the face's second
+// differences a..d, whose smoothness indicators are
 // 13(x-y)^2 + 3(..)^2 = 12 times the reference's (computed here divided by 3,
 // 13/3 (x-y)^2 + (..)^2, with ε scaled alike: see WenoConst):
 //   12 φ⁻(i+1) = 12C(i+1) + T2 - (.4 t2t3 T1 + .6 t1t2 T2) / (.1 t2t3 + .6 t1t3 + .3 t1t2)
 //   12 φ⁺(i)   = 12C(i)   - T1 + (.4 t1t2 T2 + .6 t2t3 T1) / (.1 t1t2 + .6 t1t3 + .3 t2t3)
+// The kernel carries 6φ: with s = D_i + D_{i+1} (cell i = f+1) the bases are
+// 6C + T2/2 = 3s - (c-b) and 6C - T2/2 = 3s - (d-c), one fma each, and each
+// ratio is halved, then scaled by 5/3 above and below: with U = t2t3 T1 and
+// V = t1t2 T2 the numerators are 2/3 U + V and U + 2/3 V over
+// 1/3 t2t3 + 2 t1t3 + t1t2 and t2t3 + 2 t1t3 + 1/3 t1t2 (two fma each).  T2 is the
+// difference of the third differences c-b and d-c, and g13(c, d) squares the latter.
 // Differences, squares, g terms, third differences and central parts slide
-// with the walk, so a face costs about 57 operations against ~116 per axis of
-// the cell form.  The Godunov sum of the first passes goes to `out` (x pass:
+// with the walk, so each face set is built once per pass, at about 44
+// arithmetic instructions.  The Godunov sum of the first passes goes to `out` (x pass:
 // stored, y pass: added); the last pass adds its own and applies the update.
 // 13/3 (x-y)^2: the indicators here are 13(x-y)^2 + 3 l^2 divided by 3 (with ε
 // alike), so the second square enters with weight 1 (one fma per indicator).
@@ -1156,48 +1170,46 @@ __global__ void __launch_bounds__(256) kWenoSweep(G<D, T> g, const T *__restrict
 	T Q1 = E1 * E1, Q2 = E2 * E2, Q3 = E3 * E3, Q4 = E4 * E4;
 	T a = E2 - E1, b = E3 - E2, c = E4 - E3;                                // Δ_f .. Δ_{f+2}
 	T gab = g13(a, b), gbc = g13(b, c);
-	T T1 = fma(T(-2), b, a + c);
-	T T1x4 = T(0.4) * T1, T1x6 = T(0.6) * T1;
-	T C12 = T(0), dmCarry = T(0);
-	const T k = g.inv * T(1.0 / 12.0);
+	T e2 = c - b;                                                             // third difference
+	T T1 = e2 - (b - a);
+	T dpBase = T(0), dmCarry = T(0);
+	const T k = g.inv * T(1.0 / 6.0);
 	for (int f = f0; f < w1; f++) {
 		const T pn = ld(f + 3);
 		const T E5 = pn - phiF2, Q5 = E5 * E5;
 		const T d = E5 - E4;
-		const T T2 = fma(T(-2), c, b + d);
-		const T T2x4 = T(0.4) * T2, T2x6 = T(0.6) * T2;
-		const T gcd = g13(c, d);
+		const T e3 = d - c;
+		const T T2 = e3 - e2;                                                 // b - 2c + d
+		const T gcd = (T(13.0 / 3.0) * e3) * e3;                              // g13(c, d)
 		const T l0 = fma(T(-3), b, a), l1 = b + c, l2 = fma(T(3), c, -d);
 		const T is0 = fma(l0, l0, gab), is1 = fma(l1, l1, gbc), is2 = fma(l2, l2, gcd);
 		const T Qm = maxNonNeg(maxNonNeg(maxNonNeg(Q1, Q2), maxNonNeg(Q3, Q4)), Q5);
 		const T eps = fma(Qm, WenoConst<T>::epsScale, epsFloor);
-		const T sc = pow2NegExp(eps), es = eps * sc;
+		const T sc = pow2NegExp(eps), es = significandOf(eps);                  // es = eps·sc
 		const T q1 = fma(is0, sc, es), q2 = fma(is1, sc, es), q3 = fma(is2, sc, es);
 		const T t1 = q1 * q1, t2 = q2 * q2, t3 = q3 * q3;
-		const T Aw = t2 * t3, Bw = T(0.6) * (t1 * t3), Cw = t1 * t2;
-		const T Cn = fma(T(7), E3 + E4, -(E2 + E5));                            // 12 C(f+1)
-		const T denR = fma(T(0.3), Cw, fma(T(0.1), Aw, Bw));
-		const T numR = fma(Aw, T1x4, Cw * T2x6);
-		const T dmNext = fma(-numR, recipPos(denR), Cn + T2);                   // 12 φ⁻(f+1)
+		const T Aw = t2 * t3, T13 = t1 * t3, Cw = t1 * t2;
+		const T U = Aw * T1, V = Cw * T2;
+		const T s = E3 + E4;
+		const T denR = fma(T(1.0 / 3.0), Aw, fma(T(2), T13, Cw));
+		const T dmNext = fma(-fma(T(2.0 / 3.0), U, V), recipPos(denR), fma(T(3), s, -e2));   // 6 φ⁻(f+1)
 		if (f >= w0) {
-			const T denL = fma(T(0.3), Aw, fma(T(0.1), Cw, Bw));
-			const T numL = fma(Cw, T2x4, Aw * T1x6);
-			const T dpF = fma(numL, recipPos(denL), C12 - T1);                  // 12 φ⁺(f)
+			const T denL = fma(T(1.0 / 3.0), Cw, fma(T(2), T13, Aw));
+			const T dpF = fma(fma(T(2.0 / 3.0), V, U), recipPos(denL), dpBase);             // 6 φ⁺(f)
 			const bool neg = isNegative(phiF);
 			const T x = signBit(dmCarry) == neg ? dmCarry : T(0);
 			const T y = signBit(dpF) != neg ? dpF : T(0);
-			const T sum = fma(x, x, y * y);
 			const int64_t id = lb + int64_t(f) * st;
-			if (Stage == 0) out[id] = sum;
-			else if (Stage == 1) out[id] = out[id] + sum;
-			else out[id] = rkUpdate<T, Mode>(phiF, out[id] + sum, k, g.dx, dt, base, id);
+			if (Stage == 0) out[id] = fma(x, x, y * y);
+			else if (Stage == 1) out[id] = fma(x, x, fma(y, y, out[id]));
+			else out[id] = rkUpdate<T, Mode>(phiF, fma(x, x, fma(y, y, out[id])), k, g.dx, dt, base, id);
 		}
-		dmCarry = dmNext; C12 = Cn;
+		dmCarry = dmNext; dpBase = fma(T(3), s, -e3);                           // 6 C(f+1) - T2 / 2
 		E1 = E2; E2 = E3; E3 = E4; E4 = E5;
 		Q1 = Q2; Q2 = Q3; Q3 = Q4; Q4 = Q5;
 		a = b; b = c; c = d;
 		gab = gbc; gbc = gcd;
-		T1 = T2; T1x4 = T2x4; T1x6 = T2x6;
+		e2 = e3; T1 = T2;
 		phiF = phiF1; phiF1 = phiF2; phiF2 = pn;
 	}
 }

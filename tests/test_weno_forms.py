@@ -11,7 +11,12 @@ equations"), one face gives both
     12 φ⁻(i+1) = 12C(i+1) + T2 - (.4 t2t3 T1 + .6 t1t2 T2) / (.1 t2t3 + .6 t1t3 + .3 t1t2)
     12 φ⁺(i)   = 12C(i)   - T1 + (.4 t1t2 T2 + .6 t2t3 T1) / (.1 t1t2 + .6 t1t3 + .3 t2t3)
 with t_k = ((IS_k + ε')·2^-e)^2, 2^e ≤ ε' < 2^(e+1) (an exact scale that keeps the
-products of two t_k in range).
+products of two t_k in range).  The sweep kernel carries 6φ: with s = D_i + D_{i+1}
+the bases 6C ± T/2 are 3s - (c-b) and 3s - (d-c); each ratio is halved and scaled by
+5/3 above and below (U = t2t3 T1, V = t1t2 T2: numerators 2/3 U + V and U + 2/3 V
+over 1/3 t2t3 + 2 t1t3 + t1t2 and t2t3 + 2 t1t3 + 1/3 t1t2); T2 is the difference of
+the third differences c-b and d-c, and ε'·2^-e is ε''s significand.  face_form
+follows that arrangement.
 """
 from __future__ import annotations
 
@@ -39,27 +44,32 @@ def reference_weno(v):
 
 
 def face_form(phi):
-    """(12 φ⁻, 12 φ⁺) of every cell of a clamped line, built face by face."""
+    """(6 φ⁻, 6 φ⁺) of every cell of a clamped line, built face by face."""
     n = len(phi)
     at = lambda k: phi[min(max(k, 0), n - 1)]
     dm, dp = np.zeros(n), np.zeros(n)
     for f in range(-1, n):                      # face between f and f+1
         E = [at(f - 1 + q) - at(f - 2 + q) for q in range(5)]   # D_{f-1} .. D_{f+3}
         a, b, c, d = E[1] - E[0], E[2] - E[1], E[3] - E[2], E[4] - E[3]
-        T1, T2 = a - 2 * b + c, b - 2 * c + d
-        is0 = 13 * (a - b) ** 2 + 3 * (a - 3 * b) ** 2
-        is1 = 13 * (b - c) ** 2 + 3 * (b + c) ** 2
-        is2 = 13 * (c - d) ** 2 + 3 * (3 * c - d) ** 2
-        eps = 12 * (max(e * e for e in E) * 1e-6 + 1e-99)
-        sc = 2.0 ** -np.floor(np.log2(eps))          # exact power-of-two scale, as on the device
-        t1, t2, t3 = ((is0 + eps) * sc) ** 2, ((is1 + eps) * sc) ** 2, ((is2 + eps) * sc) ** 2
-        A, B, Cc = t2 * t3, .6 * t1 * t3, t1 * t2
-        C_left = 7 * (E[1] + E[2]) - (E[0] + E[3])     # cell f
-        C_right = 7 * (E[2] + E[3]) - (E[1] + E[4])    # cell f+1
+        T1 = (c - b) - (b - a)                       # a - 2b + c
+        T2 = (d - c) - (c - b)                       # b - 2c + d
+        # the indicators and ε divided by 3 (12/3 = 4 times the reference's)
+        is0 = 13 / 3 * (a - b) ** 2 + (a - 3 * b) ** 2
+        is1 = 13 / 3 * (b - c) ** 2 + (b + c) ** 2
+        is2 = 13 / 3 * (d - c) ** 2 + (3 * c - d) ** 2
+        eps = max(e * e for e in E) * 4e-6 + 4e-99
+        m, ex = np.frexp(eps)                        # eps = m·2^ex, m in [0.5, 1)
+        sc, es = 2.0 ** (1 - ex), 2.0 * m            # exact power-of-two scale; es = eps·sc
+        assert es == eps * sc and 1.0 <= es < 2.0
+        t1, t2, t3 = (is0 * sc + es) ** 2, (is1 * sc + es) ** 2, (is2 * sc + es) ** 2
+        A, T13, Cc = t2 * t3, t1 * t3, t1 * t2
+        U, V = A * T1, Cc * T2
+        s_left = E[1] + E[2]                          # D around cell f
+        s_right = E[2] + E[3]                         # D around cell f+1
         if f + 1 < n:
-            dm[f + 1] = C_right + T2 - (.4 * A * T1 + .6 * Cc * T2) / (.1 * A + B + .3 * Cc)
+            dm[f + 1] = 3 * s_right - (c - b) - (2 / 3 * U + V) / (A / 3 + 2 * T13 + Cc)
         if f >= 0:
-            dp[f] = C_left - T1 + (.4 * Cc * T2 + .6 * A * T1) / (.1 * Cc + B + .3 * A)
+            dp[f] = 3 * s_left - (c - b) + (U + 2 / 3 * V) / (A + 2 * T13 + Cc / 3)
     return dm, dp
 
 
@@ -82,5 +92,21 @@ def test_face_form_matches_reference():
             v = [phi[min(max(i + t - 3, 0), n - 1)] for t in range(7)]
             rm, rp = reference_weno(v)
             scale = max(1e-300, max(abs(q) for q in np.diff(v)) if n > 1 else 1.0)
-            assert abs(dm[i] / 12 - rm) <= 1e-12 * scale, (trial, i)
-            assert abs(dp[i] / 12 - rp) <= 1e-12 * scale, (trial, i)
+            assert abs(dm[i] / 6 - rm) <= 1e-12 * scale, (trial, i)
+            assert abs(dp[i] / 6 - rp) <= 1e-12 * scale, (trial, i)
+
+
+def test_significand_equals_the_exact_scaling():
+    """ε·2^-e, formed on the device by setting ε's exponent field to the bias, equals the
+    product with the power-of-two scale bit for bit (both in FP64 and FP32)."""
+    rng = np.random.default_rng(3)
+    x = np.concatenate([4e-99 + rng.uniform(0, 1, 500) * 10.0 ** rng.uniform(-90, 10, 500), [4e-99, 1.0, 1.5, 2.0 ** 60]])
+    bits = x.view(np.uint64)
+    sig = ((bits & np.uint64(0x000FFFFFFFFFFFFF)) | np.uint64(0x3FF0000000000000)).view(np.float64)
+    scale = ((np.uint64(2046) << np.uint64(52)) - (bits & np.uint64(0x7FF0000000000000))).view(np.float64)
+    assert np.array_equal(sig, x * scale) and np.all((sig >= 1) & (sig < 2))
+    xf = (4e-30 + rng.uniform(0, 1, 500) * 10.0 ** rng.uniform(-28, 10, 500)).astype(np.float32)
+    fb = xf.view(np.uint32)
+    sigf = ((fb & np.uint32(0x007FFFFF)) | np.uint32(0x3F800000)).view(np.float32)
+    scalef = ((np.uint32(254) << np.uint32(23)) - (fb & np.uint32(0x7F800000))).view(np.float32)
+    assert np.array_equal(sigf, xf * scalef)
