@@ -265,6 +265,23 @@ __device__ __forceinline__ double rsqrtNR(double x) {
 	const double e = fma(-(x * y), y, 1.0);
 	return fma(y, e * fma(e, 0.375, 0.5), y);
 }
+// sqrt(x) over the same range from the same seed y ≈ 1/sqrt(x): the step runs on
+// s = x·y, s ← s(1 + e/2 + 3e²/8) with e = 1 − s·y, so the product with x is not a
+// separate instruction; the rounding of x·y enters e and is halved by the step.
+__device__ __forceinline__ double sqrtNR(double x) {
+	const int hi = __double2hiint(x), lo = __double2loint(x);
+	const int ex = ((hi >> 20) & 0x7ff) - 1023;
+	const unsigned man = (unsigned(hi & 0xfffff) << 3) | (unsigned(lo) >> 29);
+	const float xf = __int_as_float(((ex + 127) << 23) | int(man));
+	float yf;
+	asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(xf));
+	const int yb = __float_as_int(yf);
+	const int ey = ((yb >> 23) & 0xff) - 127;
+	const double y = __hiloint2double(((ey + 1023) << 20) | ((yb & 0x7fffff) >> 3), (yb & 7) << 29);
+	const double sq = x * y;
+	const double e = fma(-sq, y, 1.0);
+	return fma(sq, e * fma(e, 0.375, 0.5), sq);
+}
 // φ < 0 without an FP64 comparison (-0 counts as not negative, as in the comparison).
 __device__ __forceinline__ bool isNegative(double x) {
 	const long long b = __double_as_longlong(x);
@@ -286,28 +303,30 @@ template <typename T> struct WenoConst {
 template <typename T> struct Ratio { T num, den; };
 
 // Scaled squared weights of a face set: with q_k = (s_k+ε)·2^-e (2^e ≤ ε < 2^(e+1),
-// an exact scale) every q_k lies in [1, ~7e7], so products of two q_k^2 neither overflow nor
-// underflow in FP32 or FP64; α_k = d_k/(s_k+ε)^2 then normalises to the same
-// weights as w_1 = .1 q_2^2 q_3^2, w_2 = .6 q_1^2 q_3^2, w_3 = .3 q_1^2 q_2^2.
-template <typename T> struct FaceWeights { T a, b, c; };  // a = t2 t3, b = .6 t1 t3, c = t1 t2
+// an exact scale, so q_k = s_k·2^-e + ε's significand in one rounding) every q_k lies in
+// [1, ~7e7], so products of two q_k^2 neither overflow nor underflow in FP32 or FP64;
+// α_k = d_k/(s_k+ε)^2 then normalises to the same weights as w_1 = q_2^2 q_3^2,
+// w_2 = 6 q_1^2 q_3^2, w_3 = 3 q_1^2 q_2^2 (ten times d_k = .1, .6, .3: each ratio's
+// numerator and denominator carry the same factor, and the first weight needs no product).
+template <typename T> struct FaceWeights { T a, b, c; };  // a = t2 t3, b = 6 t1 t3, c = t1 t2
 template <typename T>
 __device__ __forceinline__ FaceWeights<T> faceWeights(T s1, T s2, T s3, T eps) {
-	const T sc = pow2NegExp(eps);
-	const T q1 = (s1 + eps) * sc, q2 = (s2 + eps) * sc, q3 = (s3 + eps) * sc;
+	const T sc = pow2NegExp(eps), es = significandOf(eps);
+	const T q1 = fma(s1, sc, es), q2 = fma(s2, sc, es), q3 = fma(s3, sc, es);
 	const T t1 = q1 * q1, t2 = q2 * q2, t3 = q3 * q3;
-	return {t2 * t3, T(0.6) * (t1 * t3), t1 * t2};
+	return {t2 * t3, T(6) * (t1 * t3), t1 * t2};
 }
-// φ⁻ of the cell right of the face: stencils on (E1..E5) with weights (.1a, b, .3c).
+// φ⁻ of the cell right of the face: stencils on (E1..E5) with weights (a, b, 3c).
 template <typename T>
 __device__ __forceinline__ Ratio<T> rightRole(const FaceWeights<T> &w, T P1, T P2, T P3) {
-	const T w1 = T(0.1) * w.a, w3 = T(0.3) * w.c;
-	return {fma(w1, P1, fma(w.b, P2, w3 * P3)), w1 + w.b + w3};
+	const T w3 = T(3) * w.c;
+	return {fma(w.a, P1, fma(w.b, P2, w3 * P3)), w.a + w.b + w3};
 }
-// φ⁺ of the cell left of the face: stencils on (E5..E1) with weights (.1c, b, .3a).
+// φ⁺ of the cell left of the face: stencils on (E5..E1) with weights (c, b, 3a).
 template <typename T>
 __device__ __forceinline__ Ratio<T> leftRole(const FaceWeights<T> &w, T R1, T R2, T R3) {
-	const T w1 = T(0.1) * w.c, w3 = T(0.3) * w.a;
-	return {fma(w1, R1, fma(w.b, R2, w3 * R3)), w1 + w.b + w3};
+	const T w3 = T(3) * w.a;
+	return {fma(w.c, R1, fma(w.b, R2, w3 * R3)), w.c + w.b + w3};
 }
 // Smoothness indicators of (v1, v2, v3) in the three positions of a face set
 // (Derivatives.h:147-149): g = 13/12 (v1-2v2+v3)^2 is common to all three.
@@ -359,7 +378,7 @@ template <typename T, int Mode>
 __device__ __forceinline__ T rkUpdate(T f, T rawSum, T k, T dx, T dt, const T *base, int64_t id) {
 	T grad, sgn;
 	if constexpr (sizeof(T) == 8) {
-		grad = (rsqrtRange(rawSum) ? rawSum * rsqrtNR(rawSum) : sqrt(rawSum)) * k;
+		grad = (rsqrtRange(rawSum) ? sqrtNR(rawSum) : sqrt(rawSum)) * k;
 		const T sp = dx * grad;
 		const T q = fma(f, f, sp * sp);
 		sgn = f * (rsqrtRange(q) ? rsqrtNR(q) : rsqrt(q));
@@ -408,18 +427,18 @@ __device__ __forceinline__ F2 stencil2_2(F2 a, F2 b, F2 c) { return fma2(a, f2(-
 __device__ __forceinline__ F2 stencil3_2(F2 a, F2 b, F2 c) { return fma2(c, f2(-1.f), fma2(b, f2(5.f), mul2(a, f2(2.f)))); }
 struct FaceWeights2 { F2 a, b, c; };
 __device__ __forceinline__ FaceWeights2 faceWeights2(F2 s1, F2 s2, F2 s3, F2 eps) {
-	const F2 sc = pow2NegExp2(eps);
-	const F2 q1 = mul2(add2(s1, eps), sc), q2 = mul2(add2(s2, eps), sc), q3 = mul2(add2(s3, eps), sc);
+	const F2 sc = pow2NegExp2(eps), es = f2(significandOf(eps.v.x), significandOf(eps.v.y));
+	const F2 q1 = fma2(s1, sc, es), q2 = fma2(s2, sc, es), q3 = fma2(s3, sc, es);
 	const F2 t1 = mul2(q1, q1), t2 = mul2(q2, q2), t3 = mul2(q3, q3);
-	return {mul2(t2, t3), mul2(f2(0.6f), mul2(t1, t3)), mul2(t1, t2)};
+	return {mul2(t2, t3), mul2(f2(6.f), mul2(t1, t3)), mul2(t1, t2)};
 }
 __device__ __forceinline__ Ratio2 rightRole2(const FaceWeights2 &w, F2 P1, F2 P2, F2 P3) {
-	const F2 w1 = mul2(f2(0.1f), w.a), w3 = mul2(f2(0.3f), w.c);
-	return {fma2(w1, P1, fma2(w.b, P2, mul2(w3, P3))), add2(add2(w1, w.b), w3)};
+	const F2 w3 = mul2(f2(3.f), w.c);
+	return {fma2(w.a, P1, fma2(w.b, P2, mul2(w3, P3))), add2(add2(w.a, w.b), w3)};
 }
 __device__ __forceinline__ Ratio2 leftRole2(const FaceWeights2 &w, F2 R1, F2 R2, F2 R3) {
-	const F2 w1 = mul2(f2(0.1f), w.c), w3 = mul2(f2(0.3f), w.a);
-	return {fma2(w1, R1, fma2(w.b, R2, mul2(w3, R3))), add2(add2(w1, w.b), w3)};
+	const F2 w3 = mul2(f2(3.f), w.a);
+	return {fma2(w.c, R1, fma2(w.b, R2, mul2(w3, R3))), add2(add2(w.c, w.b), w3)};
 }
 __device__ __forceinline__ void wenoCell2(const F2 v[7], Ratio2 &m, Ratio2 &p) {
 	const F2 D1 = sub2(v[1], v[0]), D2 = sub2(v[2], v[1]), D3 = sub2(v[3], v[2]), D4 = sub2(v[4], v[3]), D5 = sub2(v[5], v[4]), D6 = sub2(v[6], v[5]);
@@ -717,7 +736,7 @@ __global__ void __launch_bounds__(kPairBlockMax) kReinitPairs(G<3, float> g, con
 			const FaceWeights<float> wm = faceWeights(smoothL(smoothG(D2, D3, D4), D2, D3, D4), smoothM(smoothG(D3, D4, D5), D3, D5),
 			                                          smoothR(smoothG(D4, D5, D6), D4, D5, D6),
 			                                          fma(M, WenoConst<float>::epsScale, WenoConst<float>::floorEps4));
-			const F2 W1 = mul2(f2(0.1f), f2(wm.c, wm.a)), Wb = f2(wm.b), W3 = mul2(f2(0.3f), f2(wm.a, wm.c));
+			const F2 W1 = f2(wm.c, wm.a), Wb = f2(wm.b), W3 = mul2(f2(3.f), f2(wm.a, wm.c));
 			const F2 S1m = stencil1_2(f2(D6, D2), f2(D5, D3), f2(D4, D4));
 			const F2 S2m = stencil2_2(f2(D5, D3), f2(D4, D4), f2(D3, D5));
 			const F2 S3m = stencil3_2(f2(D4, D4), f2(D3, D5), f2(D2, D6));
@@ -994,7 +1013,7 @@ __global__ void __launch_bounds__(kPtX * kPtY, 4) kReinitPairsTiled(const __grid
 			const FaceWeights<float> wm = faceWeights(smoothL(smoothG(D2, D3, D4), D2, D3, D4), smoothM(smoothG(D3, D4, D5), D3, D5),
 			                                          smoothR(smoothG(D4, D5, D6), D4, D5, D6),
 			                                          fma(M, WenoConst<float>::epsScale, WenoConst<float>::floorEps4));
-			const F2 W1 = mul2(f2(0.1f), f2(wm.c, wm.a)), Wb = f2(wm.b), W3 = mul2(f2(0.3f), f2(wm.a, wm.c));
+			const F2 W1 = f2(wm.c, wm.a), Wb = f2(wm.b), W3 = mul2(f2(3.f), f2(wm.a, wm.c));
 			const F2 S1m = stencil1_2(f2(D6, D2), f2(D5, D3), f2(D4, D4));
 			const F2 S2m = stencil2_2(f2(D5, D3), f2(D4, D4), f2(D3, D5));
 			const F2 S3m = stencil3_2(f2(D4, D4), f2(D3, D5), f2(D2, D6));

@@ -101,3 +101,27 @@ def test_inverse_sqrt_within_two_ulp():
             rel = abs(Fraction(r) ** 2 * Fraction(x) - 1) / 2
             worst = max(worst, float(rel))
     assert worst <= 2.0 ** -52, worst
+
+
+def sqrt_refine(x: float, y: float) -> float:
+    """s(1 + e/2 + 3e^2/8) with s = x*y rounded and e = 1 - s*y: the FP64 update's square
+    root, refined on s = x·y rather than on y, with the device's fused operations."""
+    sq = float(Fraction(x) * Fraction(y))
+    e = fma(-sq, y, 1.0)
+    t = e * fma(e, 0.375, 0.5)
+    return fma(sq, t, sq)
+
+
+def test_square_root_within_two_ulp():
+    """The WENO5 update's |∇φ| (FP64 form) from the FP32 inverse-square-root seed, over the
+    same range [2^-120, 2^120], against exact arithmetic."""
+    rng = random.Random(11)
+    worst = 0.0
+    for _ in range(3000):
+        x = 2.0 ** rng.uniform(-120.0, 120.0)
+        for ulps in (-2, 0, 2):
+            r = sqrt_refine(x, rsqrt_seed(x, ulps))
+            # |r^2/x - 1| ~ 2 * relative error of r
+            rel = abs(Fraction(r) ** 2 / Fraction(x) - 1) / 2
+            worst = max(worst, float(rel))
+    assert worst <= 2.0 ** -52, worst
