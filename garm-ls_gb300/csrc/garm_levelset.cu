@@ -252,7 +252,9 @@ __device__ __forceinline__ bool rsqrtRange(double x) {
 	const int ex = ((__double2hiint(x) >> 20) & 0x7ff) - 1023;
 	return ex >= -120 && ex <= 120;  // also false for 0, subnormals, inf and NaN
 }
-__device__ __forceinline__ double rsqrtNR(double x) {
+// The FP32 hardware approximation of 1/sqrt(x) for x in the range above (x's mantissa
+// truncated to float), returned as a double.
+__device__ __forceinline__ double rsqrtSeed(double x) {
 	const int hi = __double2hiint(x), lo = __double2loint(x);
 	const int ex = ((hi >> 20) & 0x7ff) - 1023;
 	const unsigned man = (unsigned(hi & 0xfffff) << 3) | (unsigned(lo) >> 29);
@@ -261,7 +263,10 @@ __device__ __forceinline__ double rsqrtNR(double x) {
 	asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(xf));
 	const int yb = __float_as_int(yf);
 	const int ey = ((yb >> 23) & 0xff) - 127;
-	const double y = __hiloint2double(((ey + 1023) << 20) | ((yb & 0x7fffff) >> 3), (yb & 7) << 29);
+	return __hiloint2double(((ey + 1023) << 20) | ((yb & 0x7fffff) >> 3), (yb & 7) << 29);
+}
+__device__ __forceinline__ double rsqrtNR(double x) {
+	const double y = rsqrtSeed(x);
 	const double e = fma(-(x * y), y, 1.0);
 	return fma(y, e * fma(e, 0.375, 0.5), y);
 }
@@ -269,15 +274,7 @@ __device__ __forceinline__ double rsqrtNR(double x) {
 // s = x·y, s ← s(1 + e/2 + 3e²/8) with e = 1 − s·y, so the product with x is not a
 // separate instruction; the rounding of x·y enters e and is halved by the step.
 __device__ __forceinline__ double sqrtNR(double x) {
-	const int hi = __double2hiint(x), lo = __double2loint(x);
-	const int ex = ((hi >> 20) & 0x7ff) - 1023;
-	const unsigned man = (unsigned(hi & 0xfffff) << 3) | (unsigned(lo) >> 29);
-	const float xf = __int_as_float(((ex + 127) << 23) | int(man));
-	float yf;
-	asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(xf));
-	const int yb = __float_as_int(yf);
-	const int ey = ((yb >> 23) & 0xff) - 127;
-	const double y = __hiloint2double(((ey + 1023) << 20) | ((yb & 0x7fffff) >> 3), (yb & 7) << 29);
+	const double y = rsqrtSeed(x);
 	const double sq = x * y;
 	const double e = fma(-sq, y, 1.0);
 	return fma(sq, e * fma(e, 0.375, 0.5), sq);
@@ -1185,7 +1182,8 @@ __global__ void __launch_bounds__(256) kWenoSweep(G<D, T> g, const T *__restrict
 	const int f0 = w0 - 1;
 	const T p0 = ld(f0 - 2), p1 = ld(f0 - 1);
 	T phiF = ld(f0), phiF1 = ld(f0 + 1), phiF2 = ld(f0 + 2);
-	T E1 = p1 - p0, E2 = phiF - p1, E3 = phiF1 - phiF, E4 = phiF2 - phiF1;   // D_{f-1} .. D_{f+2}
+	const T E1 = p1 - p0, E2 = phiF - p1;                                    // D_{f-1}, D_f
+	T E3 = phiF1 - phiF, E4 = phiF2 - phiF1;                                  // D_{f+1}, D_{f+2}
 	T Q1 = E1 * E1, Q2 = E2 * E2, Q3 = E3 * E3, Q4 = E4 * E4;
 	T a = E2 - E1, b = E3 - E2, c = E4 - E3;                                // Δ_f .. Δ_{f+2}
 	T gab = g13(a, b), gbc = g13(b, c);
@@ -1224,7 +1222,7 @@ __global__ void __launch_bounds__(256) kWenoSweep(G<D, T> g, const T *__restrict
 			else out[id] = rkUpdate<T, Mode>(phiF, fma(x, x, fma(y, y, out[id])), k, g.dx, dt, base, id);
 		}
 		dmCarry = dmNext; dpBase = fma(T(3), s, -e3);                           // 6 C(f+1) - T2 / 2
-		E1 = E2; E2 = E3; E3 = E4; E4 = E5;
+		E3 = E4; E4 = E5;
 		Q1 = Q2; Q2 = Q3; Q3 = Q4; Q4 = Q5;
 		a = b; b = c; c = d;
 		gab = gbc; gbc = gcd;
