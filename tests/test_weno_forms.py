@@ -17,6 +17,11 @@ the bases 6C ± T/2 are 3s - (c-b) and 3s - (d-c); each ratio is halved and scal
 over 1/3 t2t3 + 2 t1t3 + t1t2 and t2t3 + 2 t1t3 + 1/3 t1t2); T2 is the difference of
 the third differences c-b and d-c, and ε'·2^-e is ε''s significand.  face_form
 follows that arrangement.
+
+Cell form (the cell, column and pair kernels): each one-sided derivative from its own
+face set, with the candidate stencils times six and the weights ten times the
+reference's (q2²q3², 6 q1²q3², 3 q1²q2²), so that the first needs no product;
+cell_form follows it.
 """
 from __future__ import annotations
 
@@ -110,3 +115,52 @@ def test_significand_equals_the_exact_scaling():
     sigf = ((fb & np.uint32(0x007FFFFF)) | np.uint32(0x3F800000)).view(np.float32)
     scalef = ((np.uint32(254) << np.uint32(23)) - (fb & np.uint32(0x7F800000))).view(np.float32)
     assert np.array_equal(sigf, xf * scalef)
+
+
+def cell_form(v):
+    """(6 φ⁻, 6 φ⁺) of one cell from its seven values in the cell, column and pair forms'
+    arrangement (wenoCell): one face set per derivative, weights ten times the reference's
+    (q2²q3², 6 q1²q3², 3 q1²q2²: the first without a product), candidate stencils six times."""
+    D = [v[k + 1] - v[k] for k in range(6)]
+
+    def weights(s1, s2, s3, eps):
+        m, ex = np.frexp(eps)
+        sc, es = 2.0 ** (1 - ex), 2.0 * m
+        t1, t2, t3 = (s1 * sc + es) ** 2, (s2 * sc + es) ** 2, (s3 * sc + es) ** 2
+        return t2 * t3, 6 * (t1 * t3), t1 * t2
+
+    g = lambda a, b, c: 13 / 3 * (a - 2 * b + c) ** 2
+    sL = lambda a, b, c: g(a, b, c) + (a - 4 * b + 3 * c) ** 2
+    sM = lambda a, b, c: g(a, b, c) + (a - c) ** 2
+    sR = lambda a, b, c: g(a, b, c) + (3 * a - 4 * b + c) ** 2
+    st1 = lambda a, b, c: 2 * a - 7 * b + 11 * c
+    st2 = lambda a, b, c: -a + 5 * b + 2 * c
+    st3 = lambda a, b, c: 2 * a + 5 * b - c
+    M = max(d * d for d in D[1:5])
+    epsM, epsP = max(M, D[0] ** 2) * 4e-6 + 4e-99, max(M, D[5] ** 2) * 4e-6 + 4e-99
+    a, b, c = weights(sL(*D[0:3]), sM(*D[1:4]), sR(*D[2:5]), epsM)
+    P2, P3 = st2(*D[1:4]), st3(*D[2:5])
+    m = (a * st1(*D[0:3]) + b * P2 + 3 * c * P3) / (a + b + 3 * c)
+    a, b, c = weights(sL(*D[1:4]), sM(*D[2:5]), sR(*D[3:6]), epsP)
+    p = (c * st1(D[5], D[4], D[3]) + b * P3 + 3 * a * P2) / (c + b + 3 * a)
+    return m, p
+
+
+def test_cell_form_matches_reference():
+    rng = np.random.default_rng(1)
+    for trial in range(400):
+        kind = trial % 4
+        x = np.arange(7) * 0.1
+        if kind == 0:
+            v = rng.normal(size=7)
+        elif kind == 1:
+            v = np.abs(x - rng.uniform(0, 0.7)) - 0.3          # kink
+        elif kind == 2:
+            v = np.full(7, rng.normal())                       # flat: ε floor only
+        else:
+            v = np.cumsum(rng.normal(size=7)) * 1e-3
+        m, p = cell_form(list(v))
+        rm, rp = reference_weno(list(v))
+        scale = max(1e-300, max(abs(q) for q in np.diff(v)))
+        assert abs(m / 6 - rm) <= 1e-12 * scale, trial
+        assert abs(p / 6 - rp) <= 1e-12 * scale, trial
