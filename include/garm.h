@@ -224,9 +224,10 @@ garm_status garm_sim_graph_active(const garm_sim *sim, int *active);
 garm_status garm_sim_reinit_plan(garm_sim *sim, int *form, int *threads, int *cells_per_thread, float *ms);
 /* Pin the reinitialisation plan of one grid shape (cell counts per axis, storage
  * layout) and precision on the current device, replacing the autotuner's choice.
- * For the column and sweep forms threads is 32..256 (a multiple of 32) and
- * cells_per_thread >= 1; the cell form ignores both.  threads 0 forgets the
- * pinned or tuned plan, so the next use tunes again. */
+ * For every form but the cell form threads is 32..256 (a multiple of 32) and
+ * cells_per_thread >= 1 (the cells, or planes, each thread walks); the cell form
+ * ignores both, and the two tiled forms always run 128 threads per block.  threads 0
+ * forgets the pinned or tuned plan, so the next use tunes again. */
 garm_status garm_reinit_plan_set(int dim, int precision, const int *size, int form, int threads, int cells_per_thread);
 
 /* calculateVolume (Source/Core/LevelSetLiquid.cpp:1162-1190): volume (2D: area) of the
