@@ -242,6 +242,19 @@ def profiled_fp64_ops(plan: dict):
     return None
 
 
+def profiled_fp64_inst(plan: dict):
+    """FP64 instructions per storage cell and sub-stage (DFMA + DADD + DMUL executed, each
+    one issue slot of the FP64 pipe) from the same ncu summary as profiled_fp64_ops."""
+    name = PROFILED_PLANS.get((plan["form"], "fp64"))
+    p = REPO / "profiles" / name if name else None
+    if p is None or not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        if ln.startswith("fp64_inst_per_cell_substage:"):
+            return float(ln.split(":")[1])
+    return None
+
+
 def reinit_roofline(sim, torch, stream, n_cells: int, esz: int, iters: int, peaks: dict) -> dict:
     """Time the WENO5 reinitialisation stage alone with CUDA events on the sim's stream
     and express its algorithmic bytes per launch against the measured HBM peak.  In the
@@ -280,6 +293,12 @@ def reinit_roofline(sim, torch, stream, n_cells: int, esz: int, iters: int, peak
                     "peak_source": "measured: garm_fp64_peak_selftest (FP64 FMA chains, CUDA events) on this device",
                     "unit": "TFLOP/s", "frac": round(tflops / fp64_peak, 4),
                     "fp64_ops_per_launch": int(ops * n_cells), "fp64_ops_per_cell": ops, "hbm": hbm})
+        inst = profiled_fp64_inst(plan)
+        if inst:
+            # the same peak as FP64 instructions: an FMA chain issues one DFMA per 2 operations
+            rate = inst * n_cells / (ms_per_launch * 1e-3) / 1e12
+            out["fp64_issue"] = {"inst_per_cell": inst, "achieved": round(rate, 4), "peak": round(fp64_peak / 2, 4),
+                                 "unit": "T inst/s", "frac": round(rate / (fp64_peak / 2), 4)}
     return out
 
 

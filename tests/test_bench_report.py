@@ -65,3 +65,5 @@ def test_profiles_named_by_the_bench_parse():
         assert traffic is not None and traffic > 0, (form, precision)
     ops = bench.profiled_fp64_ops({"form": "sweeps"})
     assert ops is not None and 100 < ops < 1000
+    inst = bench.profiled_fp64_inst({"form": "sweeps"})
+    assert inst is not None and ops / 2 < inst < ops  # an FMA is one instruction, two operations
