@@ -50,28 +50,32 @@ def _stale(target: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build_library(force: bool = False, verbose: bool = False) -> Path:
+def build_library(force: bool = False, verbose: bool = False, extra_flags: tuple[str, ...] = (), tag: str = "") -> Path:
+    """libgarm.so, or with a tag a variant built with extra nvcc flags into _build_<tag>/ and
+    libgarm_<tag>.so beside it (diagnostic builds; the library the package loads is untagged)."""
     nvcc = _nvcc()
-    BUILD_DIR.mkdir(exist_ok=True)
+    build_dir = BUILD_DIR.with_name(f"_build_{tag}") if tag else BUILD_DIR
+    lib_path = LIB_PATH.with_name(f"libgarm_{tag}.so") if tag else LIB_PATH
+    build_dir.mkdir(exist_ok=True)
     sources = sorted(CSRC.glob("*.cu"))
     headers = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [REPO / "include" / "garm.h"]
     objs = []
     jobs = []
     for src in sources:
-        obj = BUILD_DIR / (src.stem + ".o")
+        obj = build_dir / (src.stem + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, "-I", str(REPO / "include"), "-c", str(src), "-o", str(obj)])
+            jobs.append([nvcc, *ARCH, *NVCC_FLAGS, *extra_flags, "-I", str(REPO / "include"), "-c", str(src), "-o", str(obj)])
     if jobs:
         workers = min(len(jobs), max(1, os.cpu_count() or 1))
         with cf.ThreadPoolExecutor(max_workers=workers) as ex:
             for _ in ex.map(_run, jobs):
                 pass
-    if force or jobs or _stale(LIB_PATH, objs):
-        _run([nvcc, *ARCH, "-shared", "-o", str(LIB_PATH), *map(str, objs), "-lcudart"])
+    if force or jobs or _stale(lib_path, objs):
+        _run([nvcc, *ARCH, "-shared", "-o", str(lib_path), *map(str, objs), "-lcudart"])
     if verbose:
-        print(f"built {LIB_PATH}", file=sys.stderr)
-    return LIB_PATH
+        print(f"built {lib_path}", file=sys.stderr)
+    return lib_path
 
 
 DEMO_SRC = PKG_DIR / "host" / "garm_demo.cpp"
